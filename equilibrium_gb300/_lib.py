@@ -1,0 +1,112 @@
+"""ctypes binding of the C ABI in ``include/eqfluid.h`` (``libeqfluid.so``).
+
+Loading fails loudly when the library is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "libeqfluid.so")
+HEADER = os.path.join(ROOT, "include", "eqfluid.h")
+
+EQ_OK, EQ_ERR_ARG, EQ_ERR_CUDA, EQ_ERR_TIMEOUT, EQ_ERR_OOM, EQ_ERR_STATE = range(6)
+FIELD_SCRATCH, FIELD_DENSITY, FIELD_VX, FIELD_VY, FIELD_VX0, FIELD_VY0 = range(6)
+MODE_ADJUST_ROW, MODE_ADJUST_COLUMN, MODE_PASSIVE = range(3)
+
+
+class EqError(RuntimeError):
+    """A non-zero status from the C ABI (the reference panics in these places)."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[eqfluid status {code}] {msg}")
+        self.code = code
+
+
+class SimulationConfigsC(ctypes.Structure):
+    _fields_ = [("delta_t", ctypes.c_float), ("frames", ctypes.c_int64),
+                ("size", ctypes.c_uint32)]
+
+
+class FluidConfigsC(ctypes.Structure):
+    _fields_ = [("diffusion", ctypes.c_float), ("viscousity", ctypes.c_float),
+                ("has_perlin_noise", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def header_functions() -> list[str]:
+    """Every function the public header declares."""
+    with open(HEADER) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(eq_[a-z0-9_]+)\s*\(", text)))
+
+
+def load(path: str = LIB_PATH):
+    """Load the library and declare signatures. Raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
+            " (the CUDA library is required; there is no CPU fallback)")
+    L = ctypes.CDLL(path)
+    P, H = ctypes.c_void_p, ctypes.c_void_p
+    i32, i64, u32, u64, f32 = (ctypes.c_int, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint64,
+                               ctypes.c_float)
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    sigs = {
+        "eq_abi_version": (i32, []),
+        "eq_last_error": (ctypes.c_char_p, []),
+        "eq_fluid_new": (i32, [ctypes.POINTER(FluidConfigsC), ctypes.POINTER(SimulationConfigsC),
+                               i32, PP]),
+        "eq_fluid_default": (i32, [i32, PP]),
+        "eq_fluid_init": (i32, [H]),
+        "eq_fluid_clone": (i32, [H, PP]),
+        "eq_fluid_free": (i32, [H]),
+        "eq_fluid_get_configs": (i32, [H, ctypes.POINTER(FluidConfigsC),
+                                       ctypes.POINTER(SimulationConfigsC)]),
+        "eq_fluid_set_configs": (i32, [H, ctypes.POINTER(FluidConfigsC),
+                                       ctypes.POINTER(SimulationConfigsC)]),
+        "eq_fluid_step": (i32, [H]),
+        "eq_fluid_step_n": (i32, [H, i64]),
+        "eq_fluid_synchronize": (i32, [H]),
+        "eq_fluid_add_density": (i32, [H, u32, u32, f32]),
+        "eq_fluid_add_velocity": (i32, [H, u32, u32, f32, f32]),
+        "eq_fluid_add_sources": (i32, [H, i64, P, P, P, P, P]),
+        "eq_fluid_run_device_sources": (i32, [H, i64, i64, P, P, P, P, P]),
+        "eq_rectangle_check": (i32, [i64, i64, i64, i64, u32]),
+        "eq_fluid_fill_obstacle": (i32, [H, i64, i64, i64, i64]),
+        "eq_fluid_read_field": (i32, [H, i32, P, u64]),
+        "eq_fluid_write_field": (i32, [H, i32, P, u64]),
+        "eq_fluid_read_field_async": (i32, [H, i32, P, u64]),
+        "eq_fluid_write_field_async": (i32, [H, i32, P, u64]),
+        "eq_fluid_read_cells": (i32, [H, P, u64]),
+        "eq_fluid_write_cells": (i32, [H, P, u64]),
+        "eq_fluid_set_boundaries": (i32, [H, i32, i32]),
+        "eq_fluid_lin_solve": (i32, [H, i32, i32, i32, f32, f32]),
+        "eq_fluid_diffuse": (i32, [H, i32, i32, i32, f32]),
+        "eq_fluid_project": (i32, [H, i32, i32, i32, i32]),
+        "eq_fluid_advect": (i32, [H, i32, i32, i32, i32, i32]),
+        "eq_fluid_device_field": (i32, [H, i32, PP, ctypes.POINTER(ctypes.c_uint32)]),
+        "eq_fluid_launch_count": (i32, [H, ctypes.POINTER(ctypes.c_uint64)]),
+        "eq_fluid_set_spin_limit": (i32, [H, i64]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc: int):
+    if rc != EQ_OK:
+        msg = load().eq_last_error()
+        raise EqError(rc, msg.decode() if msg else "")

@@ -1,0 +1,797 @@
+// C ABI (include/eqfluid.h) and host orchestration of the sm_103a frame step.
+//
+// One handle = one scene: the six pitched f32 grids of Fluid (fluid.rs:59-77),
+// a spare grid for lin_solve's double buffering, the wall mask with its
+// derived per-cell boundary codes, and the lin_solve wavefront's sync state.
+// Every launch goes to the handle's own stream; nothing here falls back to
+// the CPU -- if a CUDA call fails the entry point reports EQ_ERR_CUDA.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/eqfluid.h"
+#include "common.cuh"
+#include "kernels.cuh"
+#include "linsolve.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define EQ_CUDA(call)                                                                   \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return fail(EQ_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));     \
+  } while (0)
+
+constexpr int kMaxSweepsPerLaunch = 64;
+constexpr long long kDefaultSpinLimit = 1ll << 22;
+
+}  // namespace
+
+struct eq_fluid {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint32_t S = 0;
+  int P = 0;  // row pitch (elements)
+  float dt = 0.f, diff = 0.f, visc = 0.f;
+  int64_t frames = 0;
+  int32_t has_perlin_noise = 0;
+
+  float* block = nullptr;  // 7 grids
+  float* field[6] = {};
+  float* spare = nullptr;
+  uint8_t* cells = nullptr;  // pitched mask, 1 = wall
+  uint8_t* code = nullptr;   // pitched boundary codes
+  uint8_t* rowfl = nullptr;  // [S] row has a fluid cell
+  uint8_t* colfl = nullptr;  // [S] column has a fluid cell
+  std::vector<uint8_t> host_cells;  // authoritative mirror of cells_type
+  bool mask_dirty = true;
+
+  // lin_solve wavefront state
+  int B = 0;  // strips for kMaxSweepsPerLaunch
+  float* edge = nullptr;
+  unsigned long long* progress = nullptr;
+  unsigned* counters = nullptr;  // [0] ticket, [1] done
+  int* err = nullptr;
+  long long spin_limit = kDefaultSpinLimit;
+
+  // source staging
+  uint8_t* d_src = nullptr;
+  size_t d_src_cap = 0;
+  uint8_t* h_src = nullptr;  // pinned
+  size_t h_src_cap = 0;
+  cudaEvent_t src_ev = nullptr;
+
+  uint64_t launches = 0;
+
+  size_t grid_elems() const { return (size_t)P * S; }
+};
+
+namespace {
+
+int strips_for(int S, int K) { return (S + 2 * K + 31) / 32; }
+
+int select_device(const eq_fluid* h) {
+  EQ_CUDA(cudaSetDevice(h->device));
+  return EQ_OK;
+}
+
+int check_field(int f) { return (f >= 0 && f < 6) ? EQ_OK : fail(EQ_ERR_ARG, "field index out of range"); }
+
+int check_mode(int m) {
+  return (m >= 0 && m <= 2) ? EQ_OK : fail(EQ_ERR_ARG, "mode out of range");
+}
+
+// Derives the per-cell boundary codes and the row/column fluid flags from the
+// host mask and uploads mask + codes.
+int upload_mask(eq_fluid* h) {
+  if (!h->mask_dirty) return EQ_OK;
+  const int S = (int)h->S, P = h->P, N = S - 2;
+  const std::vector<uint8_t>& m = h->host_cells;
+  auto wall = [&](int i, int j) { return m[(size_t)j * S + i] != 0; };
+  std::vector<uint8_t> code((size_t)P * S, 0), cellsP((size_t)P * S, 0), rowfl(S, 0),
+      colfl(S, 0);
+  for (int j = 0; j < S; ++j) {
+    for (int i = 0; i < S; ++i) {
+      uint8_t c = 0;
+      const bool w = wall(i, j);
+      cellsP[(size_t)j * P + i] = w ? 1 : 0;
+      if (w) c |= eqk::kCodeWall;
+      if (!w && i >= 1 && i <= N && j >= 1 && j <= N) {
+        rowfl[j] = 1;
+        colfl[i] = 1;
+        if (wall(i + 1, j))
+          c |= eqk::kCodeRowRight;
+        else if (wall(i - 1, j))
+          c |= eqk::kCodeRowLeft;
+        if (wall(i, j - 1))
+          c |= eqk::kCodeColUp;
+        else if (wall(i, j + 1))
+          c |= eqk::kCodeColDown;
+      }
+      // (i, j-1) has kCodeColDown: it is fluid, (i, j-2) is not a wall, (i, j) is.
+      if (j >= 2 && j - 1 <= N && i >= 1 && i <= N && w && !wall(i, j - 1) &&
+          !wall(i, j - 2))
+        c |= eqk::kCodeAboveDown;
+      code[(size_t)j * P + i] |= c;
+    }
+  }
+  EQ_CUDA(cudaMemcpyAsync(h->cells, cellsP.data(), cellsP.size(), cudaMemcpyHostToDevice,
+                          h->stream));
+  EQ_CUDA(cudaMemcpyAsync(h->code, code.data(), code.size(), cudaMemcpyHostToDevice,
+                          h->stream));
+  EQ_CUDA(cudaMemcpyAsync(h->rowfl, rowfl.data(), S, cudaMemcpyHostToDevice, h->stream));
+  EQ_CUDA(cudaMemcpyAsync(h->colfl, colfl.data(), S, cudaMemcpyHostToDevice, h->stream));
+  // The staging vectors are pageable: the async copies above are staged
+  // synchronously, but wait anyway before they go out of scope.
+  EQ_CUDA(cudaStreamSynchronize(h->stream));
+  h->mask_dirty = false;
+  return EQ_OK;
+}
+
+int check_launch(eq_fluid* h) {
+  h->launches++;
+  EQ_CUDA(cudaGetLastError());
+  return EQ_OK;
+}
+
+dim3 grid2d(int nx, int ny, dim3 blk) {
+  return dim3((nx + blk.x - 1) / blk.x, (ny + blk.y - 1) / blk.y);
+}
+
+int launch_bnd(eq_fluid* h, int mode, float* x) {
+  const dim3 blk(32, 8);
+  const dim3 grd = grid2d((int)h->S, (int)h->S, blk);
+  switch (mode) {
+    case eqk::kRow:
+      eqk::k_set_boundaries<eqk::kRow><<<grd, blk, 0, h->stream>>>(x, h->code, h->rowfl, h->colfl, (int)h->S, h->P);
+      break;
+    case eqk::kCol:
+      eqk::k_set_boundaries<eqk::kCol><<<grd, blk, 0, h->stream>>>(x, h->code, h->rowfl, h->colfl, (int)h->S, h->P);
+      break;
+    default:
+      eqk::k_set_boundaries<eqk::kPassive><<<grd, blk, 0, h->stream>>>(x, h->code, h->rowfl, h->colfl, (int)h->S, h->P);
+      break;
+  }
+  return check_launch(h);
+}
+
+// lin_solve (fluid.rs:301-325) on device grids.
+int launch_lin_solve(eq_fluid* h, int mode, float* x, const float* x0, float a, float c) {
+  const int64_t K = h->frames;
+  if (K <= 0) return EQ_OK;
+  const float c_recip = 1.0f / c;  // fluid.rs:311, IEEE f32 division
+  const int S = (int)h->S;
+  for (int64_t done = 0; done < K; done += kMaxSweepsPerLaunch) {
+    const int Kc = (int)std::min<int64_t>(kMaxSweepsPerLaunch, K - done);
+    EQ_CUDA(cudaMemcpyAsync(h->spare, x, h->grid_elems() * sizeof(float),
+                            cudaMemcpyDeviceToDevice, h->stream));
+    eqk::LinSolveArgs A;
+    A.x = x;
+    A.spare = h->spare;
+    A.x0 = x0;
+    A.code = h->code;
+    A.rowfl = h->rowfl;
+    A.colfl = h->colfl;
+    A.edge = h->edge;
+    A.progress = h->progress;
+    A.ticket = h->counters;
+    A.done = h->counters + 1;
+    A.err = h->err;
+    A.spin_limit = h->spin_limit;
+    A.S = S;
+    A.P = h->P;
+    A.K = Kc;
+    A.B = strips_for(S, Kc);
+    A.a = a;
+    A.c_recip = c_recip;
+    const unsigned ntasks = (unsigned)(A.B * Kc);
+    switch (mode) {
+      case eqk::kRow:
+        eqk::k_lin_solve<eqk::kRow><<<ntasks, 32, 0, h->stream>>>(A);
+        break;
+      case eqk::kCol:
+        eqk::k_lin_solve<eqk::kCol><<<ntasks, 32, 0, h->stream>>>(A);
+        break;
+      default:
+        eqk::k_lin_solve<eqk::kPassive><<<ntasks, 32, 0, h->stream>>>(A);
+        break;
+    }
+    int rc = check_launch(h);
+    if (rc) return rc;
+  }
+  return EQ_OK;
+}
+
+// diffuse (fluid.rs:276-298).
+int launch_diffuse(eq_fluid* h, int mode, float* x, const float* x0, float diffusion) {
+  const float sf = (float)(h->S - 2);
+  const float a = ((h->dt * diffusion) * sf) * sf;
+  const float c = 1.0f + 4.0f * a;
+  return launch_lin_solve(h, mode, x, x0, a, c);
+}
+
+// project (fluid.rs:330-375).
+int launch_project(eq_fluid* h, float* vx, float* vy, float* p, float* div) {
+  const int S = (int)h->S, N = S - 2;
+  const dim3 blk(32, 8);
+  const dim3 grd = grid2d(N, N, blk);
+  eqk::k_divergence<<<grd, blk, 0, h->stream>>>(vx, vy, p, div, S, h->P);
+  int rc = check_launch(h);
+  if (rc) return rc;
+  if ((rc = launch_bnd(h, eqk::kPassive, div))) return rc;
+  if ((rc = launch_bnd(h, eqk::kPassive, p))) return rc;
+  if ((rc = launch_lin_solve(h, eqk::kPassive, p, div, 1.0f, 4.0f))) return rc;
+  eqk::k_gradient<<<grd, blk, 0, h->stream>>>(vx, vy, p, S, h->P);
+  if ((rc = check_launch(h))) return rc;
+  if ((rc = launch_bnd(h, eqk::kRow, vx))) return rc;
+  return launch_bnd(h, eqk::kCol, vy);
+}
+
+// advect (fluid.rs:378-432).
+int launch_advect(eq_fluid* h, int mode, float* d, const float* d0, const float* u,
+                  const float* v) {
+  const int S = (int)h->S, N = S - 2;
+  const float dt0 = h->dt * (float)(h->S - 2);
+  const int threads = std::min(256, ((N + 31) / 32) * 32);
+  eqk::k_advect_rows<<<N, threads, 0, h->stream>>>(d, d0, u, v, S, h->P, dt0);
+  int rc = check_launch(h);
+  if (rc) return rc;
+  return launch_bnd(h, mode, d);
+}
+
+int launch_copy(eq_fluid* h, float* dst, const float* src) {
+  const size_t n4 = h->grid_elems() / 4;
+  const int threads = 256;
+  const int blocks = (int)std::min<size_t>((n4 + threads - 1) / threads, 152 * 16);
+  eqk::k_copy<<<blocks, threads, 0, h->stream>>>(dst, src, n4);
+  return check_launch(h);
+}
+
+// step (fluid.rs:437-524), with the reference's aliasing of the six arrays.
+int launch_step(eq_fluid* h) {
+  int rc = upload_mask(h);
+  if (rc) return rc;
+  float* sc = h->field[EQ_FIELD_SCRATCH];
+  float* de = h->field[EQ_FIELD_DENSITY];
+  float* vx = h->field[EQ_FIELD_VX];
+  float* vy = h->field[EQ_FIELD_VY];
+  float* vx0 = h->field[EQ_FIELD_VX0];
+  float* vy0 = h->field[EQ_FIELD_VY0];
+  if ((rc = launch_diffuse(h, eqk::kRow, vx0, vx, h->visc))) return rc;
+  if ((rc = launch_diffuse(h, eqk::kCol, vy0, vy, h->visc))) return rc;
+  if ((rc = launch_project(h, vx0, vy0, vx, vy))) return rc;
+  if ((rc = launch_advect(h, eqk::kRow, vx, vx0, vx0, vy0))) return rc;
+  if ((rc = launch_advect(h, eqk::kCol, vy, vy0, vx0, vy0))) return rc;
+  if ((rc = launch_project(h, vx, vy, vx0, vy0))) return rc;
+  if ((rc = launch_diffuse(h, eqk::kPassive, sc, de, h->diff))) return rc;
+  if ((rc = launch_advect(h, eqk::kPassive, de, sc, vx, vy))) return rc;
+  return launch_copy(h, sc, de);
+}
+
+int ensure_src_capacity(eq_fluid* h, size_t bytes) {
+  if (bytes <= h->d_src_cap && bytes <= h->h_src_cap) return EQ_OK;
+  size_t cap = std::max<size_t>(bytes, 4096);
+  if (h->src_ev) EQ_CUDA(cudaEventSynchronize(h->src_ev));
+  if (h->d_src) cudaFree(h->d_src);
+  if (h->h_src) cudaFreeHost(h->h_src);
+  h->d_src = nullptr;
+  h->h_src = nullptr;
+  h->d_src_cap = h->h_src_cap = 0;
+  if (cudaMalloc(&h->d_src, cap) != cudaSuccess) return fail(EQ_ERR_OOM, "cudaMalloc (sources)");
+  if (cudaMallocHost(&h->h_src, cap) != cudaSuccess)
+    return fail(EQ_ERR_OOM, "cudaMallocHost (sources)");
+  h->d_src_cap = h->h_src_cap = cap;
+  return EQ_OK;
+}
+
+void free_handle(eq_fluid* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaFree(h->block);
+  cudaFree(h->cells);
+  cudaFree(h->code);
+  cudaFree(h->rowfl);
+  cudaFree(h->colfl);
+  cudaFree(h->edge);
+  cudaFree(h->progress);
+  cudaFree(h->counters);
+  cudaFree(h->err);
+  cudaFree(h->d_src);
+  if (h->h_src) cudaFreeHost(h->h_src);
+  if (h->src_ev) cudaEventDestroy(h->src_ev);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int alloc_handle(uint32_t size, int device, eq_fluid** out) {
+  if (device < 0) {
+    EQ_CUDA(cudaGetDevice(&device));
+  }
+  EQ_CUDA(cudaSetDevice(device));
+  eq_fluid* h = new eq_fluid();
+  h->device = device;
+  h->S = size;
+  h->P = (int)(((size + 31u) / 32u) * 32u);
+  auto bail = [&](int code, const char* what) {
+    free_handle(h);
+    return fail(code, what);
+  };
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(EQ_ERR_CUDA, "cudaStreamCreate");
+  if (cudaEventCreateWithFlags(&h->src_ev, cudaEventDisableTiming) != cudaSuccess)
+    return bail(EQ_ERR_CUDA, "cudaEventCreate");
+  const size_t g = h->grid_elems();
+  if (cudaMalloc(&h->block, 7 * g * sizeof(float)) != cudaSuccess)
+    return bail(EQ_ERR_OOM, "cudaMalloc (grids)");
+  for (int f = 0; f < 6; ++f) h->field[f] = h->block + f * g;
+  h->spare = h->block + 6 * g;
+  if (cudaMalloc(&h->cells, g) != cudaSuccess || cudaMalloc(&h->code, g) != cudaSuccess ||
+      cudaMalloc(&h->rowfl, size) != cudaSuccess || cudaMalloc(&h->colfl, size) != cudaSuccess)
+    return bail(EQ_ERR_OOM, "cudaMalloc (mask)");
+  h->B = strips_for((int)size, kMaxSweepsPerLaunch);
+  const size_t ntasks = (size_t)h->B * kMaxSweepsPerLaunch;
+  if (cudaMalloc(&h->edge, ntasks * h->P * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&h->progress, ntasks * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&h->counters, 2 * sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(&h->err, sizeof(int)) != cudaSuccess)
+    return bail(EQ_ERR_OOM, "cudaMalloc (wavefront state)");
+  if (cudaMemsetAsync(h->block, 0, 7 * g * sizeof(float), h->stream) != cudaSuccess ||
+      cudaMemsetAsync(h->progress, 0, ntasks * sizeof(unsigned long long), h->stream) != cudaSuccess ||
+      cudaMemsetAsync(h->counters, 0, 2 * sizeof(unsigned), h->stream) != cudaSuccess ||
+      cudaMemsetAsync(h->err, 0, sizeof(int), h->stream) != cudaSuccess)
+    return bail(EQ_ERR_CUDA, "cudaMemsetAsync");
+  h->host_cells.assign((size_t)size * size, 0);
+  *out = h;
+  return EQ_OK;
+}
+
+// init() (fluid.rs:602-606) applied to the current state: computed on the
+// host (it is O(size^2) set-up, not the hot path) and written back.
+int apply_init(eq_fluid* h) {
+  const uint32_t S = h->S;
+  const size_t n = (size_t)S * S;
+  std::vector<float> f[6];
+  for (int q = 0; q < 6; ++q) {
+    f[q].resize(n);
+    int rc = eq_fluid_read_field(h, q, f[q].data(), n);
+    if (rc) return rc;
+  }
+  auto idx = [&](int64_t x, int64_t y) {
+    const int64_t s = S;
+    x = x < 0 ? 0 : (x > s - 1 ? s - 1 : x);
+    y = y < 0 ? 0 : (y > s - 1 ? s - 1 : y);
+    return (size_t)(x + y * s);
+  };
+  for (uint32_t j = 0; j < S; ++j)
+    for (uint32_t i = 0; i < S; ++i) {
+      f[EQ_FIELD_VX][idx(i, j)] += 1.0f;
+      f[EQ_FIELD_VY][idx(i, j)] += 1.0f;
+    }
+  for (uint32_t j = 0; j < S; ++j)
+    for (uint32_t i = 0; i < S; ++i) {
+      f[EQ_FIELD_DENSITY][idx(i, j)] += 0.0f;
+      f[EQ_FIELD_SCRATCH][idx(i, j)] += 0.0f;
+    }
+  for (uint32_t j = S / 2 - 10; j <= S / 2 + 10; ++j)
+    for (uint32_t i = S / 2 - 10; i <= S / 2 + 10; ++i) {
+      f[EQ_FIELD_DENSITY][idx(i, j)] += 0.9f;
+      f[EQ_FIELD_SCRATCH][idx(i, j)] += 0.9f;
+    }
+  for (uint32_t i = 0; i < S; ++i) {
+    h->host_cells[idx(i, 0)] = 1;
+    h->host_cells[idx(i, S - 1)] = 1;
+  }
+  for (uint32_t j = 0; j < S; ++j) {
+    h->host_cells[idx(0, j)] = 1;
+    h->host_cells[idx(S - 1, j)] = 1;
+  }
+  h->mask_dirty = true;
+  for (int q = 0; q < 6; ++q) {
+    int rc = eq_fluid_write_field(h, q, f[q].data(), n);
+    if (rc) return rc;
+  }
+  EQ_CUDA(cudaStreamSynchronize(h->stream));
+  return upload_mask(h);
+}
+
+int read_err_word(eq_fluid* h) {
+  int e = 0;
+  EQ_CUDA(cudaMemcpyAsync(&e, h->err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  EQ_CUDA(cudaStreamSynchronize(h->stream));
+  if (e != 0) {
+    // Leave the wavefront state clean for the next launch.
+    const size_t ntasks = (size_t)h->B * kMaxSweepsPerLaunch;
+    EQ_CUDA(cudaMemsetAsync(h->progress, 0, ntasks * sizeof(unsigned long long), h->stream));
+    EQ_CUDA(cudaMemsetAsync(h->counters, 0, 2 * sizeof(unsigned), h->stream));
+    EQ_CUDA(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
+    EQ_CUDA(cudaStreamSynchronize(h->stream));
+    if (e == EQ_ERR_TIMEOUT)
+      return fail(EQ_ERR_TIMEOUT, "lin_solve: a bounded inter-block wait ran out");
+    return fail(EQ_ERR_STATE, "device error word set");
+  }
+  return EQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int eq_abi_version(void) { return EQ_ABI_VERSION; }
+
+const char* eq_last_error(void) { return g_last_error.c_str(); }
+
+int eq_fluid_new(const eq_fluid_configs* fluid, const eq_simulation_configs* sim, int device,
+                 eq_fluid** out) {
+  if (!fluid || !sim || !out) return fail(EQ_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (sim->size < 20) return fail(EQ_ERR_ARG, "size must be >= 20 (fluid.rs:534 underflows)");
+  if (sim->size > 65536) return fail(EQ_ERR_ARG, "size too large");
+  if (sim->frames < 0) return fail(EQ_ERR_ARG, "frames must be >= 0");
+  eq_fluid* h = nullptr;
+  int rc = alloc_handle(sim->size, device, &h);
+  if (rc) return rc;
+  h->dt = sim->delta_t;
+  h->frames = sim->frames;
+  h->diff = fluid->diffusion;
+  h->visc = fluid->viscousity;
+  h->has_perlin_noise = fluid->has_perlin_noise;
+  if ((rc = apply_init(h))) {
+    free_handle(h);
+    return rc;
+  }
+  *out = h;
+  return EQ_OK;
+}
+
+int eq_fluid_default(int device, eq_fluid** out) {
+  // configs.rs:14-22 and 50-60.
+  eq_simulation_configs sim{0.02f, 16, 128};
+  eq_fluid_configs fl{0.0f, 0.001f, 1};
+  int rc = eq_fluid_new(&fl, &sim, device, out);
+  if (rc) return rc;
+  rc = apply_init(*out);  // Default calls init() a second time (fluid.rs:86)
+  if (rc) {
+    free_handle(*out);
+    *out = nullptr;
+  }
+  return rc;
+}
+
+int eq_fluid_init(eq_fluid* h) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  int rc = select_device(h);
+  if (rc) return rc;
+  return apply_init(h);
+}
+
+int eq_fluid_clone(const eq_fluid* src, eq_fluid** out) {
+  if (!src || !out) return fail(EQ_ERR_ARG, "null argument");
+  *out = nullptr;
+  eq_fluid* h = nullptr;
+  int rc = alloc_handle(src->S, src->device, &h);
+  if (rc) return rc;
+  h->dt = src->dt;
+  h->frames = src->frames;
+  h->diff = src->diff;
+  h->visc = src->visc;
+  h->has_perlin_noise = src->has_perlin_noise;
+  h->spin_limit = src->spin_limit;
+  h->host_cells = src->host_cells;
+  h->mask_dirty = true;
+  // Order the copy after the source's pending work.
+  cudaEvent_t ev;
+  if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventRecord(ev, src->stream) != cudaSuccess ||
+      cudaStreamWaitEvent(h->stream, ev, 0) != cudaSuccess) {
+    free_handle(h);
+    return fail(EQ_ERR_CUDA, "clone: event");
+  }
+  cudaEventDestroy(ev);
+  if (cudaMemcpyAsync(h->block, src->block, 6 * h->grid_elems() * sizeof(float),
+                      cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess) {
+    free_handle(h);
+    return fail(EQ_ERR_CUDA, "clone: copy");
+  }
+  if ((rc = upload_mask(h))) {
+    free_handle(h);
+    return rc;
+  }
+  *out = h;
+  return EQ_OK;
+}
+
+int eq_fluid_free(eq_fluid* h) {
+  free_handle(h);
+  return EQ_OK;
+}
+
+int eq_fluid_get_configs(const eq_fluid* h, eq_fluid_configs* fluid,
+                         eq_simulation_configs* sim) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  if (fluid) {
+    fluid->diffusion = h->diff;
+    fluid->viscousity = h->visc;
+    fluid->has_perlin_noise = h->has_perlin_noise;
+  }
+  if (sim) {
+    sim->delta_t = h->dt;
+    sim->frames = h->frames;
+    sim->size = h->S;
+  }
+  return EQ_OK;
+}
+
+int eq_fluid_set_configs(eq_fluid* h, const eq_fluid_configs* fluid,
+                         const eq_simulation_configs* sim) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  if (sim) {
+    if (sim->size != h->S) return fail(EQ_ERR_ARG, "size cannot change");
+    if (sim->frames < 0) return fail(EQ_ERR_ARG, "frames must be >= 0");
+    h->dt = sim->delta_t;
+    h->frames = sim->frames;
+  }
+  if (fluid) {
+    h->diff = fluid->diffusion;
+    h->visc = fluid->viscousity;
+    h->has_perlin_noise = fluid->has_perlin_noise;
+  }
+  return EQ_OK;
+}
+
+int eq_fluid_step(eq_fluid* h) { return eq_fluid_step_n(h, 1); }
+
+int eq_fluid_step_n(eq_fluid* h, int64_t nframes) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  if (nframes < 0) return fail(EQ_ERR_ARG, "nframes must be >= 0");
+  int rc = select_device(h);
+  if (rc) return rc;
+  for (int64_t f = 0; f < nframes; ++f)
+    if ((rc = launch_step(h))) return rc;
+  return EQ_OK;
+}
+
+int eq_fluid_synchronize(eq_fluid* h) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  int rc = select_device(h);
+  if (rc) return rc;
+  EQ_CUDA(cudaStreamSynchronize(h->stream));
+  return read_err_word(h);
+}
+
+int eq_fluid_add_sources(eq_fluid* h, int64_t n, const uint32_t* x, const uint32_t* y,
+                         const float* density, const float* vx, const float* vy) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  if (n < 0) return fail(EQ_ERR_ARG, "n must be >= 0");
+  if (n == 0) return EQ_OK;
+  if (!x || !y) return fail(EQ_ERR_ARG, "null coordinates");
+  int rc = select_device(h);
+  if (rc) return rc;
+  const size_t bytes = (size_t)n * (2 * sizeof(uint32_t) + 3 * sizeof(float));
+  if ((rc = ensure_src_capacity(h, bytes))) return rc;
+  EQ_CUDA(cudaEventSynchronize(h->src_ev));  // previous upload has consumed the staging
+  uint8_t* p = h->h_src;
+  std::memcpy(p, x, n * sizeof(uint32_t));
+  std::memcpy(p + n * 4, y, n * sizeof(uint32_t));
+  float* fd = reinterpret_cast<float*>(p + n * 8);
+  float* fu = fd + n;
+  float* fv = fu + n;
+  for (int64_t s = 0; s < n; ++s) {
+    fd[s] = density ? density[s] : 0.0f;
+    fu[s] = vx ? vx[s] : 0.0f;
+    fv[s] = vy ? vy[s] : 0.0f;
+  }
+  EQ_CUDA(cudaMemcpyAsync(h->d_src, h->h_src, bytes, cudaMemcpyHostToDevice, h->stream));
+  EQ_CUDA(cudaEventRecord(h->src_ev, h->stream));
+  const uint32_t* dx = reinterpret_cast<const uint32_t*>(h->d_src);
+  const uint32_t* dy = dx + n;
+  const float* dd = reinterpret_cast<const float*>(h->d_src + n * 8);
+  eqk::k_sources<<<1, 1, 0, h->stream>>>(
+      h->field[EQ_FIELD_DENSITY], h->field[EQ_FIELD_SCRATCH], h->field[EQ_FIELD_VX],
+      h->field[EQ_FIELD_VY], (int)h->S, h->P, n, dx, dy, density ? dd : nullptr,
+      vx ? dd + n : nullptr, vy ? dd + 2 * n : nullptr);
+  return check_launch(h);
+}
+
+int eq_fluid_add_density(eq_fluid* h, uint32_t x, uint32_t y, float amount) {
+  return eq_fluid_add_sources(h, 1, &x, &y, &amount, nullptr, nullptr);
+}
+
+int eq_fluid_add_velocity(eq_fluid* h, uint32_t x, uint32_t y, float amount_x,
+                          float amount_y) {
+  return eq_fluid_add_sources(h, 1, &x, &y, nullptr, &amount_x, &amount_y);
+}
+
+int eq_fluid_run_device_sources(eq_fluid* h, int64_t nframes, int64_t nsrc,
+                                const uint32_t* d_x, const uint32_t* d_y,
+                                const float* d_density, const float* d_vx,
+                                const float* d_vy) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  if (nframes < 0 || nsrc < 0) return fail(EQ_ERR_ARG, "negative count");
+  if (nsrc > 0 && (!d_x || !d_y)) return fail(EQ_ERR_ARG, "null coordinates");
+  int rc = select_device(h);
+  if (rc) return rc;
+  for (int64_t f = 0; f < nframes; ++f) {
+    if (nsrc > 0) {
+      const int64_t o = f * nsrc;
+      eqk::k_sources<<<1, 1, 0, h->stream>>>(
+          h->field[EQ_FIELD_DENSITY], h->field[EQ_FIELD_SCRATCH], h->field[EQ_FIELD_VX],
+          h->field[EQ_FIELD_VY], (int)h->S, h->P, nsrc, d_x + o, d_y + o,
+          d_density ? d_density + o : nullptr, d_vx ? d_vx + o : nullptr,
+          d_vy ? d_vy + o : nullptr);
+      if ((rc = check_launch(h))) return rc;
+    }
+    if ((rc = launch_step(h))) return rc;
+  }
+  return EQ_OK;
+}
+
+int eq_rectangle_check(int64_t dl_x, int64_t dl_y, int64_t ur_x, int64_t ur_y,
+                       uint32_t size) {
+  const int64_t s = size;
+  const bool ok = dl_x != ur_x && dl_y != ur_y && dl_x < ur_x && dl_y < ur_y && dl_x < s &&
+                  dl_y < s && ur_x < s && ur_y < s;
+  return ok ? EQ_OK : fail(EQ_ERR_ARG, "Invalid input for Rectangle");
+}
+
+int eq_fluid_fill_obstacle(eq_fluid* h, int64_t x0, int64_t y0, int64_t x1, int64_t y1) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  const int64_t S = h->S;
+  for (int64_t x = x0; x < x1; ++x)
+    for (int64_t y = y0; y < y1; ++y) {
+      const int64_t cx = x < 0 ? 0 : (x > S - 1 ? S - 1 : x);
+      const int64_t cy = y < 0 ? 0 : (y > S - 1 ? S - 1 : y);
+      h->host_cells[(size_t)(cx + cy * S)] = 1;
+    }
+  h->mask_dirty = true;
+  return EQ_OK;
+}
+
+static int field_copy(eq_fluid* h, int field, void* host, uint64_t n, bool to_host,
+                      bool sync) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  int rc = check_field(field);
+  if (rc) return rc;
+  if (n != (uint64_t)h->S * h->S) return fail(EQ_ERR_ARG, "element count must be size*size");
+  if (!host) return fail(EQ_ERR_ARG, "null host buffer");
+  if ((rc = select_device(h))) return rc;
+  const size_t w = (size_t)h->S * sizeof(float);
+  if (to_host)
+    EQ_CUDA(cudaMemcpy2DAsync(host, w, h->field[field], (size_t)h->P * sizeof(float), w, h->S,
+                              cudaMemcpyDeviceToHost, h->stream));
+  else
+    EQ_CUDA(cudaMemcpy2DAsync(h->field[field], (size_t)h->P * sizeof(float), host, w, w, h->S,
+                              cudaMemcpyHostToDevice, h->stream));
+  if (sync) EQ_CUDA(cudaStreamSynchronize(h->stream));
+  return EQ_OK;
+}
+
+int eq_fluid_read_field(eq_fluid* h, int field, float* host, uint64_t n) {
+  int rc = field_copy(h, field, host, n, true, true);
+  if (rc) return rc;
+  return read_err_word(h);
+}
+int eq_fluid_write_field(eq_fluid* h, int field, const float* host, uint64_t n) {
+  return field_copy(h, field, const_cast<float*>(host), n, false, true);
+}
+int eq_fluid_read_field_async(eq_fluid* h, int field, float* host, uint64_t n) {
+  return field_copy(h, field, host, n, true, false);
+}
+int eq_fluid_write_field_async(eq_fluid* h, int field, const float* host, uint64_t n) {
+  return field_copy(h, field, const_cast<float*>(host), n, false, false);
+}
+
+int eq_fluid_read_cells(eq_fluid* h, uint8_t* host, uint64_t n) {
+  if (!h || !host) return fail(EQ_ERR_ARG, "null argument");
+  if (n != (uint64_t)h->S * h->S) return fail(EQ_ERR_ARG, "element count must be size*size");
+  std::memcpy(host, h->host_cells.data(), n);
+  return EQ_OK;
+}
+
+int eq_fluid_write_cells(eq_fluid* h, const uint8_t* host, uint64_t n) {
+  if (!h || !host) return fail(EQ_ERR_ARG, "null argument");
+  const uint32_t S = h->S;
+  if (n != (uint64_t)S * S) return fail(EQ_ERR_ARG, "element count must be size*size");
+  for (uint32_t i = 0; i < S; ++i)
+    if (!host[i] || !host[(size_t)(S - 1) * S + i] || !host[(size_t)i * S] ||
+        !host[(size_t)i * S + S - 1])
+      return fail(EQ_ERR_ARG, "the ghost frame must stay DefaultWall");
+  for (uint64_t q = 0; q < n; ++q) h->host_cells[q] = host[q] ? 1 : 0;
+  h->mask_dirty = true;
+  return EQ_OK;
+}
+
+int eq_fluid_set_boundaries(eq_fluid* h, int mode, int field) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  int rc;
+  if ((rc = check_mode(mode)) || (rc = check_field(field)) || (rc = select_device(h)) ||
+      (rc = upload_mask(h)))
+    return rc;
+  return launch_bnd(h, mode, h->field[field]);
+}
+
+int eq_fluid_lin_solve(eq_fluid* h, int mode, int x_field, int x0_field, float a, float c) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  int rc;
+  if ((rc = check_mode(mode)) || (rc = check_field(x_field)) || (rc = check_field(x0_field)))
+    return rc;
+  if (x_field == x0_field) return fail(EQ_ERR_ARG, "x and x0 must differ");
+  if ((rc = select_device(h)) || (rc = upload_mask(h))) return rc;
+  return launch_lin_solve(h, mode, h->field[x_field], h->field[x0_field], a, c);
+}
+
+int eq_fluid_diffuse(eq_fluid* h, int mode, int x_field, int x0_field, float diffusion) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  int rc;
+  if ((rc = check_mode(mode)) || (rc = check_field(x_field)) || (rc = check_field(x0_field)))
+    return rc;
+  if (x_field == x0_field) return fail(EQ_ERR_ARG, "x and x0 must differ");
+  if ((rc = select_device(h)) || (rc = upload_mask(h))) return rc;
+  return launch_diffuse(h, mode, h->field[x_field], h->field[x0_field], diffusion);
+}
+
+int eq_fluid_project(eq_fluid* h, int vx_field, int vy_field, int p_field, int div_field) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  int rc;
+  if ((rc = check_field(vx_field)) || (rc = check_field(vy_field)) ||
+      (rc = check_field(p_field)) || (rc = check_field(div_field)))
+    return rc;
+  const int f[4] = {vx_field, vy_field, p_field, div_field};
+  for (int a = 0; a < 4; ++a)
+    for (int b = a + 1; b < 4; ++b)
+      if (f[a] == f[b]) return fail(EQ_ERR_ARG, "project fields must be distinct");
+  if ((rc = select_device(h)) || (rc = upload_mask(h))) return rc;
+  return launch_project(h, h->field[vx_field], h->field[vy_field], h->field[p_field],
+                        h->field[div_field]);
+}
+
+int eq_fluid_advect(eq_fluid* h, int mode, int d_field, int d0_field, int u_field,
+                    int v_field) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  int rc;
+  if ((rc = check_mode(mode)) || (rc = check_field(d_field)) || (rc = check_field(d0_field)) ||
+      (rc = check_field(u_field)) || (rc = check_field(v_field)))
+    return rc;
+  if (d_field == d0_field || d_field == u_field || d_field == v_field)
+    return fail(EQ_ERR_ARG, "advect destination must differ from its inputs");
+  if ((rc = select_device(h)) || (rc = upload_mask(h))) return rc;
+  return launch_advect(h, mode, h->field[d_field], h->field[d0_field], h->field[u_field],
+                       h->field[v_field]);
+}
+
+int eq_fluid_device_field(eq_fluid* h, int field, float** dptr, uint32_t* pitch_elems) {
+  if (!h || !dptr) return fail(EQ_ERR_ARG, "null argument");
+  int rc = check_field(field);
+  if (rc) return rc;
+  *dptr = h->field[field];
+  if (pitch_elems) *pitch_elems = (uint32_t)h->P;
+  return EQ_OK;
+}
+
+int eq_fluid_launch_count(const eq_fluid* h, uint64_t* count) {
+  if (!h || !count) return fail(EQ_ERR_ARG, "null argument");
+  *count = h->launches;
+  return EQ_OK;
+}
+
+int eq_fluid_set_spin_limit(eq_fluid* h, int64_t iterations) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  if (iterations < 1) return fail(EQ_ERR_ARG, "spin limit must be >= 1");
+  h->spin_limit = iterations;
+  return EQ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,224 @@
+/*
+ * eqfluid.h -- C ABI of the GB300-native (sm_103a) stable-fluids frame step.
+ *
+ * This is the drop-in boundary for Equilibrium's solver
+ * (vkabadzhova/equilibrium, src/simulation/fluid.rs). A Rust (or any other)
+ * host binds these functions with a plain `extern "C"` block; no C++ or torch
+ * type crosses the boundary: only opaque handles, plain pointers, sizes and
+ * IEEE-754 scalars.
+ *
+ * State layout. A handle owns the six f32 arrays of `Fluid` (fluid.rs:59-77),
+ * each `size * size` cells including the ghost frame, x fastest
+ * (idx = x + y*size, fluid.rs:31-35), plus the wall mask `cells_type`
+ * (fluid.rs:80) as one byte per cell: 1 = DefaultWall, 0 = NoWall. Host
+ * buffers passed to the read/write functions use exactly that dense layout.
+ * On the device the rows are padded to a 128-byte pitch.
+ *
+ * Errors. Every function returns EQ_OK (0) or a positive EQ_ERR_* code; the
+ * reference panics in the same places (Rectangle::new, obstacle.rs:126-128),
+ * which a Rust wrapper reproduces by panicking on a non-zero return.
+ * eq_last_error() gives a message for the calling thread's last failure.
+ *
+ * Threading. One handle is used by one host thread at a time (the reference
+ * moves a Fluid into its simulation thread and clones it per frame,
+ * renderer.rs:125-128, renderer_helpers.rs:61-64). Each handle owns a CUDA
+ * stream on its device; every entry point selects that device first, so a
+ * handle may be driven from any host thread.
+ *
+ * Arithmetic. The plain step is bit-identical to the reference's f32 step:
+ * kernels use explicitly rounded adds and multiplies (never contracted into
+ * FMA), IEEE division, the reference's evaluation order and its quirks
+ * (advect's row break, aliasing of the six arrays, obstacle-blind scalar
+ * boundaries).
+ */
+#ifndef EQFLUID_H
+#define EQFLUID_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EQ_ABI_VERSION 1
+
+/* Status codes. */
+#define EQ_OK 0
+#define EQ_ERR_ARG 1     /* invalid argument (size, field, rectangle, mask frame) */
+#define EQ_ERR_CUDA 2    /* a CUDA runtime call failed */
+#define EQ_ERR_TIMEOUT 3 /* a bounded inter-block wait ran out (device error word) */
+#define EQ_ERR_OOM 4     /* device or host allocation failed */
+#define EQ_ERR_STATE 5   /* handle in an unusable state */
+
+/* Field indices: the six arrays of Fluid in declaration order (fluid.rs:59-77). */
+#define EQ_FIELD_SCRATCH 0 /* scratch_space (private in the reference) */
+#define EQ_FIELD_DENSITY 1 /* pub density */
+#define EQ_FIELD_VX 2      /* pub velocities_x */
+#define EQ_FIELD_VY 3      /* pub velocities_y */
+#define EQ_FIELD_VX0 4     /* velocities_x0 (private) */
+#define EQ_FIELD_VY0 5     /* velocities_y0 (private) */
+
+/* Orientation (fluid.rs:21-29). */
+#define EQ_MODE_ADJUST_ROW 0
+#define EQ_MODE_ADJUST_COLUMN 1
+#define EQ_MODE_PASSIVE 2
+
+/* SimulationConfigs (configs.rs:5-12). `frames` is both the app's frame count
+ * and the Gauss-Seidel sweep count of every lin_solve (fluid.rs:312). */
+typedef struct eq_simulation_configs {
+  float delta_t;
+  int64_t frames;
+  uint32_t size; /* cells per side including the ghost frame */
+} eq_simulation_configs;
+
+/* FluidConfigs (configs.rs:37-48); the two display colours stay on the host. */
+typedef struct eq_fluid_configs {
+  float diffusion;
+  float viscousity;
+  int32_t has_perlin_noise;
+} eq_fluid_configs;
+
+typedef struct eq_fluid eq_fluid; /* opaque; owns device state */
+
+/* ---- lifecycle --------------------------------------------------------- */
+
+/* Fluid::new (fluid.rs:93-110): zeroed arrays, all NoWall, then init()
+ * (fluid.rs:602-606): vx = vy = 1 everywhere, +0.9 density (and scratch) on
+ * the 21x21 block centred at size/2, frame = DefaultWall. Requires
+ * size >= 20 (smaller sizes underflow `size/2 - 10`, fluid.rs:534) and
+ * frames >= 0. `device` < 0 means the current CUDA device. */
+int eq_fluid_new(const eq_fluid_configs* fluid, const eq_simulation_configs* sim,
+                 int device, eq_fluid** out);
+
+/* Fluid::default (fluid.rs:83-89): new() with the default configs
+ * (configs.rs:14-22, 50-60), then init() a second time (velocities 2.0,
+ * block density 1.8). */
+int eq_fluid_default(int device, eq_fluid** out);
+
+/* Re-applies init() (fluid.rs:602-606) on top of the current state. */
+int eq_fluid_init(eq_fluid* h);
+
+/* #[derive(Clone)] (fluid.rs:51): a deep device-to-device copy. */
+int eq_fluid_clone(const eq_fluid* h, eq_fluid** out);
+
+/* Drop: frees the device state. Accepts NULL. */
+int eq_fluid_free(eq_fluid* h);
+
+int eq_fluid_get_configs(const eq_fluid* h, eq_fluid_configs* fluid,
+                         eq_simulation_configs* sim);
+
+/* Changes delta_t / frames / diffusion / viscousity (the pub config fields,
+ * fluid.rs:54-56). `size` must stay the same. */
+int eq_fluid_set_configs(eq_fluid* h, const eq_fluid_configs* fluid,
+                         const eq_simulation_configs* sim);
+
+/* ---- the hot path ------------------------------------------------------ */
+
+/* Fluid::step (fluid.rs:437-524): diffuse vx/vy, project, advect vx/vy,
+ * project, diffuse + advect density, scratch = density. Asynchronous on the
+ * handle's stream; returns after launching. */
+int eq_fluid_step(eq_fluid* h);
+
+/* `nframes` consecutive steps. */
+int eq_fluid_step_n(eq_fluid* h, int64_t nframes);
+
+/* Blocks until the handle's stream is idle and reports any device-side
+ * error (EQ_ERR_TIMEOUT when a bounded wait ran out). */
+int eq_fluid_synchronize(eq_fluid* h);
+
+/* ---- sources (fluid.rs:120-131) ---------------------------------------- */
+
+/* add_density: density[idx] += amount; scratch[idx] += amount, with idx!'s
+ * clamping of (x, y) into the grid (fluid.rs:31-35). */
+int eq_fluid_add_density(eq_fluid* h, uint32_t x, uint32_t y, float amount);
+
+/* add_velocity: vx[idx] += amount_x; vy[idx] += amount_y. */
+int eq_fluid_add_velocity(eq_fluid* h, uint32_t x, uint32_t y, float amount_x,
+                          float amount_y);
+
+/* n sources from HOST arrays, applied in array order: for each s,
+ * add_density(x[s], y[s], density[s]) and add_velocity(x[s], y[s], vx[s],
+ * vy[s]). Any of density/vx/vy may be NULL (treated as no contribution). */
+int eq_fluid_add_sources(eq_fluid* h, int64_t n, const uint32_t* x, const uint32_t* y,
+                         const float* density, const float* vx, const float* vy);
+
+/* `nframes` frames, each = that frame's sources then step(), with the sources
+ * read from DEVICE arrays of shape [nframes][nsrc] (frame-major). This is
+ * the form a frame loop with pre-staged inputs uses. */
+int eq_fluid_run_device_sources(eq_fluid* h, int64_t nframes, int64_t nsrc,
+                                const uint32_t* d_x, const uint32_t* d_y,
+                                const float* d_density, const float* d_vx,
+                                const float* d_vy);
+
+/* ---- obstacles (fluid.rs:610-619, obstacle.rs:115-147) ------------------ */
+
+/* Rectangle::new validation: EQ_OK if dl.x < ur.x, dl.y < ur.y and all four
+ * coordinates are < size, else EQ_ERR_ARG (the reference panics). */
+int eq_rectangle_check(int64_t dl_x, int64_t dl_y, int64_t ur_x, int64_t ur_y,
+                       uint32_t size);
+
+/* fill_obstacle: marks [x0,x1) x [y0,y1) as DefaultWall (clamped idx!). */
+int eq_fluid_fill_obstacle(eq_fluid* h, int64_t x0, int64_t y0, int64_t x1, int64_t y1);
+
+/* ---- the pub fields: host <-> device ------------------------------------ */
+
+/* Dense size*size copies. `n` is the element count of the host buffer and
+ * must equal size*size. Reads synchronise the handle's stream. */
+int eq_fluid_read_field(eq_fluid* h, int field, float* host, uint64_t n);
+int eq_fluid_write_field(eq_fluid* h, int field, const float* host, uint64_t n);
+
+/* Asynchronous variants on the handle's stream (host memory should be pinned
+ * for true asynchrony); complete at the next eq_fluid_synchronize. */
+int eq_fluid_read_field_async(eq_fluid* h, int field, float* host, uint64_t n);
+int eq_fluid_write_field_async(eq_fluid* h, int field, const float* host, uint64_t n);
+
+/* cells_type (fluid.rs:80) as bytes, 1 = DefaultWall. A written mask must keep
+ * the whole ghost frame as DefaultWall (init_walls, fluid.rs:552-570, makes it
+ * so and nothing in the reference clears it); otherwise EQ_ERR_ARG. */
+int eq_fluid_read_cells(eq_fluid* h, uint8_t* host, uint64_t n);
+int eq_fluid_write_cells(eq_fluid* h, const uint8_t* host, uint64_t n);
+
+/* ---- single phases (the reference's private functions), on fields ------- */
+
+/* set_boundaries (fluid.rs:252-272) on one field. */
+int eq_fluid_set_boundaries(eq_fluid* h, int mode, int field);
+
+/* lin_solve (fluid.rs:301-325): `frames` Gauss-Seidel sweeps of
+ * x = (x0 + a*(x[i+1]+x[i-1]+x[j+1]+x[j-1])) / c, each followed by
+ * set_boundaries(mode). x_field != x0_field. */
+int eq_fluid_lin_solve(eq_fluid* h, int mode, int x_field, int x0_field, float a, float c);
+
+/* diffuse (fluid.rs:276-298): lin_solve with a = dt*diff*(size-2)^2, c = 1+4a. */
+int eq_fluid_diffuse(eq_fluid* h, int mode, int x_field, int x0_field, float diffusion);
+
+/* project (fluid.rs:330-375) on four distinct fields. */
+int eq_fluid_project(eq_fluid* h, int vx_field, int vy_field, int p_field, int div_field);
+
+/* advect (fluid.rs:378-432); d_field must differ from d0/u/v. */
+int eq_fluid_advect(eq_fluid* h, int mode, int d_field, int d0_field, int u_field,
+                    int v_field);
+
+/* ---- diagnostics ------------------------------------------------------- */
+
+/* Device pointer of a field (pitched rows) and the row pitch in elements. */
+int eq_fluid_device_field(eq_fluid* h, int field, float** dptr, uint32_t* pitch_elems);
+
+/* Number of kernel launches this handle has issued since creation. */
+int eq_fluid_launch_count(const eq_fluid* h, uint64_t* count);
+
+/* Bounded-wait budget of the inter-block waits, in polling iterations
+ * (default: about one second of polling). Lowering it makes a wait that
+ * cannot complete end with EQ_ERR_TIMEOUT sooner. */
+int eq_fluid_set_spin_limit(eq_fluid* h, int64_t iterations);
+
+/* Message for the calling thread's last non-zero status ("" if none). */
+const char* eq_last_error(void);
+
+int eq_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EQFLUID_H */

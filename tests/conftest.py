@@ -1,0 +1,22 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    config.addinivalue_line("markers", "slow: long-running")
+
+
+@pytest.fixture(scope="session")
+def eqlib():
+    """The CUDA library, built in place if needed. GPU tests fail loudly if it
+    cannot be built or loaded: there is no CPU fallback."""
+    from equilibrium_gb300 import build, _lib
+    build.build()
+    return _lib.load()
