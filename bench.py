@@ -1,0 +1,382 @@
+#!/usr/bin/env python
+"""Benchmark of the plain (bit-exact) stable-fluids frame step on GB300.
+
+Workload (one scene, fits one GPU): N = 1024 interior cells per side
+(size 1026 with the ghost frame), dt = 0.05, diffusion = viscosity = 1e-5,
+20 Gauss-Seidel sweeps per lin_solve, four seeded rectangle obstacles of 2-8 %
+of the area each, eight seeded source cells injecting density U[0, 50] and
+velocity N(0, 3^2) every frame. A step is one frame: that frame's sources, then
+Fluid::step. The metric counts interior cells advanced one full step.
+
+  value  device-resident: sources pre-staged on the GPU, per-step CUDA events
+         on the scene's stream, L2 flushed (256 MiB write) between timed steps.
+  e2e    through the C ABI with host buffers: per step the sources go
+         host->device from pinned memory, the step runs, and the three pub
+         fields (density, velocities_x, velocities_y) come back device->host,
+         as a drop-in Fluid keeps its Vec<f32> fields current after step().
+
+`--impl reference` times the reference's algorithm on the host CPU instead:
+the C++ restatement in oracle/ (the Rust reference cannot be built here), one
+thread, as the reference runs step() on one thread.
+
+Multi-GPU (torchrun, N > 1): the plain single grid does not shard; every rank
+runs an independent replica (weak scaling) and `value` sums the replicas.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SIZE, DT, DIFF, VISC, ITERS, NSRC, SEED = 1026, 0.05, 1e-5, 1e-5, 20, 8, 2
+N = SIZE - 2
+BYTES_PER_CELL_LINSOLVE = 13  # read x0, read x, write x (f32) + mask byte, per S^2 cell
+BYTES_PER_CELL_FRAME = 164    # fused-phase compulsory traffic per S^2 cell per frame
+
+
+def baseline_metric():
+    try:
+        with open(os.path.join(ROOT, "BASELINE.json")) as f:
+            return json.load(f)["metric"]
+    except Exception:
+        return "cell-steps/s on 1 GB300"
+
+
+def scene(seed=SEED, nframes=1):
+    """Seeded obstacles (valid Rectangle inputs) and per-frame sources."""
+    rng = np.random.default_rng(seed)
+    rects = []
+    while len(rects) < 4:
+        frac = rng.uniform(0.02, 0.08)
+        aspect = rng.uniform(0.5, 2.0)
+        w = int(round(math.sqrt(frac * N * N * aspect)))
+        h = int(round(frac * N * N / max(w, 1)))
+        if w < 2 or h < 2 or w > N - 2 or h > N - 2:
+            continue
+        x0 = int(rng.integers(1, SIZE - 1 - w))
+        y0 = int(rng.integers(1, SIZE - 1 - h))
+        rects.append((x0, y0, x0 + w, y0 + h))
+    cells = rng.integers(1, SIZE - 1, size=(NSRC, 2))
+    # Box-Muller on the same stream for the velocity impulses
+    u1 = rng.uniform(size=(nframes, NSRC, 2))
+    u2 = rng.uniform(size=(nframes, NSRC, 2))
+    gauss = np.sqrt(-2.0 * np.log(np.maximum(u1, 1e-12))) * np.cos(2 * np.pi * u2) * 3.0
+    dens = rng.uniform(0.0, 50.0, size=(nframes, NSRC))
+    sx = np.broadcast_to(cells[:, 0], (nframes, NSRC)).astype(np.uint32).copy()
+    sy = np.broadcast_to(cells[:, 1], (nframes, NSRC)).astype(np.uint32).copy()
+    return (rects, sx, sy, dens.astype(np.float32), gauss[..., 0].astype(np.float32),
+            gauss[..., 1].astype(np.float32))
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(
+        os.environ.get("WORLD_SIZE", 1))
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu, self.proc, self.lines = gpu, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1].split()[0]))
+                mx.append(float(p[2].split()[0]))
+            except ValueError:
+                continue
+            for name, val in zip(names, p[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM traffic of the lin_solve wavefront from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "lin_solve_traffic.json")) as f:
+            d = json.load(f)
+        return d.get("dram_bytes_per_launch"), d.get("source")
+    except Exception:
+        return None, None
+
+
+def cpu_baseline_run(nframes: int):
+    """The oracle port (single thread) on the same workload from its initial state."""
+    import oracle
+    rects, sx, sy, sd, su, sv = scene(SEED, nframes)
+    f = oracle.OracleFluid(SIZE, DT, ITERS, DIFF, VISC)
+    for r in rects:
+        f.fill_obstacle(*r)
+    secs = f.run(nframes, sx, sy, sd, su, sv, timed=True)
+    return {"value": N * N * nframes / secs, "unit": "cell-steps/s", "cores": 1, "kind": "port",
+            "sample": f"{nframes} frames of the N=1024 workload from its initial state "
+                      f"({secs:.1f} s, oracle/ C++ restatement, -O3 -ffp-contract=off)"}
+
+
+def config_dict():
+    return {"workload": "plain frame step, N=1024 (size 1026), 20 GS sweeps, dt=0.05, "
+                        "diff=visc=1e-5, 4 seeded rectangles, 8 seeded sources/frame",
+            "size": SIZE, "interior_n": N, "gs_iterations": ITERS, "delta_t": DT,
+            "diffusion": DIFF, "viscosity": VISC, "obstacles": 4, "sources_per_frame": NSRC,
+            "seed": SEED, "l2": "flushed between timed steps (256 MiB write, untimed)",
+            "form": "plain, bit-exact vs the reference step"}
+
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    # Each step is one CPU frame (~1 s at N=1024): time at most 30 of them so
+    # the run stays within a few minutes whatever --steps is.
+    warm = min(args.warmup, 3)
+    timed = min(args.steps, 30)
+    rects, sx, sy, sd, su, sv = scene(SEED, warm + timed)
+    f = oracle.OracleFluid(SIZE, DT, ITERS, DIFF, VISC)
+    for r in rects:
+        f.fill_obstacle(*r)
+    for w in range(warm):
+        f.run(1, sx[w:w + 1], sy[w:w + 1], sd[w:w + 1], su[w:w + 1], sv[w:w + 1])
+    times = []
+    for s in range(timed):
+        q = warm + s
+        times.append(f.run(1, sx[q:q + 1], sy[q:q + 1], sd[q:q + 1], su[q:q + 1], sv[q:q + 1],
+                           timed=True))
+    t = statistics.mean(times)
+    value = N * N / t
+    line = {"impl": "reference", "metric": baseline_metric(), "value": value,
+            "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(),
+            "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": 1, "kind": "port",
+                             "sample": f"{timed} frames (one per step, after {warm} warm-up "
+                                       "frames) of the workload on the host CPU: the oracle/ C++ "
+                                       "restatement of the reference step, one thread like the "
+                                       "reference"},
+            "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    from equilibrium_gb300 import build as eqbuild
+    from equilibrium_gb300 import _lib
+    from equilibrium_gb300.simulation import Fluid, FluidConfigs, SimulationConfigs
+
+    rank, local_rank, world = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    eqbuild.build()
+    L = _lib.load()
+
+    total = args.warmup + args.steps
+    rects, sx, sy, sd, su, sv = scene(SEED + rank, 2 * total)
+    fl = Fluid(FluidConfigs(DIFF, VISC, False), SimulationConfigs(DT, ITERS, SIZE), device=local_rank)
+    for r in rects:
+        _lib.check(L.eq_fluid_fill_obstacle(fl.handle, *r))
+    stream_ptr = ctypes.c_void_p()
+    _lib.check(L.eq_fluid_get_stream(fl.handle, ctypes.byref(stream_ptr)))
+    stream = torch.cuda.ExternalStream(stream_ptr.value)
+    dev = torch.device("cuda", local_rank)
+    d_sx = torch.from_numpy(sx.astype(np.int32)).to(dev)
+    d_sy = torch.from_numpy(sy.astype(np.int32)).to(dev)
+    d_sd, d_su, d_sv = (torch.from_numpy(a).to(dev) for a in (sd, su, sv))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+
+    def frame(q):
+        o = q * NSRC * 4
+        _lib.check(L.eq_fluid_run_device_sources(
+            fl.handle, 1, NSRC, d_sx.data_ptr() + o, d_sy.data_ptr() + o, d_sd.data_ptr() + o,
+            d_su.data_ptr() + o, d_sv.data_ptr() + o))
+
+    for w in range(args.warmup):
+        frame(w)
+    fl.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- device-resident timed region
+    count0 = ctypes.c_uint64()
+    _lib.check(L.eq_fluid_launch_count(fl.handle, ctypes.byref(count0)))
+    _lib.check(L.eq_fluid_set_profiling(fl.handle, 1))
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    with ClockSampler(local_rank) as clk:
+        for s in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(s))
+                starts[s].record(stream)
+            frame(args.warmup + s)
+            ends[s].record(stream)
+        fl.synchronize()
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    barrier()
+    count1 = ctypes.c_uint64()
+    _lib.check(L.eq_fluid_launch_count(fl.handle, ctypes.byref(count1)))
+    ls_ms, ls_n = ctypes.c_double(), ctypes.c_uint64()
+    _lib.check(L.eq_fluid_kernel_stats(fl.handle, 0, ctypes.byref(ls_ms), ctypes.byref(ls_n)))
+    _lib.check(L.eq_fluid_set_profiling(fl.handle, 0))
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    dev_s = sum(step_ms) / 1e3
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([dev_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s = float(t.item())
+    ms_per_step = dev_s / args.steps * 1e3
+    value = world * N * N * args.steps / dev_s
+
+    # ---- end to end through the C ABI with host buffers
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    h_sx, h_sy, h_sd, h_su, h_sv = (pin(a) for a in (sx, sy, sd, su, sv))
+    outs = [torch.empty(SIZE * SIZE, dtype=torch.float32).pin_memory() for _ in range(3)]
+    e2e_times = []
+    base = total
+    barrier()
+    for s in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(s))
+        torch.cuda.synchronize()
+        fl.synchronize()
+        t0 = time.perf_counter()
+        q = (base + s) % (2 * total)
+        o = q * NSRC
+        _lib.check(L.eq_fluid_add_sources(
+            fl.handle, NSRC, h_sx.data_ptr() + 4 * o, h_sy.data_ptr() + 4 * o,
+            h_sd.data_ptr() + 4 * o, h_su.data_ptr() + 4 * o, h_sv.data_ptr() + 4 * o))
+        _lib.check(L.eq_fluid_step(fl.handle))
+        for f_idx, buf in zip((_lib.FIELD_DENSITY, _lib.FIELD_VX, _lib.FIELD_VY), outs):
+            _lib.check(L.eq_fluid_read_field(fl.handle, f_idx, buf.data_ptr(), SIZE * SIZE))
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_times)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * N * N * args.steps / e2e_s
+    assert np.isfinite(outs[0].numpy()).all()
+
+    if rank != 0:
+        return
+    hbm, peak_kind = peaks()
+    avg_ls = ls_ms.value / max(ls_n.value, 1) / 1e3
+    achieved = BYTES_PER_CELL_LINSOLVE * SIZE * SIZE / avg_ls / 1e9 if avg_ls > 0 else None
+    traffic, traffic_src = profile_traffic()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
+                "kernel": "k_lin_solve (persistent temporal-wavefront Gauss-Seidel)",
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_launch": BYTES_PER_CELL_LINSOLVE * SIZE * SIZE,
+                "launches_timed": int(ls_n.value), "avg_launch_ms": avg_ls * 1e3,
+                "share_of_step": (ls_ms.value / (dev_s / world * 1e3)) if dev_s else None,
+                "frame_roofline_frac": (BYTES_PER_CELL_FRAME * SIZE * SIZE /
+                                        (ms_per_step / 1e3) / 1e9 / hbm),
+                "traffic_source": traffic_src}
+    try:
+        cpu = cpu_baseline_run(args.cpu_frames)
+    except Exception as e:  # the oracle is only the reported baseline
+        cpu = {"value": None, "unit": "cell-steps/s", "cores": 1, "kind": "port",
+               "sample": f"failed: {e}"}
+    line = {"metric": baseline_metric(), "value": value, "unit": "cell-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded obstacles and sources; no dataset)",
+            "config": config_dict(), "roofline": roofline, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "cell-steps/s",
+                    "h2d_bytes_per_step": NSRC * 20,
+                    "d2h_bytes_per_step": 3 * SIZE * SIZE * 4,
+                    "ms_per_step": e2e_s / args.steps * 1e3},
+            "gpu_launches": int(count1.value - count0.value), "clocks": clk.summary(),
+            "wall_s_timed_region": wall}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-frames", type=int, default=12)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

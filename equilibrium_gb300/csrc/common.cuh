@@ -20,6 +20,7 @@ enum : uint8_t {
   kCodeColDown = 8u,     // AdjustColumn takes -x[i, j+1]
   kCodeColUp = 16u,      // AdjustColumn takes -x[i, j-1]
   kCodeAboveDown = 32u,  // the cell (i, j-1) has kCodeColDown
+  kCodeColFluid = 64u,   // column i holds a fluid cell (Passive frame rule)
 };
 constexpr uint8_t kCodeRowMask = kCodeRowLeft | kCodeRowRight;
 constexpr uint8_t kCodeColMask = kCodeColDown | kCodeColUp;
@@ -68,5 +69,25 @@ __device__ __forceinline__ unsigned atom_add_acq_rel_u32(unsigned* p, unsigned v
                : "memory");
   return old;
 }
+
+// Asynchronous global -> shared copies (L2 only for the 16-byte form, so data
+// another block released is read coherently after the acquire).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool pred) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile(
+      "{ .reg .pred p; setp.ne.b32 p, %2, 0; @p cp.async.cg.shared.global [%0], [%1], 16; }" ::"r"(s),
+      "l"(gmem), "r"((int)pred)
+      : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem, bool pred) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile(
+      "{ .reg .pred p; setp.ne.b32 p, %2, 0; @p cp.async.ca.shared.global [%0], [%1], 4; }" ::"r"(s),
+      "l"(gmem), "r"((int)pred)
+      : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 }  // namespace eqk

@@ -49,9 +49,8 @@ struct eq_fluid {
   int64_t frames = 0;
   int32_t has_perlin_noise = 0;
 
-  float* block = nullptr;  // 7 grids
+  float* block = nullptr;  // the 6 grids
   float* field[6] = {};
-  float* spare = nullptr;
   uint8_t* cells = nullptr;  // pitched mask, 1 = wall
   uint8_t* code = nullptr;   // pitched boundary codes
   uint8_t* rowfl = nullptr;  // [S] row has a fluid cell
@@ -61,9 +60,10 @@ struct eq_fluid {
 
   // lin_solve wavefront state
   int B = 0;  // strips for kMaxSweepsPerLaunch
-  float* edge = nullptr;
-  unsigned long long* progress = nullptr;
-  unsigned* counters = nullptr;  // [0] ticket, [1] done
+  unsigned long long* wt = nullptr;    // 2 sequence-tagged grids
+  unsigned long long* edge = nullptr;  // tagged last rows [B*64][P]
+  unsigned* counters = nullptr;        // [0] ticket, [1] done
+  uint32_t tag = 1;                    // next W(-1) tag (monotonic)
   int* err = nullptr;
   long long spin_limit = kDefaultSpinLimit;
 
@@ -75,6 +75,10 @@ struct eq_fluid {
   cudaEvent_t src_ev = nullptr;
 
   uint64_t launches = 0;
+
+  // optional kernel timing (event pairs around each wavefront launch)
+  bool profiling = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ls_events;
 
   size_t grid_elems() const { return (size_t)P * S; }
 };
@@ -128,6 +132,9 @@ int upload_mask(eq_fluid* h) {
       code[(size_t)j * P + i] |= c;
     }
   }
+  for (int j = 0; j < S; ++j)
+    for (int i = 0; i < S; ++i)
+      if (colfl[i]) code[(size_t)j * P + i] |= eqk::kCodeColFluid;
   EQ_CUDA(cudaMemcpyAsync(h->cells, cellsP.data(), cellsP.size(), cudaMemcpyHostToDevice,
                           h->stream));
   EQ_CUDA(cudaMemcpyAsync(h->code, code.data(), code.size(), cudaMemcpyHostToDevice,
@@ -176,17 +183,30 @@ int launch_lin_solve(eq_fluid* h, int mode, float* x, const float* x0, float a, 
   const int S = (int)h->S;
   for (int64_t done = 0; done < K; done += kMaxSweepsPerLaunch) {
     const int Kc = (int)std::min<int64_t>(kMaxSweepsPerLaunch, K - done);
-    EQ_CUDA(cudaMemcpyAsync(h->spare, x, h->grid_elems() * sizeof(float),
-                            cudaMemcpyDeviceToDevice, h->stream));
+    if (h->tag > 0xF0000000u) {  // tags would wrap: restart from clean buffers
+      EQ_CUDA(cudaMemsetAsync(h->wt, 0, 2 * h->grid_elems() * 8, h->stream));
+      EQ_CUDA(cudaMemsetAsync(h->edge, 0, (size_t)h->B * kMaxSweepsPerLaunch * h->P * 8,
+                              h->stream));
+      h->tag = 1;
+    }
+    {
+      const size_t n = h->grid_elems();
+      const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
+      eqk::k_ls_tag_init<<<blocks, 256, 0, h->stream>>>(h->wt, x, n, h->tag);
+      int rc0 = check_launch(h);
+      if (rc0) return rc0;
+    }
     eqk::LinSolveArgs A;
     A.x = x;
-    A.spare = h->spare;
+    A.wt[0] = h->wt;
+    A.wt[1] = h->wt + h->grid_elems();
+    A.tag0 = h->tag;
+    h->tag += (uint32_t)Kc + 1u;
     A.x0 = x0;
     A.code = h->code;
     A.rowfl = h->rowfl;
     A.colfl = h->colfl;
     A.edge = h->edge;
-    A.progress = h->progress;
     A.ticket = h->counters;
     A.done = h->counters + 1;
     A.err = h->err;
@@ -198,6 +218,12 @@ int launch_lin_solve(eq_fluid* h, int mode, float* x, const float* x0, float a, 
     A.a = a;
     A.c_recip = c_recip;
     const unsigned ntasks = (unsigned)(A.B * Kc);
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (h->profiling) {
+      EQ_CUDA(cudaEventCreate(&ev0));
+      EQ_CUDA(cudaEventCreate(&ev1));
+      EQ_CUDA(cudaEventRecord(ev0, h->stream));
+    }
     switch (mode) {
       case eqk::kRow:
         eqk::k_lin_solve<eqk::kRow><<<ntasks, 32, 0, h->stream>>>(A);
@@ -211,6 +237,10 @@ int launch_lin_solve(eq_fluid* h, int mode, float* x, const float* x0, float a, 
     }
     int rc = check_launch(h);
     if (rc) return rc;
+    if (h->profiling) {
+      EQ_CUDA(cudaEventRecord(ev1, h->stream));
+      h->ls_events.emplace_back(ev0, ev1);
+    }
   }
   return EQ_OK;
 }
@@ -301,13 +331,17 @@ void free_handle(eq_fluid* h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  for (auto& e : h->ls_events) {
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
   cudaFree(h->block);
   cudaFree(h->cells);
   cudaFree(h->code);
   cudaFree(h->rowfl);
   cudaFree(h->colfl);
   cudaFree(h->edge);
-  cudaFree(h->progress);
+  cudaFree(h->wt);
   cudaFree(h->counters);
   cudaFree(h->err);
   cudaFree(h->d_src);
@@ -335,22 +369,22 @@ int alloc_handle(uint32_t size, int device, eq_fluid** out) {
   if (cudaEventCreateWithFlags(&h->src_ev, cudaEventDisableTiming) != cudaSuccess)
     return bail(EQ_ERR_CUDA, "cudaEventCreate");
   const size_t g = h->grid_elems();
-  if (cudaMalloc(&h->block, 7 * g * sizeof(float)) != cudaSuccess)
+  if (cudaMalloc(&h->block, 6 * g * sizeof(float)) != cudaSuccess)
     return bail(EQ_ERR_OOM, "cudaMalloc (grids)");
   for (int f = 0; f < 6; ++f) h->field[f] = h->block + f * g;
-  h->spare = h->block + 6 * g;
   if (cudaMalloc(&h->cells, g) != cudaSuccess || cudaMalloc(&h->code, g) != cudaSuccess ||
       cudaMalloc(&h->rowfl, size) != cudaSuccess || cudaMalloc(&h->colfl, size) != cudaSuccess)
     return bail(EQ_ERR_OOM, "cudaMalloc (mask)");
   h->B = strips_for((int)size, kMaxSweepsPerLaunch);
   const size_t ntasks = (size_t)h->B * kMaxSweepsPerLaunch;
-  if (cudaMalloc(&h->edge, ntasks * h->P * sizeof(float)) != cudaSuccess ||
-      cudaMalloc(&h->progress, ntasks * sizeof(unsigned long long)) != cudaSuccess ||
+  if (cudaMalloc(&h->edge, ntasks * h->P * 8) != cudaSuccess ||
+      cudaMalloc(&h->wt, 2 * g * 8) != cudaSuccess ||
       cudaMalloc(&h->counters, 2 * sizeof(unsigned)) != cudaSuccess ||
       cudaMalloc(&h->err, sizeof(int)) != cudaSuccess)
     return bail(EQ_ERR_OOM, "cudaMalloc (wavefront state)");
-  if (cudaMemsetAsync(h->block, 0, 7 * g * sizeof(float), h->stream) != cudaSuccess ||
-      cudaMemsetAsync(h->progress, 0, ntasks * sizeof(unsigned long long), h->stream) != cudaSuccess ||
+  if (cudaMemsetAsync(h->block, 0, 6 * g * sizeof(float), h->stream) != cudaSuccess ||
+      cudaMemsetAsync(h->wt, 0, 2 * g * 8, h->stream) != cudaSuccess ||
+      cudaMemsetAsync(h->edge, 0, ntasks * h->P * 8, h->stream) != cudaSuccess ||
       cudaMemsetAsync(h->counters, 0, 2 * sizeof(unsigned), h->stream) != cudaSuccess ||
       cudaMemsetAsync(h->err, 0, sizeof(int), h->stream) != cudaSuccess)
     return bail(EQ_ERR_CUDA, "cudaMemsetAsync");
@@ -414,8 +448,6 @@ int read_err_word(eq_fluid* h) {
   EQ_CUDA(cudaStreamSynchronize(h->stream));
   if (e != 0) {
     // Leave the wavefront state clean for the next launch.
-    const size_t ntasks = (size_t)h->B * kMaxSweepsPerLaunch;
-    EQ_CUDA(cudaMemsetAsync(h->progress, 0, ntasks * sizeof(unsigned long long), h->stream));
     EQ_CUDA(cudaMemsetAsync(h->counters, 0, 2 * sizeof(unsigned), h->stream));
     EQ_CUDA(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
     EQ_CUDA(cudaStreamSynchronize(h->stream));
@@ -784,6 +816,38 @@ int eq_fluid_device_field(eq_fluid* h, int field, float** dptr, uint32_t* pitch_
 int eq_fluid_launch_count(const eq_fluid* h, uint64_t* count) {
   if (!h || !count) return fail(EQ_ERR_ARG, "null argument");
   *count = h->launches;
+  return EQ_OK;
+}
+
+int eq_fluid_get_stream(eq_fluid* h, void** stream) {
+  if (!h || !stream) return fail(EQ_ERR_ARG, "null argument");
+  *stream = (void*)h->stream;
+  return EQ_OK;
+}
+
+int eq_fluid_set_profiling(eq_fluid* h, int enable) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  h->profiling = enable != 0;
+  return EQ_OK;
+}
+
+int eq_fluid_kernel_stats(eq_fluid* h, int kernel, double* total_ms, uint64_t* launches) {
+  if (!h || !total_ms || !launches) return fail(EQ_ERR_ARG, "null argument");
+  if (kernel != 0) return fail(EQ_ERR_ARG, "unknown kernel id");
+  int rc = select_device(h);
+  if (rc) return rc;
+  EQ_CUDA(cudaStreamSynchronize(h->stream));
+  double sum = 0.0;
+  for (auto& e : h->ls_events) {
+    float ms = 0.f;
+    EQ_CUDA(cudaEventElapsedTime(&ms, e.first, e.second));
+    sum += ms;
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
+  *total_ms = sum;
+  *launches = h->ls_events.size();
+  h->ls_events.clear();
   return EQ_OK;
 }
 

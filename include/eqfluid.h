@@ -212,6 +212,17 @@ int eq_fluid_launch_count(const eq_fluid* h, uint64_t* count);
  * cannot complete end with EQ_ERR_TIMEOUT sooner. */
 int eq_fluid_set_spin_limit(eq_fluid* h, int64_t iterations);
 
+/* The handle's CUDA stream (a cudaStream_t), for callers that order their own
+ * work or events against the handle's launches. */
+int eq_fluid_get_stream(eq_fluid* h, void** stream);
+
+/* Kernel timing: while enabled, every lin_solve wavefront launch is bracketed
+ * by CUDA events on the handle's stream. eq_fluid_kernel_stats synchronises,
+ * returns the summed device time (ms) and the launch count since the last
+ * reset, and resets. `kernel` 0 = the lin_solve wavefront. */
+int eq_fluid_set_profiling(eq_fluid* h, int enable);
+int eq_fluid_kernel_stats(eq_fluid* h, int kernel, double* total_ms, uint64_t* launches);
+
 /* Message for the calling thread's last non-zero status ("" if none). */
 const char* eq_last_error(void);
 
