@@ -80,6 +80,13 @@ def scene(seed=SEED, nframes=1):
             gauss[..., 1].astype(np.float32))
 
 
+def replicas_value(local_seconds: float, steps: int, world: int, reduce_max=None):
+    """Whole-job cell-steps/s of `world` independent replicas: every rank ran
+    `steps` frames; the job time is the slowest rank's (max over ranks)."""
+    t = reduce_max(local_seconds) if (reduce_max and world > 1) else local_seconds
+    return world * N * N * steps / t, t
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(
         os.environ.get("WORLD_SIZE", 1))
@@ -287,14 +294,14 @@ def run_ours(args):
     _lib.check(L.eq_fluid_kernel_stats(fl.handle, 0, ctypes.byref(ls_ms), ctypes.byref(ls_n)))
     _lib.check(L.eq_fluid_set_profiling(fl.handle, 0))
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-    dev_s = sum(step_ms) / 1e3
-    if world > 1:
+    def reduce_max(x):
         import torch.distributed as dist
-        t = torch.tensor([dev_s], device=dev)
+        t = torch.tensor([x], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s = float(t.item())
+        return float(t.item())
+
+    value, dev_s = replicas_value(sum(step_ms) / 1e3, args.steps, world, reduce_max)
     ms_per_step = dev_s / args.steps * 1e3
-    value = world * N * N * args.steps / dev_s
 
     # ---- end to end through the C ABI with host buffers
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
@@ -318,13 +325,7 @@ def run_ours(args):
         for f_idx, buf in zip((_lib.FIELD_DENSITY, _lib.FIELD_VX, _lib.FIELD_VY), outs):
             _lib.check(L.eq_fluid_read_field(fl.handle, f_idx, buf.data_ptr(), SIZE * SIZE))
         e2e_times.append(time.perf_counter() - t0)
-    e2e_s = sum(e2e_times)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * N * N * args.steps / e2e_s
+    e2e_value, e2e_s = replicas_value(sum(e2e_times), args.steps, world, reduce_max)
     assert np.isfinite(outs[0].numpy()).all()
 
     if rank != 0:

@@ -189,6 +189,7 @@ int launch_lin_solve(eq_fluid* h, int mode, float* x, const float* x0, float a, 
                               h->stream));
       h->tag = 1;
     }
+    EQ_CUDA(cudaMemsetAsync(h->counters, 0, 2 * sizeof(unsigned), h->stream));
     {
       const size_t n = h->grid_elems();
       const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 8);

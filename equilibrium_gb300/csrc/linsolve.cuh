@@ -53,8 +53,8 @@ struct LinSolveArgs {
   const uint8_t* rowfl;
   const uint8_t* colfl;
   unsigned long long* edge;    // [ntasks][P] tagged raw last-row values
-  unsigned* ticket;            // zero on entry, reset on exit
-  unsigned* done;              // zero on entry, reset on exit
+  unsigned* ticket;            // zeroed by the host before every launch
+  unsigned* done;              // zeroed by the host before every launch
   int* err;                    // device error word
   long long spin_limit;
   unsigned tag0;               // tag of W(-1)
@@ -104,6 +104,10 @@ __global__ void __launch_bounds__(32) k_lin_solve(LinSolveArgs A) {
   if (lane == 0) t = atomicAdd(A.ticket, 1u);
   t = __shfl_sync(FULL, t, 0);
   const int K = A.K, S = A.S, P = A.P, N = S - 2;
+  if (t >= (unsigned)(A.B * K)) {  // counters not reset: never index past the tasks
+    if (lane == 0) atomicExch(A.err, 5 /* EQ_ERR_STATE */);
+    return;
+  }
   const int b = (int)(t / (unsigned)K), k = (int)(t % (unsigned)K);
   const int j = 32 * b + lane - 2 * k - 2;
   const unsigned tagIn = A.tag0 + (unsigned)k;  // tag of W(k-1)
@@ -382,7 +386,7 @@ __global__ void __launch_bounds__(32) k_lin_solve(LinSolveArgs A) {
   }
   cp_async_wait<0>();
 
-  // ---- completion; the last task computes the corners and resets the counters
+  // ---- completion; the last task computes the corners (no sweep reads them)
   __syncwarp();
   unsigned prev = 0;
   if (lane == 0) {
@@ -393,11 +397,7 @@ __global__ void __launch_bounds__(32) k_lin_solve(LinSolveArgs A) {
   const unsigned ntasks = (unsigned)(A.B * A.K);
   if (prev == ntasks - 1) {
     __threadfence();
-    if (lane == 0) {
-      corners<MODE>(A.x, A.rowfl, A.colfl, S, P);
-      *A.ticket = 0u;
-      *A.done = 0u;
-    }
+    if (lane == 0) corners<MODE>(A.x, A.rowfl, A.colfl, S, P);
   }
 }
 
