@@ -860,3 +860,7 @@ int eq_fluid_set_spin_limit(eq_fluid* h, int64_t iterations) {
 }
 
 }  // extern "C"
+
+// The allocation-free lin_solve entry point and its static scratch, compiled
+// in this translation unit (it shares the kernels above).
+#include "noalloc.cu"

@@ -199,6 +199,28 @@ int eq_fluid_project(eq_fluid* h, int vx_field, int vy_field, int p_field, int d
 int eq_fluid_advect(eq_fluid* h, int mode, int d_field, int d0_field, int u_field,
                     int v_field);
 
+/* ---- lin_solve that allocates nothing ----------------------------------- */
+
+/* No counterpart in the reference. lin_solve (the same kernels, the same
+ * bit-exact result as eq_fluid_lin_solve) for callers that cannot allocate
+ * device memory: code inside an open CUDA stream capture, where cudaMalloc is
+ * not allowed; frame loops that must not take the implicit device
+ * synchronisation cudaMalloc / cudaFree can cause; hosts whose GPU memory is
+ * owned by another allocator. The caller passes device pointers to x (in/out),
+ * x0 and the wall mask (1 = DefaultWall, ghost frame all walls), each `size`
+ * rows with a row pitch of `pitch` elements (pitch % 4 == 0, buffers 16-byte
+ * aligned), and the stream to run on (NULL = legacy default stream).
+ * All scratch lives in one static device array sized for
+ * size <= 258 and pitch <= 288 (about 3.2 MB per GPU that loads the library,
+ * held until exit); larger grids return EQ_ERR_ARG. The first call on a device
+ * (that device current) looks the array up and clears it: make it before any
+ * stream capture. Every call shares the array, so calls that overlap on the
+ * GPU race. Synchronises `stream` before returning (to report the device
+ * error word: EQ_ERR_TIMEOUT, or EQ_ERR_ARG if the frame is not all walls). */
+int eq_lin_solve_noalloc(int mode, float* x, const float* x0, const uint8_t* cells,
+                         uint32_t size, uint32_t pitch, int64_t iters, float a, float c,
+                         void* stream);
+
 /* ---- diagnostics ------------------------------------------------------- */
 
 /* Device pointer of a field (pitched rows) and the row pitch in elements. */
