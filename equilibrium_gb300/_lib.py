@@ -31,6 +31,12 @@ class SimulationConfigsC(ctypes.Structure):
                 ("size", ctypes.c_uint32)]
 
 
+class SceneDescC(ctypes.Structure):
+    _fields_ = [("size", ctypes.c_uint32), ("delta_t", ctypes.c_float),
+                ("frames", ctypes.c_int64), ("diffusion", ctypes.c_float),
+                ("viscousity", ctypes.c_float)]
+
+
 class FluidConfigsC(ctypes.Structure):
     _fields_ = [("diffusion", ctypes.c_float), ("viscousity", ctypes.c_float),
                 ("has_perlin_noise", ctypes.c_int32)]
@@ -101,6 +107,26 @@ def load(path: str = LIB_PATH):
         "eq_fluid_set_profiling": (i32, [H, i32]),
         "eq_fluid_kernel_stats": (i32, [H, i32, ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_uint64)]),
+        "eq_batch_new": (i32, [i64, ctypes.POINTER(SceneDescC), i32, PP]),
+        "eq_batch_free": (i32, [H]),
+        "eq_batch_scene_count": (i32, [H, ctypes.POINTER(ctypes.c_int64)]),
+        "eq_batch_cell_count": (i32, [H, ctypes.POINTER(ctypes.c_uint64)]),
+        "eq_batch_fill_obstacle": (i32, [H, i64, i64, i64, i64, i64]),
+        "eq_batch_read_cells": (i32, [H, i64, P, u64]),
+        "eq_batch_set_sources": (i32, [H, i64, i64, P, P, P, P, P]),
+        "eq_batch_read_field": (i32, [H, i64, i32, P, u64]),
+        "eq_batch_write_field": (i32, [H, i64, i32, P, u64]),
+        "eq_batch_step": (i32, [H, i64]),
+        "eq_batch_step_eager": (i32, [H, i64]),
+        "eq_batch_synchronize": (i32, [H]),
+        "eq_batch_lin_solve": (i32, [H, i32, i32, i32, f32, f32]),
+        "eq_batch_set_tuning": (i32, [H, i32, i32]),
+        "eq_batch_get_tuning": (i32, [H, ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_int)]),
+        "eq_batch_autotune": (i32, [H, i32, ctypes.POINTER(ctypes.c_double), i32,
+                                    ctypes.POINTER(ctypes.c_int)]),
+        "eq_batch_get_stream": (i32, [H, PP]),
+        "eq_batch_launch_count": (i32, [H, ctypes.POINTER(ctypes.c_uint64)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)

@@ -98,20 +98,19 @@ int check_mode(int m) {
   return (m >= 0 && m <= 2) ? EQ_OK : fail(EQ_ERR_ARG, "mode out of range");
 }
 
-// Derives the per-cell boundary codes and the row/column fluid flags from the
-// host mask and uploads mask + codes.
-int upload_mask(eq_fluid* h) {
-  if (!h->mask_dirty) return EQ_OK;
-  const int S = (int)h->S, P = h->P, N = S - 2;
-  const std::vector<uint8_t>& m = h->host_cells;
+// Derives the per-cell boundary codes (pitched, P per row) and the row /
+// column "has a fluid cell" flags from a dense size*size wall mask.
+void derive_codes(const std::vector<uint8_t>& m, int S, int P, uint8_t* code, uint8_t* rowfl,
+                  uint8_t* colfl) {
+  const int N = S - 2;
   auto wall = [&](int i, int j) { return m[(size_t)j * S + i] != 0; };
-  std::vector<uint8_t> code((size_t)P * S, 0), cellsP((size_t)P * S, 0), rowfl(S, 0),
-      colfl(S, 0);
+  std::memset(code, 0, (size_t)P * S);
+  std::memset(rowfl, 0, S);
+  std::memset(colfl, 0, S);
   for (int j = 0; j < S; ++j) {
     for (int i = 0; i < S; ++i) {
       uint8_t c = 0;
       const bool w = wall(i, j);
-      cellsP[(size_t)j * P + i] = w ? 1 : 0;
       if (w) c |= eqk::kCodeWall;
       if (!w && i >= 1 && i <= N && j >= 1 && j <= N) {
         rowfl[j] = 1;
@@ -135,6 +134,18 @@ int upload_mask(eq_fluid* h) {
   for (int j = 0; j < S; ++j)
     for (int i = 0; i < S; ++i)
       if (colfl[i]) code[(size_t)j * P + i] |= eqk::kCodeColFluid;
+}
+
+// Uploads the mask and its derived codes / flags when the mask changed.
+int upload_mask(eq_fluid* h) {
+  if (!h->mask_dirty) return EQ_OK;
+  const int S = (int)h->S, P = h->P;
+  const std::vector<uint8_t>& m = h->host_cells;
+  std::vector<uint8_t> code((size_t)P * S, 0), cellsP((size_t)P * S, 0), rowfl(S, 0),
+      colfl(S, 0);
+  for (int j = 0; j < S; ++j)
+    for (int i = 0; i < S; ++i) cellsP[(size_t)j * P + i] = m[(size_t)j * S + i] ? 1 : 0;
+  derive_codes(m, S, P, code.data(), rowfl.data(), colfl.data());
   EQ_CUDA(cudaMemcpyAsync(h->cells, cellsP.data(), cellsP.size(), cudaMemcpyHostToDevice,
                           h->stream));
   EQ_CUDA(cudaMemcpyAsync(h->code, code.data(), code.size(), cudaMemcpyHostToDevice,
@@ -864,3 +875,6 @@ int eq_fluid_set_spin_limit(eq_fluid* h, int64_t iterations) {
 // The allocation-free lin_solve entry point and its static scratch, compiled
 // in this translation unit (it shares the kernels above).
 #include "noalloc.cu"
+
+// The batched form (many scenes per launch).
+#include "batch.cu"

@@ -199,6 +199,79 @@ int eq_fluid_project(eq_fluid* h, int vx_field, int vy_field, int p_field, int d
 int eq_fluid_advect(eq_fluid* h, int mode, int d_field, int d0_field, int u_field,
                     int v_field);
 
+/* ---- batches of independent scenes -------------------------------------- */
+
+/* Many independent Fluid states (fluid.rs:52-81), each with its own size,
+ * delta_t, sweep count (`frames`), diffusion and viscousity, advanced
+ * together: eq_batch_step runs Fluid::step (fluid.rs:437-524) once per frame
+ * on every scene. The reference has one Fluid per simulation thread
+ * (renderer.rs:125-128); a batch replaces N such threads. Every scene's result
+ * is bit-identical to stepping an eq_fluid of the same configs (and to the
+ * reference's f32 step): a scene is computed by one thread block with the
+ * reference's operation order, and scenes never interact. */
+typedef struct eq_scene_desc {
+  uint32_t size; /* cells per side including the ghost frame, >= 20 */
+  float delta_t;
+  int64_t frames; /* Gauss-Seidel sweeps per lin_solve (fluid.rs:312) */
+  float diffusion;
+  float viscousity;
+} eq_scene_desc;
+
+typedef struct eq_batch eq_batch; /* opaque; owns device state */
+
+/* Creates `nscenes` scenes, each in the Fluid::new state (fluid.rs:93-110:
+ * init() once, frame = DefaultWall). `device` < 0 = current device. */
+int eq_batch_new(int64_t nscenes, const eq_scene_desc* scenes, int device, eq_batch** out);
+int eq_batch_free(eq_batch* b); /* accepts NULL */
+int eq_batch_scene_count(const eq_batch* b, int64_t* n);
+/* Sum over scenes of (size-2)^2: the interior cells one frame advances. */
+int eq_batch_cell_count(const eq_batch* b, uint64_t* interior_cells);
+
+/* fill_obstacle (fluid.rs:610-619) on one scene: [x0,x1) x [y0,y1) walls. */
+int eq_batch_fill_obstacle(eq_batch* b, int64_t scene, int64_t x0, int64_t y0, int64_t x1,
+                           int64_t y1);
+int eq_batch_read_cells(eq_batch* b, int64_t scene, uint8_t* host, uint64_t n);
+
+/* Per-scene sources applied before every step, in array order:
+ * add_density(x, y, density) then add_velocity(x, y, vx, vy) for each s
+ * (fluid.rs:120-131). NULL value arrays count as zeros; n = 0 clears. */
+int eq_batch_set_sources(eq_batch* b, int64_t scene, int64_t n, const uint32_t* x,
+                         const uint32_t* y, const float* density, const float* vx,
+                         const float* vy);
+
+/* Dense size*size copies of one scene's field (synchronous). */
+int eq_batch_read_field(eq_batch* b, int64_t scene, int field, float* host, uint64_t n);
+int eq_batch_write_field(eq_batch* b, int64_t scene, int field, const float* host,
+                         uint64_t n);
+
+/* `nframes` frames of every scene: one persistent kernel launch per frame
+ * (thread blocks take scenes from a work queue, largest first), the whole
+ * sequence captured once into a CUDA graph and replayed (the graph is kept
+ * for the next call with the same nframes and tuning). Asynchronous. */
+int eq_batch_step(eq_batch* b, int64_t nframes);
+/* The same frames launched directly (no graph). */
+int eq_batch_step_eager(eq_batch* b, int64_t nframes);
+int eq_batch_synchronize(eq_batch* b);
+
+/* One lin_solve (fluid.rs:301-325) of field x_field from x0_field on every
+ * scene with each scene's sweep count, by the same block solver. */
+int eq_batch_lin_solve(eq_batch* b, int mode, int x_field, int x0_field, float a, float c);
+
+/* Tuning: sweeps per wavefront pass (warps per thread block, 1..20; a
+ * lin_solve of K sweeps takes ceil(K / sweeps_per_pass) passes) and thread
+ * blocks per SM. The default is min(max K, 20) and 1. */
+int eq_batch_set_tuning(eq_batch* b, int sweeps_per_pass, int blocks_per_sm);
+int eq_batch_get_tuning(const eq_batch* b, int* sweeps_per_pass, int* blocks_per_sm);
+
+/* Autotuner: times `trial_frames` frames for every candidate tuning from a
+ * snapshot of the state (restored after each trial, so the simulation state
+ * is unchanged), keeps the fastest. ms_out[q] (q < cap) receives candidate q's
+ * ms per frame (0 if it does not fit); *ncand the candidate count. */
+int eq_batch_autotune(eq_batch* b, int trial_frames, double* ms_out, int cap, int* ncand);
+
+int eq_batch_get_stream(eq_batch* b, void** stream);
+int eq_batch_launch_count(const eq_batch* b, uint64_t* count);
+
 /* ---- lin_solve that allocates nothing ----------------------------------- */
 
 /* No counterpart in the reference. lin_solve (the same kernels, the same

@@ -1,0 +1,194 @@
+"""The batched form (eq_batch_*) against the oracle, bit for bit.
+
+Each scene of a batch is computed by one thread block (a block-level temporal
+wavefront for every lin_solve), so every scene must equal the reference's f32
+step of that scene exactly: all six arrays, ghost cells included.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from equilibrium_gb300 import _lib
+from equilibrium_gb300.batch import Batch, SceneConfig
+from equilibrium_gb300.simulation import Fluid, FluidConfigs, SimulationConfigs
+from tests.util import assert_bitexact, random_rects
+
+pytestmark = pytest.mark.gpu
+
+ROW, COL, PAS = _lib.MODE_ADJUST_ROW, _lib.MODE_ADJUST_COLUMN, _lib.MODE_PASSIVE
+SC, DE, VX, VY, VX0, VY0 = range(6)
+
+
+def make_pair(cfgs, rects_per_scene, seed=0, randomize=True, vel_scale=1.0):
+    """A batch and one oracle scene per batch scene, in the same state."""
+    b = Batch(cfgs)
+    refs = []
+    rng = np.random.default_rng(seed)
+    for s, (c, rects) in enumerate(zip(cfgs, rects_per_scene)):
+        r = oracle.OracleFluid(c.size, c.delta_t, c.frames, c.diffusion, c.viscousity)
+        for rc in rects:
+            r.fill_obstacle(*rc)
+            b.fill_obstacle(s, *rc)
+        assert np.array_equal(b.cells(s), r.cells)
+        if randomize:
+            n = c.size * c.size
+            for f in range(6):
+                lo, hi = ((-vel_scale, vel_scale) if f in (VX, VY, VX0, VY0) else (0.0, 2.0))
+                r.fields[f][:] = rng.uniform(lo, hi, n).astype(np.float32)
+                b.write_field(s, f, r.fields[f])
+        else:
+            for f in range(6):
+                assert_bitexact(b.read_field(s, f), r.fields[f], f"init scene {s} field {f}",
+                                c.size)
+        refs.append(r)
+    return b, refs
+
+
+def compare(b, refs, what, fields=range(6)):
+    for s, r in enumerate(refs):
+        for f in fields:
+            assert_bitexact(b.read_field(s, f), r.fields[f],
+                            f"{what} scene {s} (size {r.size}, K {r.frames}) field "
+                            f"{oracle.FIELDS[f]}", r.size)
+
+
+SIZES_K = [(20, 1), (21, 2), (23, 3), (34, 20), (40, 7), (66, 20), (97, 13), (130, 20),
+           (33, 0), (64, 33)]
+
+
+def scene_rects(rng, size, kind):
+    if kind == 0:
+        return []
+    if kind == 1:
+        return random_rects(rng, size, 4)
+    if kind == 2:
+        return [(0, 5, 4, 9), (size - 4, 2, size, 6), (6, 0, 9, 3), (3, size - 3, 8, size)]
+    if kind == 3:
+        return [(x, y, x + 1, y + 1) for x in range(2, size - 2, 3) for y in range(2, size - 2, 3)]
+    return [(0, size // 2, size, size // 2 + 1), (size // 3, 0, size // 3 + 2, size)]
+
+
+@pytest.mark.parametrize("mode", [ROW, COL, PAS])
+@pytest.mark.parametrize("tuning", [None, (3, 1), (1, 1), (10, 2)])
+def test_batch_lin_solve(eqlib, mode, tuning):
+    rng = np.random.default_rng(11 + mode)
+    cfgs = [SceneConfig(s, 0.1, k) for s, k in SIZES_K]
+    rects = [scene_rects(rng, c.size, q % 5) for q, c in enumerate(cfgs)]
+    b, refs = make_pair(cfgs, rects, seed=mode)
+    if tuning:
+        b.set_tuning(*tuning)
+    a = np.float32(0.37)
+    c = np.float32(1.0) + np.float32(4.0) * a
+    b.lin_solve(mode, VX0, VX, a, c)
+    for r in refs:
+        oracle.lin_solve(mode, r.fields[VX0], r.fields[VX], a, c, r.size, r.frames, r.cells)
+    compare(b, refs, f"batch lin_solve mode={mode} tuning={tuning}", [VX0, VX])
+    b.close()
+
+
+@pytest.mark.parametrize("tuning", [None, (4, 1), (10, 2)])
+def test_batch_frames_random_state(eqlib, tuning):
+    rng = np.random.default_rng(3)
+    cfgs = [SceneConfig(s, 0.1, k, 1e-3, 2e-3) for s, k in SIZES_K]
+    rects = [scene_rects(rng, c.size, (q + 1) % 5) for q, c in enumerate(cfgs)]
+    b, refs = make_pair(cfgs, rects, seed=5, vel_scale=2.0)
+    if tuning:
+        b.set_tuning(*tuning)
+    for fr in range(3):
+        b.step(1)
+        for r in refs:
+            r.step()
+        compare(b, refs, f"batch frame {fr} tuning={tuning}")
+    b.close()
+
+
+def test_batch_init_sources_and_graph_replay(eqlib):
+    """Fluid::new state, per-scene sources every frame, a 4-frame graph replayed
+    twice (8 frames), the eager path for 2 more."""
+    rng = np.random.default_rng(21)
+    cfgs = [SceneConfig(66, 0.1, 20, 1e-4, 1e-4), SceneConfig(41, 0.05, 5, 1e-5, 3e-4),
+            SceneConfig(128, 0.02, 16, 0.0, 1e-3), SceneConfig(20, 0.2, 2, 1e-3, 1e-3)]
+    rects = [[(20, 30, 40, 45)], random_rects(rng, 41, 3), [(80, 80, 110, 110)], []]
+    b, refs = make_pair(cfgs, rects, randomize=False)
+    srcs = []
+    for s, c in enumerate(cfgs):
+        n = 5
+        xs = rng.integers(1, c.size - 1, n).astype(np.uint32)
+        ys = rng.integers(1, c.size - 1, n).astype(np.uint32)
+        xs[1] = xs[0]
+        ys[1] = ys[0]  # a repeated cell accumulates in array order
+        d = rng.uniform(0, 100, n).astype(np.float32)
+        u = rng.uniform(-5, 5, n).astype(np.float32)
+        v = rng.uniform(-5, 5, n).astype(np.float32)
+        b.set_sources(s, xs, ys, d, u, v)
+        srcs.append((xs, ys, d, u, v))
+    b.step(4)
+    b.step(4)
+    b.step(2, graph=False)
+    for s, r in enumerate(refs):
+        xs, ys, d, u, v = srcs[s]
+        r.run(10, np.tile(xs, (10, 1)), np.tile(ys, (10, 1)), np.tile(d, (10, 1)),
+              np.tile(u, (10, 1)), np.tile(v, (10, 1)))
+    compare(b, refs, "batch 10 frames with sources")
+    b.close()
+
+
+def test_batch_matches_plain_handle(eqlib):
+    """A scene stepped in a batch equals the same scene stepped by an eq_fluid
+    handle (the plain kernels), at a size where the plain path uses many
+    blocks per lin_solve."""
+    size, iters = 258, 20
+    rects = [(30, 40, 90, 70), (150, 150, 200, 240), (0, 120, 20, 140)]
+    b = Batch([SceneConfig(size, 0.05, iters, 1e-5, 1e-5), SceneConfig(50, 0.1, 3)])
+    g = Fluid(FluidConfigs(1e-5, 1e-5, False), SimulationConfigs(0.05, iters, size))
+    for rc in rects:
+        b.fill_obstacle(0, *rc)
+        assert _lib.load().eq_fluid_fill_obstacle(g.handle, *rc) == 0
+    xs = np.array([100, 101, 129], dtype=np.uint32)
+    ys = np.array([100, 100, 200], dtype=np.uint32)
+    d = np.array([40.0, 10.0, 25.0], dtype=np.float32)
+    u = np.array([3.0, -2.0, 0.5], dtype=np.float32)
+    v = np.array([-1.0, 4.0, 2.5], dtype=np.float32)
+    b.set_sources(0, xs, ys, d, u, v)
+    for _ in range(3):
+        g.add_sources(xs, ys, d, u, v)
+        g.step()
+    b.step(3)
+    g.synchronize()
+    for f in range(6):
+        assert_bitexact(b.read_field(0, f), g.read_field(f), f"batch vs plain field {f}", size)
+    g.close()
+    b.close()
+
+
+def test_batch_autotune_keeps_state(eqlib):
+    rng = np.random.default_rng(8)
+    cfgs = [SceneConfig(int(s), 0.1, 20) for s in rng.integers(20, 200, 24)]
+    rects = [random_rects(rng, c.size, 2) for c in cfgs]
+    b, refs = make_pair(cfgs, rects, randomize=False)
+    ms = b.autotune(trial_frames=1)
+    assert len(ms) >= 2 and min(m for m in ms if m > 0) > 0
+    nw, bps = b.tuning()
+    assert 1 <= nw <= 20 and bps in (1, 2)
+    compare(b, refs, "after autotune (state restored)")
+    b.step(2)
+    for r in refs:
+        r.step()
+        r.step()
+    compare(b, refs, f"after autotune + 2 frames (tuning {nw},{bps})")
+    b.close()
+
+
+def test_batch_rejects_bad_arguments(eqlib):
+    with pytest.raises(_lib.EqError):
+        Batch([SceneConfig(19)])
+    b = Batch([SceneConfig(30)])
+    with pytest.raises(_lib.EqError):
+        b.read_field(1, 0)
+    with pytest.raises(_lib.EqError):
+        b.set_tuning(21, 1)
+    with pytest.raises(_lib.EqError):
+        b.set_tuning(20, 4)
+    with pytest.raises(_lib.EqError):
+        b.lin_solve(PAS, 1, 1, 1.0, 4.0)
+    b.close()
