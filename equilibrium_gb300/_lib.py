@@ -120,6 +120,10 @@ def load(path: str = LIB_PATH):
         "eq_batch_step_eager": (i32, [H, i64]),
         "eq_batch_synchronize": (i32, [H]),
         "eq_batch_lin_solve": (i32, [H, i32, i32, i32, f32, f32]),
+        "eq_batch_diffuse": (i32, [H, i32, i32, i32, f32]),
+        "eq_batch_project": (i32, [H, i32, i32, i32, i32]),
+        "eq_batch_advect": (i32, [H, i32, i32, i32, i32, i32]),
+        "eq_batch_set_boundaries": (i32, [H, i32, i32]),
         "eq_batch_set_tuning": (i32, [H, i32, i32]),
         "eq_batch_get_tuning": (i32, [H, ctypes.POINTER(ctypes.c_int),
                                       ctypes.POINTER(ctypes.c_int)]),

@@ -104,6 +104,19 @@ class Batch:
         check(_lib.load().eq_batch_lin_solve(self.handle, mode, x_field, x0_field,
                                              np.float32(a), np.float32(c)))
 
+    def diffuse(self, mode: int, x_field: int, x0_field: int, diffusion: float):
+        check(_lib.load().eq_batch_diffuse(self.handle, mode, x_field, x0_field,
+                                           np.float32(diffusion)))
+
+    def project(self, vx: int, vy: int, p: int, div: int):
+        check(_lib.load().eq_batch_project(self.handle, vx, vy, p, div))
+
+    def advect(self, mode: int, d: int, d0: int, u: int, v: int):
+        check(_lib.load().eq_batch_advect(self.handle, mode, d, d0, u, v))
+
+    def set_boundaries(self, mode: int, field: int):
+        check(_lib.load().eq_batch_set_boundaries(self.handle, mode, field))
+
     def synchronize(self):
         check(_lib.load().eq_batch_synchronize(self.handle))
 

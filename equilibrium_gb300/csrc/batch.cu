@@ -40,8 +40,6 @@ struct eq_batch {
   uint32_t* d_sy = nullptr;
   float* d_sval = nullptr;  // d, u, v (3 x total)
   int64_t src_cap = 0;
-  float* gscratch = nullptr;
-  size_t gscratch_floats = 0;
 
   int nwmax = 20;  // sweeps per wavefront pass = warps per block
   int bps = 1;     // blocks per SM
@@ -78,7 +76,6 @@ void batch_free(eq_batch* b) {
   cudaFree(b->d_sx);
   cudaFree(b->d_sy);
   cudaFree(b->d_sval);
-  cudaFree(b->gscratch);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -186,52 +183,76 @@ int batch_upload_sources(eq_batch* b) {
 
 int batch_cs(const eq_batch* b) { return ((b->smax + 3) / 4) * 4; }
 
-// Launch shape for the current tuning: blocks, threads, dynamic shared memory
-// and whether the carry / edge rows fit in shared memory.
+// Launch shape for the current tuning: blocks, threads and dynamic shared
+// memory (the wavefront's ring, carry and edge rows).
 struct BLaunch {
   int blocks, threads;
   size_t smem;
-  bool bufs_smem;
 };
 
-int batch_launch_shape(eq_batch* b, BLaunch* L) {
-  const int cs = batch_cs(b);
-  const size_t ring = eqk::batch_ring_floats(b->nwmax) * 4;
-  const size_t bufs = eqk::batch_bufs_floats(b->nwmax, cs) * 4;
+size_t batch_smem_budget(const eq_batch* b, int bps) {
   // per-block budget with bps blocks per SM (1 KB per block is reserved)
-  const size_t budget =
-      std::min(b->max_smem_block, b->max_smem_sm / (size_t)b->bps - 1024);
-  L->threads = 32 * b->nwmax;
-  L->bufs_smem = ring + bufs <= budget;
-  L->smem = L->bufs_smem ? ring + bufs : ring;
-  if (L->smem > budget) return fail(EQ_ERR_ARG, "wavefront ring does not fit in shared memory");
+  return std::min(b->max_smem_block, b->max_smem_sm / (size_t)bps - 1024);
+}
+
+size_t batch_smem_bytes(const eq_batch* b, int nw) {
+  return eqk::wave_smem_floats(nw, batch_cs(b)) * sizeof(float);
+}
+
+int batch_launch_shape(eq_batch* b, BLaunch* L) {
+  L->threads = 32 * (b->nwmax + 1);  // + the wavefront's loader warp
+  L->smem = batch_smem_bytes(b, b->nwmax);
+  if (L->smem > batch_smem_budget(b, b->bps))
+    return fail(EQ_ERR_ARG, "the wavefront buffers do not fit in shared memory at this tuning");
   L->blocks = (int)std::min<int64_t>(b->n, (int64_t)b->num_sms * b->bps);
   if (L->blocks < 1) L->blocks = 1;
-  if (!L->bufs_smem) {
-    const size_t need = (size_t)L->blocks * eqk::batch_bufs_floats(b->nwmax, cs);
-    if (need > b->gscratch_floats) {
-      EQ_CUDA(cudaStreamSynchronize(b->stream));
-      batch_drop_graph(b);  // a captured graph holds the old scratch pointer
-      cudaFree(b->gscratch);
-      b->gscratch = nullptr;
-      b->gscratch_floats = 0;
-      if (cudaMalloc(&b->gscratch, need * 4) != cudaSuccess)
-        return fail(EQ_ERR_OOM, "cudaMalloc (batch scratch)");
-      b->gscratch_floats = need;
-    }
-  }
-  EQ_CUDA(cudaFuncSetAttribute(eqk::k_batch_frame, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  EQ_CUDA(cudaFuncSetAttribute(eqk::k_batch_run, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)L->smem));
-  EQ_CUDA(cudaFuncSetAttribute(eqk::k_batch_lin_solve<eqk::kRow>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem));
-  EQ_CUDA(cudaFuncSetAttribute(eqk::k_batch_lin_solve<eqk::kCol>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem));
-  EQ_CUDA(cudaFuncSetAttribute(eqk::k_batch_lin_solve<eqk::kPassive>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem));
   return EQ_OK;
 }
 
+// The operation list of one frame: Fluid::step (fluid.rs:437-524) with the
+// reference's aliasing (project's p and div are the other pair of velocity
+// arrays), preceded by the scene's sources.
+eqk::BOpList batch_frame_ops() {
+  eqk::BOpList L;
+  L.n = 0;
+  auto add = [&](int kind, int mode, int f0, int f1, int f2, int f3, int coef, float a,
+                 float c) {
+    eqk::BOp& o = L.op[L.n++];
+    o.kind = kind;
+    o.mode = mode;
+    o.f[0] = f0;
+    o.f[1] = f1;
+    o.f[2] = f2;
+    o.f[3] = f3;
+    o.coef = coef;
+    o.a = a;
+    o.c = c;
+  };
+  const int SC = EQ_FIELD_SCRATCH, DE = EQ_FIELD_DENSITY, VX = EQ_FIELD_VX, VY = EQ_FIELD_VY,
+            VX0 = EQ_FIELD_VX0, VY0 = EQ_FIELD_VY0;
+  add(eqk::kOpSources, 0, 0, 0, 0, 0, 0, 0.f, 0.f);
+  add(eqk::kOpDiffuse, eqk::kRow, VX0, VX, 0, 0, 0, 0.f, 0.f);  // diffuse(1, vx0, vx, visc)
+  add(eqk::kOpDiffuse, eqk::kCol, VY0, VY, 0, 0, 0, 0.f, 0.f);  // diffuse(2, vy0, vy, visc)
+  add(eqk::kOpDivergence, 0, VX0, VY0, VX, VY, 0, 0.f, 0.f);   // project(vx0, vy0, vx, vy)
+  add(eqk::kOpLinSolve, eqk::kPassive, VX, VY, 0, 0, 0, 1.0f, 4.0f);
+  add(eqk::kOpGradient, 0, VX0, VY0, VX, 0, 0, 0.f, 0.f);
+  add(eqk::kOpAdvectBreaks, 0, VX0, VY0, 0, 0, 0, 0.f, 0.f);     // u = vx0, v = vy0 (both)
+  add(eqk::kOpAdvectWrite, eqk::kRow, VX, VX0, VX0, VY0, 0, 0.f, 0.f);
+  add(eqk::kOpAdvectWrite, eqk::kCol, VY, VY0, VX0, VY0, 0, 0.f, 0.f);
+  add(eqk::kOpDivergence, 0, VX, VY, VX0, VY0, 0, 0.f, 0.f);     // project(vx, vy, vx0, vy0)
+  add(eqk::kOpLinSolve, eqk::kPassive, VX0, VY0, 0, 0, 0, 1.0f, 4.0f);
+  add(eqk::kOpGradient, 0, VX, VY, VX0, 0, 0, 0.f, 0.f);
+  add(eqk::kOpDiffuse, eqk::kPassive, SC, DE, 0, 0, 1, 0.f, 0.f);  // diffuse(0, s, d, diff)
+  add(eqk::kOpAdvectBreaks, 0, VX, VY, 0, 0, 0, 0.f, 0.f);
+  add(eqk::kOpAdvectWrite, eqk::kPassive, DE, SC, VX, VY, 0, 0.f, 0.f);
+  add(eqk::kOpCopy, 0, SC, DE, 0, 0, 0, 0.f, 0.f);  // scratch = density.clone()
+  return L;
+}
+
 eqk::BatchArgs batch_args(eq_batch* b, const BLaunch& L, unsigned* queue) {
+  (void)L;
   eqk::BatchArgs A;
   A.arena = b->arena;
   A.marena = b->marena;
@@ -244,10 +265,8 @@ eqk::BatchArgs batch_args(eq_batch* b, const BLaunch& L, unsigned* queue) {
   A.src_d = b->d_sval;
   A.src_u = b->d_sval ? b->d_sval + b->src_cap : nullptr;
   A.src_v = b->d_sval ? b->d_sval + 2 * b->src_cap : nullptr;
-  A.gscratch = b->gscratch;
   A.nwmax = b->nwmax;
   A.cs = batch_cs(b);
-  A.bufs_in_smem = L.bufs_smem ? 1 : 0;
   return A;
 }
 
@@ -274,13 +293,43 @@ int batch_ensure_queue(eq_batch* b, int64_t n) {
 // Enqueue `nframes` frame launches (counter reset first) on the batch stream.
 int batch_enqueue_frames(eq_batch* b, const BLaunch& L, int64_t nframes) {
   EQ_CUDA(cudaMemsetAsync(b->d_queue, 0, nframes * sizeof(unsigned), b->stream));
+  const eqk::BOpList ops = batch_frame_ops();
   for (int64_t f = 0; f < nframes; ++f) {
     eqk::BatchArgs A = batch_args(b, L, b->d_queue + f);
-    eqk::k_batch_frame<<<L.blocks, L.threads, L.smem, b->stream>>>(A);
+    eqk::k_batch_run<<<L.blocks, L.threads, L.smem, b->stream>>>(A, ops);
     b->launches++;
     EQ_CUDA(cudaGetLastError());
   }
   return EQ_OK;
+}
+
+// One launch of an operation list on every scene (the single-phase entries).
+int batch_run_ops(eq_batch* b, const eqk::BOpList& ops) {
+  int rc;
+  if ((rc = batch_prepare(b)) || (rc = batch_ensure_queue(b, 1))) return rc;
+  BLaunch L;
+  if ((rc = batch_launch_shape(b, &L))) return rc;
+  EQ_CUDA(cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned), b->stream));
+  const eqk::BatchArgs A = batch_args(b, L, b->d_queue);
+  eqk::k_batch_run<<<L.blocks, L.threads, L.smem, b->stream>>>(A, ops);
+  b->launches++;
+  EQ_CUDA(cudaGetLastError());
+  return EQ_OK;
+}
+
+eqk::BOp batch_op(int kind, int mode, int f0, int f1, int f2, int f3, int coef, float a,
+                  float c) {
+  eqk::BOp o;
+  o.kind = kind;
+  o.mode = mode;
+  o.f[0] = f0;
+  o.f[1] = f1;
+  o.f[2] = f2;
+  o.f[3] = f3;
+  o.coef = coef;
+  o.a = a;
+  o.c = c;
+  return o;
 }
 
 int batch_check(eq_batch* b) {
@@ -379,8 +428,11 @@ int eq_batch_new(int64_t nscenes, const eq_scene_desc* scenes, int device, eq_ba
     return bail(EQ_ERR_CUDA, "cudaMemcpy (batch tables)");
   int kmax = 1;
   for (int64_t s = 0; s < nscenes; ++s) kmax = std::max(kmax, b->desc[s].K);
-  b->nwmax = std::min(kmax, 20);
   b->bps = 1;
+  b->nwmax = std::min(kmax, 20);
+  while (b->nwmax > 1 && batch_smem_bytes(b, b->nwmax) > batch_smem_budget(b, 1)) b->nwmax--;
+  if (batch_smem_bytes(b, b->nwmax) > batch_smem_budget(b, 1))
+    return bail(EQ_ERR_ARG, "the largest scene is too large for the block wavefront");
   {
     const int blocks = (int)std::min<int64_t>(nscenes, 4096);
     k_batch_init<<<blocks, 256, 0, b->stream>>>(b->arena, b->d_desc, nscenes);
@@ -499,7 +551,7 @@ int eq_batch_set_tuning(eq_batch* b, int sweeps_per_pass, int blocks_per_sm) {
   if (sweeps_per_pass < 1 || sweeps_per_pass > 20)
     return fail(EQ_ERR_ARG, "sweeps_per_pass must be in [1, 20]");
   if (blocks_per_sm < 1 || blocks_per_sm > 4) return fail(EQ_ERR_ARG, "blocks_per_sm must be in [1, 4]");
-  if (sweeps_per_pass * 32 * blocks_per_sm > 1280)
+  if ((sweeps_per_pass + 1) * 32 * blocks_per_sm > 1344)
     return fail(EQ_ERR_ARG, "more threads per SM than the kernel's register budget allows");
   const int onw = b->nwmax, obps = b->bps;
   b->nwmax = sweeps_per_pass;
@@ -511,7 +563,7 @@ int eq_batch_set_tuning(eq_batch* b, int sweeps_per_pass, int blocks_per_sm) {
     return rc;
   }
   int active = 0;
-  EQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, eqk::k_batch_frame, L.threads,
+  EQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, eqk::k_batch_run, L.threads,
                                                         L.smem));
   if (active < blocks_per_sm) {
     b->nwmax = onw;
@@ -574,26 +626,63 @@ int eq_batch_lin_solve(eq_batch* b, int mode, int x_field, int x0_field, float a
       (rc = check_field(x0_field)))
     return rc;
   if (x_field == x0_field) return fail(EQ_ERR_ARG, "x and x0 must differ");
-  if ((rc = batch_prepare(b)) || (rc = batch_ensure_queue(b, 1))) return rc;
-  BLaunch L;
-  if ((rc = batch_launch_shape(b, &L))) return rc;
-  EQ_CUDA(cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned), b->stream));
-  const eqk::BatchArgs A = batch_args(b, L, b->d_queue);
-  const float cr = 1.0f / c;  // fluid.rs:311, IEEE f32 division
-  switch (mode) {
-    case eqk::kRow:
-      eqk::k_batch_lin_solve<eqk::kRow><<<L.blocks, L.threads, L.smem, b->stream>>>(A, x_field, x0_field, a, cr);
-      break;
-    case eqk::kCol:
-      eqk::k_batch_lin_solve<eqk::kCol><<<L.blocks, L.threads, L.smem, b->stream>>>(A, x_field, x0_field, a, cr);
-      break;
-    default:
-      eqk::k_batch_lin_solve<eqk::kPassive><<<L.blocks, L.threads, L.smem, b->stream>>>(A, x_field, x0_field, a, cr);
-      break;
-  }
-  b->launches++;
-  EQ_CUDA(cudaGetLastError());
-  return EQ_OK;
+  eqk::BOpList L;
+  L.n = 1;
+  L.op[0] = batch_op(eqk::kOpLinSolve, mode, x_field, x0_field, 0, 0, 0, a, c);
+  return batch_run_ops(b, L);
+}
+
+int eq_batch_diffuse(eq_batch* b, int mode, int x_field, int x0_field, float diffusion) {
+  int rc;
+  if ((rc = batch_check(b)) || (rc = check_mode(mode)) || (rc = check_field(x_field)) ||
+      (rc = check_field(x0_field)))
+    return rc;
+  if (x_field == x0_field) return fail(EQ_ERR_ARG, "x and x0 must differ");
+  eqk::BOpList L;
+  L.n = 1;
+  L.op[0] = batch_op(eqk::kOpDiffuse, mode, x_field, x0_field, 0, 0, 2, diffusion, 0.f);
+  return batch_run_ops(b, L);
+}
+
+int eq_batch_project(eq_batch* b, int vx_field, int vy_field, int p_field, int div_field) {
+  int rc;
+  if ((rc = batch_check(b)) || (rc = check_field(vx_field)) || (rc = check_field(vy_field)) ||
+      (rc = check_field(p_field)) || (rc = check_field(div_field)))
+    return rc;
+  const int f[4] = {vx_field, vy_field, p_field, div_field};
+  for (int x = 0; x < 4; ++x)
+    for (int y = x + 1; y < 4; ++y)
+      if (f[x] == f[y]) return fail(EQ_ERR_ARG, "project fields must be distinct");
+  eqk::BOpList L;
+  L.n = 3;
+  L.op[0] = batch_op(eqk::kOpDivergence, 0, vx_field, vy_field, p_field, div_field, 0, 0.f, 0.f);
+  L.op[1] = batch_op(eqk::kOpLinSolve, eqk::kPassive, p_field, div_field, 0, 0, 0, 1.0f, 4.0f);
+  L.op[2] = batch_op(eqk::kOpGradient, 0, vx_field, vy_field, p_field, 0, 0, 0.f, 0.f);
+  return batch_run_ops(b, L);
+}
+
+int eq_batch_advect(eq_batch* b, int mode, int d_field, int d0_field, int u_field,
+                    int v_field) {
+  int rc;
+  if ((rc = batch_check(b)) || (rc = check_mode(mode)) || (rc = check_field(d_field)) ||
+      (rc = check_field(d0_field)) || (rc = check_field(u_field)) || (rc = check_field(v_field)))
+    return rc;
+  if (d_field == d0_field || d_field == u_field || d_field == v_field)
+    return fail(EQ_ERR_ARG, "advect destination must differ from its inputs");
+  eqk::BOpList L;
+  L.n = 2;
+  L.op[0] = batch_op(eqk::kOpAdvectBreaks, 0, u_field, v_field, 0, 0, 0, 0.f, 0.f);
+  L.op[1] = batch_op(eqk::kOpAdvectWrite, mode, d_field, d0_field, u_field, v_field, 0, 0.f, 0.f);
+  return batch_run_ops(b, L);
+}
+
+int eq_batch_set_boundaries(eq_batch* b, int mode, int field) {
+  int rc;
+  if ((rc = batch_check(b)) || (rc = check_mode(mode)) || (rc = check_field(field))) return rc;
+  eqk::BOpList L;
+  L.n = 1;
+  L.op[0] = batch_op(eqk::kOpBnd, mode, field, 0, 0, 0, 0, 0.f, 0.f);
+  return batch_run_ops(b, L);
 }
 
 int eq_batch_synchronize(eq_batch* b) {
@@ -631,7 +720,7 @@ int eq_batch_autotune(eq_batch* b, int trial_frames, double* ms_out, int cap, in
   for (int nw : {20, 16, 10, 8, 5, 4}) {
     const int w = std::min(nw, kmax);
     for (int bps : {1, 2}) {
-      if (w * 32 * bps > 1280) continue;
+      if ((w + 1) * 32 * bps > 1344) continue;
       if (std::find(cand.begin(), cand.end(), std::make_pair(w, bps)) == cand.end())
         cand.emplace_back(w, bps);
     }

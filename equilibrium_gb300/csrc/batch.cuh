@@ -38,30 +38,26 @@ struct BatchArgs {
   const float* src_d;
   const float* src_u;
   const float* src_v;
-  float* gscratch;   // per-block carry/edge rows when they do not fit in shared memory
   int nwmax;         // sweeps per wavefront pass (warps per block)
   int cs;            // carry/edge row stride (floats)
-  int bufs_in_smem;  // 1: carry/edge rows in shared memory
 };
-
-__host__ __device__ inline size_t batch_ring_floats(int nwmax) {
-  return (size_t)(nwmax > 1 ? nwmax - 1 : 0) * 32 * kWRS;
-}
-__host__ __device__ inline size_t batch_bufs_floats(int nwmax, int cs) {
-  return (size_t)nwmax * 3 * cs;  // carry (2 rows) + edge (1 row) per warp
-}
 
 // ---- per-cell phases over one scene, by the whole block --------------------
 // Cells are visited by anti-diagonals (warp = diagonal, lane = row j), so the
-// 32 lanes of a warp touch consecutive addresses.
+// 32 lanes of a warp touch consecutive addresses. Each lane takes up to kU
+// cells of its diagonal per pass and issues all their loads before using
+// them (the phases are latency-bound otherwise: one block per scene).
+constexpr int kU = 4;
 
-// Visit every cell (i, j) with ilo <= i <= ihi, jlo <= j <= jhi.
+// Calls fn(r, i, j, q, ok) for r < kU cells of one diagonal pass; `ok` marks
+// the cells that exist. The callers split their work into load and use
+// passes over r so that the loads of all kU cells are in flight together.
 template <class F>
 __device__ __forceinline__ void dg_for_cells(int ilo, int ihi, int jlo, int jhi, int P, F&& fn) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
   for (int d = ilo + jlo + warp; d <= ihi + jhi; d += nwarp) {
     const int j0 = max(jlo, d - ihi), j1 = min(jhi, d - ilo);
-    for (int j = j0 + lane; j <= j1; j += 32) fn(d - j, j, (size_t)d * P + j);
+    for (int jb = j0 + lane; jb <= j1; jb += 32 * kU) fn(d, jb, j1);
   }
 }
 
@@ -83,8 +79,8 @@ __device__ __forceinline__ void blk_sources(const BatchArgs& A, const BScene& sc
 // set_boundaries (fluid.rs:252-272): the order-independent per-cell map of
 // k_set_boundaries, then the corners from post-pass frame values.
 template <int MODE>
-__device__ void blk_bnd(float* x, const uint8_t* code, const uint8_t* rowfl,
-                        const uint8_t* colfl, int S, int P) {
+__device__ void blk_bnd(float* __restrict__ x, const uint8_t* __restrict__ code,
+                        const uint8_t* rowfl, const uint8_t* colfl, int S, int P) {
   const int N = S - 2;
   if (MODE == kPassive) {
     for (int q = threadIdx.x; q < 4 * N; q += blockDim.x) {
@@ -94,19 +90,29 @@ __device__ void blk_bnd(float* x, const uint8_t* code, const uint8_t* rowfl,
       x[dg_at(i, j, P)] = dg_frame_after_pass<kPassive>(x, rowfl, colfl, S, P, i, j);
     }
   } else {
-    // neighbours: (i+-1, j) at q +- P, (i, j+-1) at q +- (P + 1)
-    dg_for_cells(1, N, 1, N, P, [&](int i, int j, size_t q) {
-      const uint8_t c = code[q];
-      if (MODE == kRow) {
-        if (c & kCodeRowRight)
-          x[q] = -x[q + P];
-        else if (c & kCodeRowLeft)
-          x[q] = -x[q - P];
-      } else {
-        if (c & kCodeColUp)
-          x[q] = -x[q - P - 1];
-        else if (c & kCodeColDown)
-          x[q] = -x[q + P + 1];
+    // neighbours: (i+-1, j) at q +- P, (i, j+-1) at q +- (P + 1). Only fluid
+    // cells next to a wall are written, from wall cells (never written).
+    dg_for_cells(1, N, 1, N, P, [&](int d, int jb, int j1) {
+      uint32_t c[kU];
+#pragma unroll
+      for (int r = 0; r < kU; ++r) {
+        const int j = jb + 32 * r;
+        c[r] = j <= j1 ? code[(size_t)d * P + j] : 0u;
+      }
+#pragma unroll
+      for (int r = 0; r < kU; ++r) {
+        const size_t q = (size_t)d * P + jb + 32 * r;
+        if (MODE == kRow) {
+          if (c[r] & kCodeRowRight)
+            x[q] = -x[q + P];
+          else if (c[r] & kCodeRowLeft)
+            x[q] = -x[q - P];
+        } else {
+          if (c[r] & kCodeColUp)
+            x[q] = -x[q - P - 1];
+          else if (c[r] & kCodeColDown)
+            x[q] = -x[q + P + 1];
+        }
       }
     });
   }
@@ -116,25 +122,59 @@ __device__ void blk_bnd(float* x, const uint8_t* code, const uint8_t* rowfl,
 }
 
 // project's divergence + zero pressure (fluid.rs:339-352).
-__device__ void blk_divergence(const float* vx, const float* vy, float* p, float* div, int S,
-                               int P) {
+__device__ void blk_divergence(const float* __restrict__ vx, const float* __restrict__ vy,
+                               float* __restrict__ p, float* __restrict__ div, int S, int P) {
   const int N = S - 2;
-  dg_for_cells(1, N, 1, N, P, [&](int i, int j, size_t q) {
-    const float inner =
-        fsub(fadd(fsub(vx[q + P], vx[q - P]), vy[q + P + 1]), vy[q - P - 1]);
-    div[q] = fdiv(fmul(-0.5f, inner), (float)S);
-    p[q] = 0.0f;
+  dg_for_cells(1, N, 1, N, P, [&](int d, int jb, int j1) {
+    float a[kU], b[kU], c[kU], e[kU];
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      const int j = jb + 32 * r;
+      const size_t q = (size_t)d * P + (j <= j1 ? j : jb);
+      a[r] = vx[q + P];
+      b[r] = vx[q - P];
+      c[r] = vy[q + P + 1];
+      e[r] = vy[q - P - 1];
+    }
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      const int j = jb + 32 * r;
+      if (j > j1) continue;
+      const size_t q = (size_t)d * P + j;
+      const float inner = fsub(fadd(fsub(a[r], b[r]), c[r]), e[r]);
+      div[q] = fdiv(fmul(-0.5f, inner), (float)S);
+      p[q] = 0.0f;
+    }
   });
   __syncthreads();
 }
 
 // project's gradient subtraction (fluid.rs:364-371).
-__device__ void blk_gradient(float* vx, float* vy, const float* p, int S, int P) {
+__device__ void blk_gradient(float* __restrict__ vx, float* __restrict__ vy,
+                             const float* __restrict__ p, int S, int P) {
   const int N = S - 2;
   const float sf = (float)S;
-  dg_for_cells(1, N, 1, N, P, [&](int i, int j, size_t q) {
-    vx[q] = fsub(vx[q], fmul(fmul(0.5f, fsub(p[q + P], p[q - P])), sf));
-    vy[q] = fsub(vy[q], fmul(fmul(0.5f, fsub(p[q + P + 1], p[q - P - 1])), sf));
+  dg_for_cells(1, N, 1, N, P, [&](int d, int jb, int j1) {
+    float x[kU], y[kU], pr[kU], pl[kU], pd[kU], pu[kU];
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      const int j = jb + 32 * r;
+      const size_t q = (size_t)d * P + (j <= j1 ? j : jb);
+      x[r] = vx[q];
+      y[r] = vy[q];
+      pr[r] = p[q + P];
+      pl[r] = p[q - P];
+      pd[r] = p[q + P + 1];
+      pu[r] = p[q - P - 1];
+    }
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      const int j = jb + 32 * r;
+      if (j > j1) continue;
+      const size_t q = (size_t)d * P + j;
+      vx[q] = fsub(x[r], fmul(fmul(0.5f, fsub(pr[r], pl[r])), sf));
+      vy[q] = fsub(y[r], fmul(fmul(0.5f, fsub(pd[r], pu[r])), sf));
+    }
   });
   __syncthreads();
 }
@@ -149,159 +189,252 @@ __device__ __forceinline__ float dg_bilerp(const Backtrace& b, const float* __re
               fmul(b.s1, fadd(fmul(b.t0, C), fmul(b.t1, D))));
 }
 
-// advect (fluid.rs:378-432). Pass 1 finds every row's first break (the
-// clamped backtrace reached size-1) with an atomic minimum per row; pass 2
-// writes the cells before it by bilinear interpolation, the break cell with
-// its left neighbour's new value (the old ghost when it is column 1), and
-// leaves the cells after it untouched. `brk` is block scratch of >= S ints.
-__device__ void blk_advect(float* d, const float* d0, const float* u, const float* v, int S,
-                           int P, float dt0, int* brk) {
+// advect's first pass (fluid.rs:400-423): every row's first break (the clamped
+// backtrace reached size-1), as an atomic minimum per row. `brk` is block
+// scratch of >= S ints. A frame's two velocity advects share u, v and so
+// share this pass.
+__device__ void blk_advect_breaks(const float* __restrict__ u, const float* __restrict__ v,
+                                  int S, int P, float dt0, int* brk) {
   const int N = S - 2;
   for (int j = threadIdx.x; j < S; j += blockDim.x) brk[j] = N + 1;
   __syncthreads();
-  dg_for_cells(1, N, 1, N, P, [&](int i, int j, size_t q) {
-    if (backtrace(i, j, u[q], v[q], dt0, S).brk) atomicMin(&brk[j], i);
+  dg_for_cells(1, N, 1, N, P, [&](int d, int jb, int j1) {
+    float uu[kU], vv[kU];
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      const int j = jb + 32 * r;
+      const size_t q = (size_t)d * P + (j <= j1 ? j : jb);
+      uu[r] = u[q];
+      vv[r] = v[q];
+    }
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      const int j = jb + 32 * r;
+      if (j <= j1 && backtrace(d - j, j, uu[r], vv[r], dt0, S).brk) atomicMin(&brk[j], d - j);
+    }
   });
   __syncthreads();
-  dg_for_cells(1, N, 1, N, P, [&](int i, int j, size_t q) {
-    const int bj = brk[j];
-    if (i > bj) return;
-    float val;
-    if (i == bj && i == 1) {
-      val = d[q - P];  // d[0, j] before this pass (column 0 is never written here)
-    } else {
-      const int ic = (i == bj) ? i - 1 : i;
-      const size_t qc = (i == bj) ? q - P : q;
-      const Backtrace b = backtrace(ic, j, u[qc], v[qc], dt0, S);
-      val = dg_bilerp(b, d0, P);
+}
+
+// advect's second pass (fluid.rs:378-432): the cells before the row's break
+// by bilinear interpolation, the break cell with its left neighbour's new
+// value (the old ghost when it is column 1); the cells after it untouched.
+__device__ void blk_advect_write(float* __restrict__ d, const float* __restrict__ d0,
+                                 const float* __restrict__ u, const float* __restrict__ v,
+                                 int S, int P, float dt0, const int* brk) {
+  const int N = S - 2;
+  dg_for_cells(1, N, 1, N, P, [&](int dd, int jb, int j1) {
+    float uu[kU], vv[kU];
+    int bj[kU];
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      const int j = jb + 32 * r;
+      const int jj = j <= j1 ? j : jb;
+      const int i = dd - jj;
+      bj[r] = brk[jj];
+      // the break cell copies its left neighbour's value: backtrace (i-1, j)
+      const size_t qc = (size_t)dd * P + jj - (i == bj[r] ? P : 0);
+      uu[r] = u[qc];
+      vv[r] = v[qc];
     }
-    d[q] = val;
+    Backtrace bt[kU];
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      const int j = jb + 32 * r;
+      const int jj = j <= j1 ? j : jb;
+      const int i = dd - jj;
+      bt[r] = backtrace(i == bj[r] ? i - 1 : i, jj, uu[r], vv[r], dt0, S);
+    }
+    float val[kU];
+#pragma unroll
+    for (int r = 0; r < kU; ++r) val[r] = dg_bilerp(bt[r], d0, P);
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      const int j = jb + 32 * r;
+      const int i = dd - j;
+      if (j > j1 || i > bj[r]) continue;
+      const size_t q = (size_t)dd * P + j;
+      if (i == bj[r] && i == 1) val[r] = d[q - P];  // d[0, j]: column 0 is never written here
+      d[q] = val[r];
+    }
   });
   __syncthreads();
 }
 
 // scratch_space = density.clone() (fluid.rs:523) over every cell.
-__device__ void blk_copy(float* dst, const float* src, int S, int P) {
-  dg_for_cells(0, S - 1, 0, S - 1, P, [&](int i, int j, size_t q) { dst[q] = src[q]; });
+__device__ void blk_copy(float* __restrict__ dst, const float* __restrict__ src, int S, int P) {
+  dg_for_cells(0, S - 1, 0, S - 1, P, [&](int d, int jb, int j1) {
+    float t[kU];
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      const int j = jb + 32 * r;
+      t[r] = src[(size_t)d * P + (j <= j1 ? j : jb)];
+    }
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      const int j = jb + 32 * r;
+      if (j <= j1) dst[(size_t)d * P + j] = t[r];
+    }
+  });
   __syncthreads();
 }
 
-// diffuse (fluid.rs:276-298): a = ((dt*diff)*sf)*sf, c = 1 + 4a, 1/c in f32.
-template <int MODE>
-__device__ void blk_diffuse(const WGrid& G, const WBufs& Bf, int K, int nwmax, float dt,
-                            float diffusion) {
-  const float sf = (float)(G.S - 2);
-  const float a = fmul(fmul(fmul(dt, diffusion), sf), sf);
-  const float c = fadd(1.0f, fmul(4.0f, a));
-  wave_lin_solve<MODE>(G, Bf, K, nwmax, a, fdiv(1.0f, c));
+// ---- operation lists ---------------------------------------------------------
+// A launch runs a short list of operations on every scene; one frame
+// (Fluid::step, fluid.rs:437-524, with the reference's aliasing of the six
+// arrays) is the list built by batch_frame_ops. The scene descriptor is kept
+// in shared memory and re-read after every operation, so nothing but the
+// operation index is live across a wavefront solve.
+enum : int {
+  kOpSources = 0,   // add_density / add_velocity of the scene's sources
+  kOpDiffuse,       // f[0] = x, f[1] = x0, a = 0: viscosity, 1: diffusion, 2: `c0` given
+  kOpLinSolve,      // f[0] = x, f[1] = x0, coefficients a, c given
+  kOpDivergence,    // f = vx, vy, p, div: div + p = 0, bnd(Passive) of div and p
+  kOpGradient,      // f = vx, vy, p: gradient subtraction, bnd(Row) vx, bnd(Col) vy
+  kOpAdvectBreaks,  // f[0] = u, f[1] = v: every row's first break
+  kOpAdvectWrite,   // f = d, d0, u, v (breaks of u, v computed before), then bnd(mode) d
+  kOpBnd,           // f[0]
+  kOpCopy,          // f[0] = f[1]
+};
+
+struct BOp {
+  int kind, mode;
+  int f[4];
+  int coef;    // kOpDiffuse: 0 viscosity, 1 diffusion, 2 use `a` as the diffusion
+  float a, c;  // kOpLinSolve coefficients (kOpDiffuse with coef 2: a = diffusion)
+};
+
+constexpr int kMaxOps = 16;
+struct BOpList {
+  int n;
+  BOp op[kMaxOps];
+};
+
+__device__ __forceinline__ float* bfield(const BatchArgs& A, const BScene& sc, int f) {
+  return A.arena + sc.foff + (size_t)f * sc.fstride;
 }
 
-// project (fluid.rs:330-375) with p and div as the reference aliases them.
-__device__ void blk_project(WGrid G, const WBufs& Bf, int K, int nwmax, float* vx, float* vy,
-                            float* p, float* div) {
-  const int S = G.S, P = G.P;
-  blk_divergence(vx, vy, p, div, S, P);
-  blk_bnd<kPassive>(div, G.code, G.rowfl, G.colfl, S, P);
-  blk_bnd<kPassive>(p, G.code, G.rowfl, G.colfl, S, P);
-  G.x = p;
-  G.x0 = div;
-  wave_lin_solve<kPassive>(G, Bf, K, nwmax, 1.0f, fdiv(1.0f, 4.0f));
-  blk_gradient(vx, vy, p, S, P);
-  blk_bnd<kRow>(vx, G.code, G.rowfl, G.colfl, S, P);
-  blk_bnd<kCol>(vy, G.code, G.rowfl, G.colfl, S, P);
-}
-
-// One Fluid::step of one scene, with the reference's aliasing of its arrays.
-__device__ void blk_frame(const BatchArgs& A, const BScene& sc, const WBufs& Bf) {
-  float* f[6];
-#pragma unroll
-  for (int q = 0; q < 6; ++q) f[q] = A.arena + sc.foff + (size_t)q * sc.fstride;
-  float *scr = f[0], *de = f[1], *vx = f[2], *vy = f[3], *vx0 = f[4], *vy0 = f[5];
+// One operation on the scene in shared memory.
+__device__ __forceinline__ void blk_op(const BatchArgs& A, const BScene* ssc, const BOp& op,
+                                       const WBufs& Bf, int* brk) {
+  const BScene& sc = *ssc;
+  const int S = sc.S, P = sc.P;
   const uint8_t* code = A.marena + sc.moff;
+  const uint8_t* rowfl = code + sc.fstride;
+  const uint8_t* colfl = rowfl + S;
+  const float dt0 = fmul(sc.dt, (float)(S - 2));
   WGrid G;
   G.code = code;
-  G.rowfl = code + sc.fstride;
-  G.colfl = G.rowfl + sc.S;
-  G.S = sc.S;
-  G.P = sc.P;
-  const int S = sc.S, P = sc.P, K = sc.K, nw = A.nwmax;
-  const float dt0 = fmul(sc.dt, (float)(S - 2));
-  int* brk = reinterpret_cast<int*>(Bf.edge);  // the edge rows are free between solves
-
-  blk_sources(A, sc, de, scr, vx, vy);
-  __syncthreads();
-  G.x = vx0; G.x0 = vx;
-  blk_diffuse<kRow>(G, Bf, K, nw, sc.dt, sc.visc);
-  G.x = vy0; G.x0 = vy;
-  blk_diffuse<kCol>(G, Bf, K, nw, sc.dt, sc.visc);
-  blk_project(G, Bf, K, nw, vx0, vy0, vx, vy);
-  blk_advect(vx, vx0, vx0, vy0, S, P, dt0, brk);
-  blk_bnd<kRow>(vx, G.code, G.rowfl, G.colfl, S, P);
-  blk_advect(vy, vy0, vx0, vy0, S, P, dt0, brk);
-  blk_bnd<kCol>(vy, G.code, G.rowfl, G.colfl, S, P);
-  blk_project(G, Bf, K, nw, vx, vy, vx0, vy0);
-  G.x = scr; G.x0 = de;
-  blk_diffuse<kPassive>(G, Bf, K, nw, sc.dt, sc.diff);
-  blk_advect(de, scr, vx, vy, S, P, dt0, brk);
-  blk_bnd<kPassive>(de, G.code, G.rowfl, G.colfl, S, P);
-  blk_copy(scr, de, S, P);
-}
-
-// One frame of every scene: persistent blocks draining the scene queue.
-__global__ void __launch_bounds__(640, 1) k_batch_frame(BatchArgs A) {
-  extern __shared__ __align__(16) float bsm[];
-  __shared__ int s_next;
-  WBufs Bf;
-  Bf.ring = bsm;
-  Bf.cs = A.cs;
-  float* bufs = A.bufs_in_smem
-                    ? bsm + batch_ring_floats(A.nwmax)
-                    : A.gscratch + (size_t)blockIdx.x * batch_bufs_floats(A.nwmax, A.cs);
-  Bf.carry = bufs;
-  Bf.edge = bufs + (size_t)A.nwmax * 2 * A.cs;
-  for (;;) {
-    if (threadIdx.x == 0) s_next = (int)atomicAdd(A.queue, 1u);
-    __syncthreads();
-    const int q = s_next;
-    __syncthreads();
-    if (q >= A.nscenes) break;
-    const BScene sc = A.scenes[A.order[q]];
-    blk_frame(A, sc, Bf);
+  G.rowfl = rowfl;
+  G.colfl = colfl;
+  G.S = S;
+  G.P = P;
+  switch (op.kind) {
+    case kOpSources:
+      blk_sources(A, sc, bfield(A, sc, 1), bfield(A, sc, 0), bfield(A, sc, 2), bfield(A, sc, 3));
+      __syncthreads();
+      break;
+    case kOpDiffuse:
+    case kOpLinSolve: {
+      G.x = bfield(A, sc, op.f[0]);
+      G.x0 = bfield(A, sc, op.f[1]);
+      float a, cr;
+      if (op.kind == kOpDiffuse) {
+        // diffuse (fluid.rs:276-298): a = ((dt*diff)*sf)*sf, c = 1 + 4a
+        const float dif = op.coef == 0 ? sc.visc : (op.coef == 1 ? sc.diff : op.a);
+        const float sf = (float)(S - 2);
+        a = fmul(fmul(fmul(sc.dt, dif), sf), sf);
+        cr = fdiv(1.0f, fadd(1.0f, fmul(4.0f, a)));
+      } else {
+        a = op.a;
+        cr = fdiv(1.0f, op.c);
+      }
+      if (op.mode == kRow)
+        wave_lin_solve<kRow>(G, Bf, sc.K, A.nwmax, a, cr);
+      else if (op.mode == kCol)
+        wave_lin_solve<kCol>(G, Bf, sc.K, A.nwmax, a, cr);
+      else
+        wave_lin_solve<kPassive>(G, Bf, sc.K, A.nwmax, a, cr);
+      break;
+    }
+    case kOpDivergence: {
+      float* p = bfield(A, sc, op.f[2]);
+      float* div = bfield(A, sc, op.f[3]);
+      blk_divergence(bfield(A, sc, op.f[0]), bfield(A, sc, op.f[1]), p, div, S, P);
+      blk_bnd<kPassive>(div, code, rowfl, colfl, S, P);
+      blk_bnd<kPassive>(p, code, rowfl, colfl, S, P);
+      break;
+    }
+    case kOpGradient: {
+      float* vx = bfield(A, sc, op.f[0]);
+      float* vy = bfield(A, sc, op.f[1]);
+      blk_gradient(vx, vy, bfield(A, sc, op.f[2]), S, P);
+      blk_bnd<kRow>(vx, code, rowfl, colfl, S, P);
+      blk_bnd<kCol>(vy, code, rowfl, colfl, S, P);
+      break;
+    }
+    case kOpAdvectBreaks:
+      blk_advect_breaks(bfield(A, sc, op.f[0]), bfield(A, sc, op.f[1]), S, P, dt0, brk);
+      break;
+    case kOpAdvectWrite: {
+      float* d = bfield(A, sc, op.f[0]);
+      blk_advect_write(d, bfield(A, sc, op.f[1]), bfield(A, sc, op.f[2]),
+                       bfield(A, sc, op.f[3]), S, P, dt0, brk);
+      if (op.mode == kRow)
+        blk_bnd<kRow>(d, code, rowfl, colfl, S, P);
+      else if (op.mode == kCol)
+        blk_bnd<kCol>(d, code, rowfl, colfl, S, P);
+      else
+        blk_bnd<kPassive>(d, code, rowfl, colfl, S, P);
+      break;
+    }
+    case kOpBnd: {
+      float* x = bfield(A, sc, op.f[0]);
+      if (op.mode == kRow)
+        blk_bnd<kRow>(x, code, rowfl, colfl, S, P);
+      else if (op.mode == kCol)
+        blk_bnd<kCol>(x, code, rowfl, colfl, S, P);
+      else
+        blk_bnd<kPassive>(x, code, rowfl, colfl, S, P);
+      break;
+    }
+    case kOpCopy:
+      blk_copy(bfield(A, sc, op.f[0]), bfield(A, sc, op.f[1]), S, P);
+      break;
+    default:
+      break;
   }
 }
 
-// A single lin_solve on field `xf` from `x0f` of every scene (a, c shared),
-// the same block solver as the frame kernel; used to check the wavefront in
-// isolation.
-template <int MODE>
-__global__ void __launch_bounds__(640, 1) k_batch_lin_solve(BatchArgs A, int xf, int x0f,
-                                                            float a, float cr) {
+// Shared-memory layout of a batch block (offsets in floats).
+__device__ __forceinline__ WBufs batch_bufs(const BatchArgs& A) {
+  WBufs Bf;
+  Bf.cs = A.cs;
+  Bf.ring = 0;
+  Bf.carry = A.nwmax * 32 * kWRS;
+  Bf.edge = Bf.carry + A.nwmax * 2 * A.cs;
+  return Bf;
+}
+
+// The operation list on every scene: persistent blocks draining the scene
+// queue (one launch = one frame when L is the frame's list).
+__global__ void __launch_bounds__(672, 1) k_batch_run(BatchArgs A, BOpList L) {
   extern __shared__ __align__(16) float bsm[];
   __shared__ int s_next;
-  WBufs Bf;
-  Bf.ring = bsm;
-  Bf.cs = A.cs;
-  float* bufs = A.bufs_in_smem
-                    ? bsm + batch_ring_floats(A.nwmax)
-                    : A.gscratch + (size_t)blockIdx.x * batch_bufs_floats(A.nwmax, A.cs);
-  Bf.carry = bufs;
-  Bf.edge = bufs + (size_t)A.nwmax * 2 * A.cs;
+  __shared__ BScene s_sc;
+  const WBufs Bf = batch_bufs(A);
+  int* brk = reinterpret_cast<int*>(bsm + Bf.edge);  // edge rows are free between solves
   for (;;) {
-    if (threadIdx.x == 0) s_next = (int)atomicAdd(A.queue, 1u);
+    if (threadIdx.x == 0) {
+      const int q = (int)atomicAdd(A.queue, 1u);
+      s_next = q;
+      if (q < A.nscenes) s_sc = A.scenes[A.order[q]];
+    }
     __syncthreads();
     const int q = s_next;
-    __syncthreads();
     if (q >= A.nscenes) break;
-    const BScene sc = A.scenes[A.order[q]];
-    WGrid G;
-    G.x = A.arena + sc.foff + (size_t)xf * sc.fstride;
-    G.x0 = A.arena + sc.foff + (size_t)x0f * sc.fstride;
-    G.code = A.marena + sc.moff;
-    G.rowfl = G.code + sc.fstride;
-    G.colfl = G.rowfl + sc.S;
-    G.S = sc.S;
-    G.P = sc.P;
-    wave_lin_solve<MODE>(G, Bf, sc.K, A.nwmax, a, cr);
+    for (int k = 0; k < L.n; ++k) blk_op(A, &s_sc, L.op[k], Bf, brk);
+    __syncthreads();
   }
 }
 

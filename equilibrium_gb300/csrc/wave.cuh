@@ -86,6 +86,17 @@ __device__ __forceinline__ void dg_corners(float* x, const uint8_t* rowfl, const
   x[dg_at(S - 1, S - 1, P)] = cSS;
 }
 
+// Shared-memory accesses through 32-bit shared-window addresses (half the
+// registers of generic pointers; ptxas folds the per-step offsets).
+__device__ __forceinline__ float lds_f32(uint32_t a) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ void sts_f32(uint32_t a, float v) {
+  asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+
 // One scene grid as the block solver sees it (diagonal layout).
 struct WGrid {
   float* x;
@@ -96,13 +107,19 @@ struct WGrid {
   int S, P;
 };
 
-// Block-private buffers (generic pointers: shared memory when they fit).
+// Block-private buffers, all in the block's dynamic shared memory, given as
+// float offsets from its start: the rings [nwmax][32][kWRS] (ring[w] is
+// written by warp w: the loader warp 0 or sweep warp w), the carry rows
+// [nwmax][2][cs] (carry[w] is written by warp w) and the sweep warps' edge
+// rows [nwmax][cs].
 struct WBufs {
-  float* ring;   // [nwmax-1][32][kWRS]  (shared)
-  float* carry;  // [nwmax][2][cs]; carry[w] (w >= 1) is written by warp w-1
-  float* edge;   // [nwmax][cs]
-  int cs;        // row stride of carry / edge, >= S
+  int ring, carry, edge;
+  int cs;  // row stride of carry / edge, >= S
 };
+
+__host__ __device__ inline size_t wave_smem_floats(int nwmax, int cs) {
+  return (size_t)nwmax * 32 * kWRS + (size_t)nwmax * 3 * cs;
+}
 
 // Strips per pass: every sweep k < nw must cover rows 0..S-1, and lane 31 of
 // the last strip must never hold an interior row (its fix-up would need a
@@ -110,82 +127,98 @@ struct WBufs {
 __host__ __device__ inline int wave_strips(int S, int nw) { return (S + 2 * nw - 1) / 32 + 1; }
 __host__ __device__ inline int wave_chunks(int S) { return (S + 31 + kWQ - 1) / kWQ; }
 
+constexpr int kWG = 4;  // steps per load group (x0 / codes prefetched one group ahead)
+
 struct WLaneState {
   float g1, g2, u1, rm1;
   float h0, h1;  // carry columns 0 / 1 of lanes 30 / 31, written at the task's end
   uint32_t c1;
 };
 
-// Per-task, per-lane constants. Every stream is (base, stride): the element
-// for column i sits at base[i * stride] (column-indexed rows: stride 1;
-// diagonal-layout grid rows: stride P, base shifted by the row) or, for ring
-// lanes, at base[slot].
+// Per-task, per-lane constants. Grid rows of the diagonal layout are given as
+// a base with column i at base[i * P]; shared rows are 32-bit shared-window
+// byte addresses, column- or slot-indexed with stride 4 bytes.
 struct WTask {
-  const float* rsrc;  // R: x row (first sweep), carry row, or ring lane
-  const float* dsrc;  // D: x row j+1 (first sweep), carry row 1, or ring lane
-  int rstr, dstr;     // 0 = ring (slot-indexed), else column stride
+  float* gout;        // last sweep: x row j, global
+  float* gfix;        // last sweep: x row j-1 (AdjustColumn fix-up), global
   const float* x0row;
   const uint8_t* crow;
-  float* out;  // ring lane (slot-indexed, ostr 0) or x row (column-indexed)
-  int ostr;
-  bool outok;
-  float* carryout;  // lanes 30/31 of a non-last warp: column-indexed carry row
-  float* fixrow;    // lane 0 (AdjustColumn): the row above, column-indexed
-  int fstr;
-  float* edge;      // this warp's edge row
-  int P;
+  uint32_t sr, sd;    // other sweeps: R / D source (ring lane, slot-indexed, or carry row)
+  uint32_t sout;      // other sweeps: this lane's ring row (slot-indexed)
+  uint32_t scarry;    // lanes 30/31 of a non-last sweep: carry row (0 = none)
+  uint32_t sfix;      // non-last sweep, lane 0: carry row 1 (column-indexed)
+  uint32_t sedge;     // this warp's edge row (column-indexed)
+  bool rring, dring;  // R / D source indexed by ring slot (else by column)
   bool valid, interior, top, bot, rowfl;
 };
 
-template <int MODE, bool EDGE>
-__device__ __forceinline__ void wave_chunk(const WTask& T, WLaneState& st, int lane, int c,
-                                           int half, int S, float a, float cr) {
+// x0 and codes of columns ib..ib+kWG-1 of this lane's row (EDGE: only the
+// ones inside the grid).
+template <bool EDGE>
+__device__ __forceinline__ void wave_prefetch(const WTask& T, int ib, int S, int P,
+                                              float (&x)[kWG], uint32_t (&c)[kWG]) {
+  const float* px = T.x0row + (ptrdiff_t)ib * P;
+  const uint8_t* pc = T.crow + (ptrdiff_t)ib * P;
+#pragma unroll
+  for (int r = 0; r < kWG; ++r) {
+    const int i = ib + r;
+    if (EDGE && !(i >= 0 && i <= S - 1)) {
+      x[r] = 0.0f;
+      c[r] = 0u;
+    } else {
+      x[r] = __ldg(px + (ptrdiff_t)r * P);
+      c[r] = __ldg(pc + (ptrdiff_t)r * P);
+    }
+  }
+}
+
+template <int MODE, bool EDGE, bool LAST>
+__device__ __forceinline__ void wave_chunk(const WTask& T, WLaneState& st, int lane, int tau0,
+                                           int half, int S, int P, float a, float cr,
+                                           bool next_in_task, bool next_edge) {
   const unsigned FULL = 0xffffffffu;
   const int N = S - 2;
-  const int P = T.P;
-  const int tau0 = c * kWQ;
   const int ib = tau0 + 1 - lane;  // column at q = 0
-  const float* pR = T.rstr ? T.rsrc + (ptrdiff_t)(ib + 1) * T.rstr : T.rsrc + half;
-  const int sR = T.rstr ? T.rstr : 1;
-  const float* pD = T.dstr ? T.dsrc + (ptrdiff_t)ib * T.dstr : T.dsrc + half;
-  const int sD = T.dstr ? T.dstr : 1;
-  float* pO = T.ostr ? T.out + (ptrdiff_t)(ib - 1) * T.ostr : T.out + half;
-  const int sO = T.ostr ? T.ostr : 1;
-  const float* pX = T.x0row + (ptrdiff_t)ib * P;
-  const uint8_t* pC = T.crow + (ptrdiff_t)ib * P;
-  float* pF = T.fixrow + (ptrdiff_t)ib * T.fstr;
+  // R / D / out streams at q = 0
+  const uint32_t sR = T.sr + 4u * (uint32_t)(T.rring ? half : ib + 1);
+  const uint32_t sD = T.sd + 4u * (uint32_t)(T.dring ? half : ib);
+  float* gO = LAST ? T.gout + (ptrdiff_t)(ib - 1) * P : nullptr;
+  const uint32_t sO = T.sout + 4u * (uint32_t)half;
+  float xa[kWG];
+  uint32_t ca[kWG];
+  wave_prefetch<EDGE>(T, ib, S, P, xa, ca);
 
-  constexpr int kG = 4;  // steps whose loads are issued together
 #pragma unroll
-  for (int q0 = 0; q0 < kWQ; q0 += kG) {
-    float Rv[kG], Dv[kG], Xv[kG], Ev[kG];
-    uint32_t Cv[kG];
-    // Loads of the group first. Safe: x0 and the codes are read-only, the
-    // edge columns lane 31 overwrites in this chunk are below the ones lane 0
-    // reads, and a lane's writes of its own row / the row below trail its reads.
+  for (int q0 = 0; q0 < kWQ; q0 += kWG) {
+    float Xv[kWG];
+    uint32_t Cv[kWG];
 #pragma unroll
-    for (int r = 0; r < kG; ++r) {
+    for (int r = 0; r < kWG; ++r) {
+      Xv[r] = xa[r];
+      Cv[r] = ca[r];
+    }
+    // prefetch the next group
+    if (q0 + kWG < kWQ) wave_prefetch<EDGE>(T, ib + q0 + kWG, S, P, xa, ca);
+    float Rv[kWG], Dv[kWG], Ev[kWG];
+#pragma unroll
+    for (int r = 0; r < kWG; ++r) {
       const int q = q0 + r;
       const int i = ib + q;
       if (EDGE) {
-        const bool okR = !T.rstr || (i + 1 >= 0 && i + 1 <= S - 1);
-        const bool okD = !T.dstr || (i >= 0 && i <= S - 1);
+        const bool okR = T.rring || (i + 1 >= 0 && i + 1 <= S - 1);
+        const bool okD = T.dring || (i >= 0 && i <= S - 1);
         const bool okI = (i >= 0 && i <= S - 1);
-        Rv[r] = okR ? pR[(ptrdiff_t)q * sR] : 0.0f;
-        Dv[r] = okD ? pD[(ptrdiff_t)q * sD] : 0.0f;
-        Xv[r] = okI ? pX[(ptrdiff_t)q * P] : 0.0f;
-        Cv[r] = okI ? (uint32_t)pC[(ptrdiff_t)q * P] : 0u;
-        Ev[r] = (lane == 0 && okI) ? T.edge[i] : 0.0f;
+        Rv[r] = okR ? lds_f32(sR + 4u * q) : 0.0f;
+        Dv[r] = okD ? lds_f32(sD + 4u * q) : 0.0f;
+        Ev[r] = (lane == 0 && okI) ? lds_f32(T.sedge + 4u * (uint32_t)i) : 0.0f;
       } else {
-        Rv[r] = pR[(ptrdiff_t)q * sR];
-        Dv[r] = pD[(ptrdiff_t)q * sD];
-        Xv[r] = pX[(ptrdiff_t)q * P];
-        Cv[r] = pC[(ptrdiff_t)q * P];
-        Ev[r] = T.edge[i];
+        Rv[r] = lds_f32(sR + 4u * q);
+        Dv[r] = lds_f32(sD + 4u * q);
+        Ev[r] = lds_f32(T.sedge + 4u * (uint32_t)i);
       }
     }
 #pragma unroll
-    for (int r = 0; r < kG; ++r) {
+    for (int r = 0; r < kWG; ++r) {
       const int q = q0 + r;
       const int i = ib + q;
       float U = __shfl_up_sync(FULL, st.g1, 1);
@@ -194,7 +227,7 @@ __device__ __forceinline__ void wave_chunk(const WTask& T, WLaneState& st, int l
       const float gc = fmul(fadd(Xv[r], fmul(a, fadd(fadd(fadd(R, st.g1), Dv[r]), U))), cr);
       const bool act = EDGE ? (T.interior && i >= 1 && i <= N) : T.interior;
       const float g = act ? gc : st.rm1;
-      const float gd = __shfl_down_sync(FULL, g, 1);
+      const float gdn = __shfl_down_sync(FULL, g, 1);
 
       // post-boundary value of column i-1
       const uint32_t c1 = st.c1;
@@ -202,33 +235,42 @@ __device__ __forceinline__ void wave_chunk(const WTask& T, WLaneState& st, int l
       if (MODE == kRow) {
         val = (c1 & kCodeRowRight) ? -g : ((c1 & kCodeRowLeft) ? -st.g2 : st.g1);
       } else if (MODE == kCol) {
-        val = (c1 & kCodeColUp) ? -st.u1 : ((c1 & kCodeColDown) ? -gd : st.g1);
+        val = (c1 & kCodeColUp) ? -st.u1 : ((c1 & kCodeColDown) ? -gdn : st.g1);
       } else {
         const bool cf = (c1 & kCodeColFluid) != 0;
-        val = (T.top && cf) ? gd : ((T.bot && cf) ? st.u1 : st.g1);
+        val = (T.top && cf) ? gdn : ((T.bot && cf) ? st.u1 : st.g1);
         if (EDGE && T.interior) {
           if (i - 1 == 0) val = T.rowfl ? g : st.g1;
           if (i - 1 == S - 1) val = T.rowfl ? st.g2 : st.g1;
         }
       }
       const bool colok = EDGE ? (i - 1 >= 0 && i - 1 <= S - 1) : true;
-      if (T.outok && colok) pO[(ptrdiff_t)q * sO] = val;
-      if (T.carryout && colok) {
-        // Columns 0 / 1 of the carry rows are produced in chunk 1, the super-step
-        // in which the next warp still reads the previous strip's columns 0 / 1;
-        // they are held back and written when the task ends.
-        if (EDGE && tau0 < 2 * kWQ) {
-          if (i - 1 == 0) st.h0 = val;
-          if (i - 1 == 1) st.h1 = val;
-        } else {
-          T.carryout[i - 1] = val;
+      if (LAST) {
+        if (T.valid && colok) gO[(ptrdiff_t)q * P] = val;
+      } else {
+        if (colok) sts_f32(sO + 4u * q, val);
+        if (T.scarry && colok) {
+          // Columns 0 / 1 of the carry rows are produced in chunk 1, the
+          // super-step in which the next warp still reads the previous strip's
+          // columns 0 / 1; they are held back and written when the task ends.
+          if (EDGE && tau0 < 2 * kWQ) {
+            if (i - 1 == 0) st.h0 = val;
+            if (i - 1 == 1) st.h1 = val;
+          } else {
+            sts_f32(T.scarry + 4u * (uint32_t)(i - 1), val);
+          }
         }
       }
-      if (lane == 31 && (EDGE ? (i >= 0 && i <= S - 1) : true)) T.edge[i] = g;
+      if (lane == 31 && (EDGE ? (i >= 0 && i <= S - 1) : true))
+        sts_f32(T.sedge + 4u * (uint32_t)i, g);
       // (a lane whose row lies outside the grid reads a clamped row's code)
       if (MODE == kCol && lane == 0 && T.valid && (Cv[r] & kCodeAboveDown) &&
-          (EDGE ? (i >= 1 && i <= N) : true))
-        pF[(ptrdiff_t)q * T.fstr] = -g;
+          (EDGE ? (i >= 1 && i <= N) : true)) {
+        if (LAST)
+          T.gfix[(ptrdiff_t)i * P] = -g;
+        else
+          sts_f32(T.sfix + 4u * (uint32_t)i, -g);
+      }
 
       st.g2 = st.g1;
       st.g1 = g;
@@ -239,98 +281,154 @@ __device__ __forceinline__ void wave_chunk(const WTask& T, WLaneState& st, int l
   }
 }
 
+template <int MODE, bool LAST>
+__device__ __forceinline__ void wave_chunk_any(const WTask& T, WLaneState& st, int lane, int c,
+                                               int NCH, int half, int S, int P, float a,
+                                               float cr) {
+  const int N = S - 2;
+  const int tau0 = c * kWQ;
+  const bool fast = (tau0 >= 32) && (tau0 + kWQ <= N);
+  const bool next_in_task = c + 1 < NCH;
+  const bool next_edge = !((tau0 + kWQ >= 32) && (tau0 + 2 * kWQ <= N));
+  if (fast)
+    wave_chunk<MODE, false, LAST>(T, st, lane, tau0, half, S, P, a, cr, next_in_task,
+                                  next_edge);
+  else
+    wave_chunk<MODE, true, LAST>(T, st, lane, tau0, half, S, P, a, cr, next_in_task,
+                                 next_edge);
+}
+
 // `K` sweeps of lin_solve on grid G by the whole block (blockDim.x = 32 *
-// nwmax), passes of at most nwmax sweeps. Ends with a block barrier; the
-// result (corners included) is in G.x.
+// (nwmax + 1): a loader warp and one warp per sweep of a pass), passes of at
+// most nwmax sweeps. Ends with a block barrier; the result (corners included)
+// is in G.x.
 template <int MODE>
 __device__ __noinline__ void wave_lin_solve(const WGrid G, const WBufs Bf, int K, int nwmax,
                                             float a, float cr) {
   if (K <= 0) return;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  extern __shared__ __align__(16) float wave_smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;  // warp 0: loader
   const int S = G.S, P = G.P, N = S - 2;
   const int NCH = wave_chunks(S);
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(wave_smem);
+  const uint32_t ring = sbase + 4u * Bf.ring;
+  const uint32_t carry = sbase + 4u * Bf.carry;
+  const uint32_t edge = sbase + 4u * Bf.edge;
+  const uint32_t cs4 = 4u * Bf.cs;
+  constexpr uint32_t kLane4 = 4u * kWRS, kWarp4 = 32u * 4u * kWRS;
   for (int k0 = 0; k0 < K; k0 += nwmax) {
     const int nw = min(nwmax, K - k0);
     const int B = wave_strips(S, nw);
     const int ntask = B * NCH;
-    const int nsup = ntask + nw - 1;
-    const bool first = (warp == 0), last = (warp == nw - 1);
-    WLaneState st{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0u};
-    WTask T;
-    T.P = P;
-    for (int s = 0; s < nsup; ++s) {
-      const int g = s - warp;
-      if (warp < nw && g >= 0 && g < ntask) {
-        const int t = g / NCH, c = g - t * NCH;
-        if (c == 0) {
-          // ---- task set-up
-          const int j = 32 * t + lane - 2 * warp - 2;
-          T.valid = (j >= 0 && j <= S - 1);
-          T.interior = (j >= 1 && j <= N);
-          T.top = (j == 0);
-          T.bot = (j == S - 1);
-          const int jc = j < 0 ? 0 : (j > S - 1 ? S - 1 : j);
-          const int jd = j + 1 < 0 ? 0 : (j + 1 > S - 1 ? S - 1 : j + 1);
-          T.rowfl = T.interior && G.rowfl[jc];
-          float* ringIn = Bf.ring + (size_t)(warp - 1) * 32 * kWRS;
-          float* carryIn = Bf.carry + (size_t)warp * 2 * Bf.cs;
-          // row j of a diagonal-layout grid: column i at base[i * P]
-          const size_t rowJ = (size_t)jc * P + jc, rowD = (size_t)jd * P + jd;
-          if (first) {
-            T.rsrc = G.x + rowJ;
-            T.dsrc = G.x + rowD;
-            T.rstr = T.dstr = P;
-          } else {
-            T.rstr = lane >= 2 ? 0 : 1;
-            T.dstr = lane >= 1 ? 0 : 1;
-            T.rsrc = lane >= 2 ? ringIn + (lane - 2) * kWRS : carryIn + (size_t)lane * Bf.cs;
-            T.dsrc = lane >= 1 ? ringIn + (lane - 1) * kWRS : carryIn + Bf.cs;
-          }
-          T.x0row = G.x0 + rowJ;
-          T.crow = G.code + rowJ;
-          T.edge = Bf.edge + (size_t)warp * Bf.cs;
-          if (last) {
-            T.out = G.x + rowJ;
-            T.ostr = P;
-            T.outok = T.valid;
-            T.carryout = nullptr;
-            const int ja = jc > 0 ? jc - 1 : 0;
-            T.fixrow = G.x + (size_t)ja * P + ja;
-            T.fstr = P;
-          } else {
-            float* carryOut = Bf.carry + (size_t)(warp + 1) * 2 * Bf.cs;
-            T.out = Bf.ring + (size_t)warp * 32 * kWRS + lane * kWRS;
-            T.ostr = 0;
-            T.outok = true;
-            T.carryout = (lane >= 30) ? carryOut + (size_t)(lane - 30) * Bf.cs : nullptr;
-            T.fixrow = carryOut + Bf.cs;
-            T.fstr = 1;
-          }
-          // Lanes 0 and 1 start inside the row: their history (G(0) for lane
-          // 0, W(k-1)[i, j] for the first step) comes from column 0 / 1 of
-          // their column-indexed R source.
-          st.g1 = st.g2 = st.u1 = st.rm1 = 0.0f;
-          st.c1 = 0u;
-          if (lane == 0) {
-            st.g1 = T.rsrc[0];
-            st.rm1 = T.rsrc[T.rstr];
-          } else if (lane == 1) {
-            st.rm1 = T.rsrc[0];
-          }
+    const int nsup = ntask + nw;
+    if (warp == 0) {
+      // ---- loader: W(-1) = x into ring 0 (and carry 0 for lanes 30/31), row
+      // j = 32 t + l, column tau - l at step tau; loads one chunk ahead.
+      float xs[kWQ];
+      float h0 = 0.0f, h1 = 0.0f;
+      auto load_chunk = [&](int gg) {
+        const int t = gg / NCH, c = gg - t * NCH;
+        const int j = 32 * t + lane;
+        const bool rowok = j >= 0 && j <= S - 1;
+        const int jc = rowok ? j : 0;
+        const float* base = G.x + (size_t)jc * P + jc;
+#pragma unroll
+        for (int q = 0; q < kWQ; ++q) {
+          const int is = c * kWQ + q - lane;
+          xs[q] = (rowok && is >= 0 && is <= S - 1) ? base[(ptrdiff_t)is * P] : 0.0f;
         }
-        const int half = (g & 1) * kWQ;
-        const int tau0 = c * kWQ;
-        const bool fast = (tau0 >= 32) && (tau0 + kWQ <= N);
-        if (fast)
-          wave_chunk<MODE, false>(T, st, lane, c, half, S, a, cr);
-        else
-          wave_chunk<MODE, true>(T, st, lane, c, half, S, a, cr);
-        if (c == NCH - 1 && T.carryout) {
-          T.carryout[0] = st.h0;
-          if (lane == 30) T.carryout[1] = st.h1;
+      };
+      load_chunk(0);
+      for (int s = 0; s < nsup; ++s) {
+        if (s < ntask) {
+          const int t = s / NCH, c = s - t * NCH;
+          const int tau0 = c * kWQ;
+          const uint32_t sO = ring + (uint32_t)lane * kLane4 + 4u * (uint32_t)((s & 1) * kWQ);
+          const uint32_t sC = carry + (uint32_t)(lane - 30) * cs4;
+#pragma unroll
+          for (int q = 0; q < kWQ; ++q) {
+            sts_f32(sO + 4u * q, xs[q]);
+            const int is = tau0 + q - lane;
+            if (lane >= 30 && is >= 0 && is <= S - 1) {
+              if (tau0 < 2 * kWQ) {  // held back: see the sweep warps' carry rows
+                if (is == 0) h0 = xs[q];
+                if (is == 1) h1 = xs[q];
+              } else {
+                sts_f32(sC + 4u * (uint32_t)is, xs[q]);
+              }
+            }
+          }
+          if (c == NCH - 1 && lane >= 30) {
+            sts_f32(sC, h0);
+            if (lane == 30) sts_f32(sC + 4u, h1);
+          }
+          if (s + 1 < ntask) load_chunk(s + 1);
         }
+        __syncthreads();
       }
-      __syncthreads();
+    } else {
+      // ---- sweep warp w performs sweep w-1 of the pass
+      const int sw = warp - 1;
+      const bool last = (sw == nw - 1);
+      WLaneState st;
+      st.g1 = st.g2 = st.u1 = st.rm1 = st.h0 = st.h1 = 0.0f;
+      st.c1 = 0u;
+      WTask T;
+      for (int s = 0; s < nsup; ++s) {
+        const int g = s - warp;
+        if (sw < nw && g >= 0 && g < ntask) {
+          const int t = g / NCH, c = g - t * NCH;
+          if (c == 0) {
+            // ---- task set-up
+            const int j = 32 * t + lane - 2 * sw - 2;
+            T.valid = (j >= 0 && j <= S - 1);
+            T.interior = (j >= 1 && j <= N);
+            T.top = (j == 0);
+            T.bot = (j == S - 1);
+            const int jc = j < 0 ? 0 : (j > S - 1 ? S - 1 : j);
+            T.rowfl = T.interior && G.rowfl[jc];
+            const uint32_t ringIn = ring + (uint32_t)(warp - 1) * kWarp4;
+            const uint32_t carryIn = carry + (uint32_t)(warp - 1) * 2u * cs4;
+            // row j of a diagonal-layout grid: column i at base[i * P]
+            const size_t rowJ = (size_t)jc * P + jc;
+            T.rring = lane >= 2;
+            T.dring = lane >= 1;
+            T.sr = T.rring ? ringIn + (uint32_t)(lane - 2) * kLane4 : carryIn + (uint32_t)lane * cs4;
+            T.sd = T.dring ? ringIn + (uint32_t)(lane - 1) * kLane4 : carryIn + cs4;
+            T.x0row = G.x0 + rowJ;
+            T.crow = G.code + rowJ;
+            T.sedge = edge + (uint32_t)sw * cs4;
+            T.gout = G.x + rowJ;
+            const int ja = jc > 0 ? jc - 1 : 0;
+            T.gfix = G.x + (size_t)ja * P + ja;
+            const uint32_t carryOut = carry + (uint32_t)warp * 2u * cs4;
+            T.sout = ring + (uint32_t)warp * kWarp4 + (uint32_t)lane * kLane4;
+            T.scarry = (!last && lane >= 30) ? carryOut + (uint32_t)(lane - 30) * cs4 : 0u;
+            T.sfix = carryOut + cs4;
+            // Lanes 0 and 1 start inside the row: their history (G(0) for
+            // lane 0, W(k-1)[i, j] for the first step) comes from column 0 / 1
+            // of their carry row.
+            st.g1 = st.g2 = st.u1 = st.rm1 = 0.0f;
+            st.c1 = 0u;
+            if (lane == 0) {
+              st.g1 = lds_f32(T.sr);
+              st.rm1 = lds_f32(T.sr + 4u);
+            } else if (lane == 1) {
+              st.rm1 = lds_f32(T.sr);
+            }
+          }
+          const int half = (g & 1) * kWQ;
+          if (last)
+            wave_chunk_any<MODE, true>(T, st, lane, c, NCH, half, S, P, a, cr);
+          else
+            wave_chunk_any<MODE, false>(T, st, lane, c, NCH, half, S, P, a, cr);
+          if (c == NCH - 1 && T.scarry) {
+            sts_f32(T.scarry, st.h0);
+            if (lane == 30) sts_f32(T.scarry + 4u, st.h1);
+          }
+        }
+        __syncthreads();
+      }
     }
   }
   if (threadIdx.x == 0) dg_corners<MODE>(G.x, G.rowfl, G.colfl, S, P);

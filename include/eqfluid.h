@@ -257,6 +257,16 @@ int eq_batch_synchronize(eq_batch* b);
  * scene with each scene's sweep count, by the same block solver. */
 int eq_batch_lin_solve(eq_batch* b, int mode, int x_field, int x0_field, float a, float c);
 
+/* The other single phases on every scene (fields as in the eq_fluid_* forms):
+ * diffuse (fluid.rs:276-298) with one `diffusion` for all scenes, project
+ * (fluid.rs:330-375), advect (fluid.rs:378-432), set_boundaries
+ * (fluid.rs:252-272). */
+int eq_batch_diffuse(eq_batch* b, int mode, int x_field, int x0_field, float diffusion);
+int eq_batch_project(eq_batch* b, int vx_field, int vy_field, int p_field, int div_field);
+int eq_batch_advect(eq_batch* b, int mode, int d_field, int d0_field, int u_field,
+                    int v_field);
+int eq_batch_set_boundaries(eq_batch* b, int mode, int field);
+
 /* Tuning: sweeps per wavefront pass (warps per thread block, 1..20; a
  * lin_solve of K sweeps takes ceil(K / sweeps_per_pass) passes) and thread
  * blocks per SM. The default is min(max K, 20) and 1. */
