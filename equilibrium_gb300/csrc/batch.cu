@@ -297,7 +297,6 @@ int batch_enqueue_frames(eq_batch* b, const BLaunch& L, int64_t nframes) {
   for (int64_t f = 0; f < nframes; ++f) {
     eqk::BatchArgs A = batch_args(b, L, b->d_queue + f);
     eqk::k_batch_run<<<L.blocks, L.threads, L.smem, b->stream>>>(A, ops);
-    b->launches++;
     EQ_CUDA(cudaGetLastError());
   }
   return EQ_OK;
@@ -606,6 +605,7 @@ int eq_batch_step(eq_batch* b, int64_t nframes) {
     b->gbps = b->bps;
   }
   EQ_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+  b->launches += (uint64_t)nframes;  // one frame kernel per replayed frame
   return EQ_OK;
 }
 
@@ -617,7 +617,9 @@ int eq_batch_step_eager(eq_batch* b, int64_t nframes) {
   if ((rc = batch_prepare(b)) || (rc = batch_ensure_queue(b, nframes))) return rc;
   BLaunch L;
   if ((rc = batch_launch_shape(b, &L))) return rc;
-  return batch_enqueue_frames(b, L, nframes);
+  if ((rc = batch_enqueue_frames(b, L, nframes))) return rc;
+  b->launches += (uint64_t)nframes;
+  return EQ_OK;
 }
 
 int eq_batch_lin_solve(eq_batch* b, int mode, int x_field, int x0_field, float a, float c) {
