@@ -16,6 +16,7 @@ HEADER = os.path.join(ROOT, "include", "eqfluid.h")
 EQ_OK, EQ_ERR_ARG, EQ_ERR_CUDA, EQ_ERR_TIMEOUT, EQ_ERR_OOM, EQ_ERR_STATE = range(6)
 FIELD_SCRATCH, FIELD_DENSITY, FIELD_VX, FIELD_VY, FIELD_VX0, FIELD_VY0 = range(6)
 MODE_ADJUST_ROW, MODE_ADJUST_COLUMN, MODE_PASSIVE = range(3)
+STORE_F16, STORE_BF16 = 1, 2
 
 
 class EqError(RuntimeError):
@@ -35,6 +36,11 @@ class SceneDescC(ctypes.Structure):
     _fields_ = [("size", ctypes.c_uint32), ("delta_t", ctypes.c_float),
                 ("frames", ctypes.c_int64), ("diffusion", ctypes.c_float),
                 ("viscousity", ctypes.c_float)]
+
+
+class HStatsC(ctypes.Structure):
+    _fields_ = [("ir_iterations", ctypes.c_int32 * 2), ("rel_residual", ctypes.c_double * 2),
+                ("div_norm_before", ctypes.c_double * 2), ("div_norm", ctypes.c_double * 2)]
 
 
 class FluidConfigsC(ctypes.Structure):
@@ -108,6 +114,7 @@ def load(path: str = LIB_PATH):
         "eq_fluid_kernel_stats": (i32, [H, i32, ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_uint64)]),
         "eq_batch_new": (i32, [i64, ctypes.POINTER(SceneDescC), i32, PP]),
+        "eq_batch_new_storage": (i32, [i64, ctypes.POINTER(SceneDescC), i32, i32, PP]),
         "eq_batch_free": (i32, [H]),
         "eq_batch_scene_count": (i32, [H, ctypes.POINTER(ctypes.c_int64)]),
         "eq_batch_cell_count": (i32, [H, ctypes.POINTER(ctypes.c_uint64)]),
@@ -130,6 +137,18 @@ def load(path: str = LIB_PATH):
         "eq_batch_autotune": (i32, [H, i32, ctypes.POINTER(ctypes.c_double), i32,
                                     ctypes.POINTER(ctypes.c_int)]),
         "eq_batch_get_stream": (i32, [H, PP]),
+        "eq_hfluid_new": (i32, [ctypes.POINTER(FluidConfigsC), ctypes.POINTER(SimulationConfigsC),
+                                i32, ctypes.c_double, i32, i32, PP]),
+        "eq_hfluid_free": (i32, [H]),
+        "eq_hfluid_fill_obstacle": (i32, [H, i64, i64, i64, i64]),
+        "eq_hfluid_add_sources": (i32, [H, i64, P, P, P, P, P]),
+        "eq_hfluid_step": (i32, [H]),
+        "eq_hfluid_synchronize": (i32, [H]),
+        "eq_hfluid_read_field": (i32, [H, i32, P, u64]),
+        "eq_hfluid_write_field": (i32, [H, i32, P, u64]),
+        "eq_hfluid_stats": (i32, [H, ctypes.POINTER(HStatsC)]),
+        "eq_hfluid_get_stream": (i32, [H, PP]),
+        "eq_hfluid_launch_count": (i32, [H, ctypes.POINTER(ctypes.c_uint64)]),
         "eq_batch_launch_count": (i32, [H, ctypes.POINTER(ctypes.c_uint64)]),
     }
     for name, (res, args) in sigs.items():

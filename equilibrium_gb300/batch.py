@@ -28,7 +28,7 @@ class SceneConfig:
 
 
 class Batch:
-    def __init__(self, scenes: Sequence[SceneConfig], device: int = 0):
+    def __init__(self, scenes: Sequence[SceneConfig], device: int = 0, storage: str = "f32"):
         L = _lib.load()
         n = len(scenes)
         arr = (_lib.SceneDescC * n)()
@@ -39,7 +39,9 @@ class Batch:
             arr[q].diffusion = float(sc.diffusion)
             arr[q].viscousity = float(sc.viscousity)
         h = ctypes.c_void_p()
-        check(L.eq_batch_new(n, arr, device, ctypes.byref(h)))
+        st = {"f32": 0, "f16": _lib.STORE_F16, "bf16": _lib.STORE_BF16}[storage]
+        check(L.eq_batch_new_storage(n, arr, st, device, ctypes.byref(h)))
+        self.storage = storage
         self.handle = h
         self.scenes = list(scenes)
 

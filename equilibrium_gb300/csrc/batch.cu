@@ -16,6 +16,8 @@
 
 struct eq_batch {
   int device = 0;
+  int storage = 0;   // 0 FP32 (bit-exact), EQ_STORE_F16, EQ_STORE_BF16
+  size_t esize = 4;  // bytes per stored cell value
   cudaStream_t stream = nullptr;
   int64_t n = 0;
   std::vector<eqk::BScene> desc;
@@ -28,8 +30,8 @@ struct eq_batch {
   bool mask_dirty = true, src_dirty = true;
   int smax = 0;
 
-  float* arena = nullptr;
-  size_t arena_floats = 0;
+  void* arena = nullptr;
+  size_t arena_elems = 0;
   uint8_t* marena = nullptr;
   size_t marena_bytes = 0;
   eqk::BScene* d_desc = nullptr;
@@ -83,12 +85,13 @@ void batch_free(eq_batch* b) {
 // Fluid::new state (fluid.rs:93-110 then init(), fluid.rs:602-606) of every
 // scene: zeros, vx = vy = 0 + 1, density = scratch = 0 + 0 (+ 0.9 on the
 // block [size/2-10, size/2+10]^2). The arena was zeroed before.
-__global__ void k_batch_init(float* arena, const eqk::BScene* scenes, int64_t n) {
+template <class ST>
+__global__ void k_batch_init(ST* arena, const eqk::BScene* scenes, int64_t n) {
   for (int64_t s = blockIdx.x; s < n; s += gridDim.x) {
     const eqk::BScene sc = scenes[s];
     const int S = sc.S, P = sc.P;
     const int lo = S / 2 - 10, hi = S / 2 + 10;
-    float* f = arena + sc.foff;
+    ST* f = arena + sc.foff;
     const size_t cells = (size_t)S * S;
     // idx! clamps the block's coordinates into the grid (fluid.rs:31-35), so for
     // size 20 the last column / row receives the 0.9 twice (the corner 4x).
@@ -103,10 +106,10 @@ __global__ void k_batch_init(float* arena, const eqk::BScene* scenes, int64_t n)
       for (int r = mult(i) * mult(j); r > 0; --r) dens = eqk::fadd(dens, 0.9f);
       const float vel = eqk::fadd(0.0f, 1.0f);
       const size_t a = eqk::dg_at(i, j, P);
-      f[a] = dens;
-      f[sc.fstride + a] = dens;
-      f[2 * sc.fstride + a] = vel;
-      f[3 * sc.fstride + a] = vel;
+      eqk::hs(f, a, dens);
+      eqk::hs(f, sc.fstride + a, dens);
+      eqk::hs(f, 2 * sc.fstride + a, vel);
+      eqk::hs(f, 3 * sc.fstride + a, vel);
     }
   }
 }
@@ -206,8 +209,12 @@ int batch_launch_shape(eq_batch* b, BLaunch* L) {
     return fail(EQ_ERR_ARG, "the wavefront buffers do not fit in shared memory at this tuning");
   L->blocks = (int)std::min<int64_t>(b->n, (int64_t)b->num_sms * b->bps);
   if (L->blocks < 1) L->blocks = 1;
-  EQ_CUDA(cudaFuncSetAttribute(eqk::k_batch_run, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)L->smem));
+  EQ_CUDA(cudaFuncSetAttribute(eqk::k_batch_run<float>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem));
+  EQ_CUDA(cudaFuncSetAttribute(eqk::k_batch_run<__half>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem));
+  EQ_CUDA(cudaFuncSetAttribute(eqk::k_batch_run<__nv_bfloat16>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem));
   return EQ_OK;
 }
 
@@ -290,13 +297,23 @@ int batch_ensure_queue(eq_batch* b, int64_t n) {
   return EQ_OK;
 }
 
+void batch_launch_run(eq_batch* b, const BLaunch& L, const eqk::BatchArgs& A,
+                      const eqk::BOpList& ops) {
+  if (b->storage == EQ_STORE_F16)
+    eqk::k_batch_run<__half><<<L.blocks, L.threads, L.smem, b->stream>>>(A, ops);
+  else if (b->storage == EQ_STORE_BF16)
+    eqk::k_batch_run<__nv_bfloat16><<<L.blocks, L.threads, L.smem, b->stream>>>(A, ops);
+  else
+    eqk::k_batch_run<float><<<L.blocks, L.threads, L.smem, b->stream>>>(A, ops);
+}
+
 // Enqueue `nframes` frame launches (counter reset first) on the batch stream.
 int batch_enqueue_frames(eq_batch* b, const BLaunch& L, int64_t nframes) {
   EQ_CUDA(cudaMemsetAsync(b->d_queue, 0, nframes * sizeof(unsigned), b->stream));
   const eqk::BOpList ops = batch_frame_ops();
   for (int64_t f = 0; f < nframes; ++f) {
     eqk::BatchArgs A = batch_args(b, L, b->d_queue + f);
-    eqk::k_batch_run<<<L.blocks, L.threads, L.smem, b->stream>>>(A, ops);
+    batch_launch_run(b, L, A, ops);
     EQ_CUDA(cudaGetLastError());
   }
   return EQ_OK;
@@ -310,7 +327,7 @@ int batch_run_ops(eq_batch* b, const eqk::BOpList& ops) {
   if ((rc = batch_launch_shape(b, &L))) return rc;
   EQ_CUDA(cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned), b->stream));
   const eqk::BatchArgs A = batch_args(b, L, b->d_queue);
-  eqk::k_batch_run<<<L.blocks, L.threads, L.smem, b->stream>>>(A, ops);
+  batch_launch_run(b, L, A, ops);
   b->launches++;
   EQ_CUDA(cudaGetLastError());
   return EQ_OK;
@@ -346,7 +363,14 @@ int batch_scene(eq_batch* b, int64_t s) {
 extern "C" {
 
 int eq_batch_new(int64_t nscenes, const eq_scene_desc* scenes, int device, eq_batch** out) {
+  return eq_batch_new_storage(nscenes, scenes, 0, device, out);
+}
+
+int eq_batch_new_storage(int64_t nscenes, const eq_scene_desc* scenes, int storage, int device,
+                         eq_batch** out) {
   if (!out || !scenes) return fail(EQ_ERR_ARG, "null argument");
+  if (storage != 0 && storage != EQ_STORE_F16 && storage != EQ_STORE_BF16)
+    return fail(EQ_ERR_ARG, "storage must be 0 (FP32), EQ_STORE_F16 or EQ_STORE_BF16");
   *out = nullptr;
   if (nscenes <= 0) return fail(EQ_ERR_ARG, "nscenes must be > 0");
   if (nscenes > (int64_t)1 << 30) return fail(EQ_ERR_ARG, "too many scenes");
@@ -361,6 +385,8 @@ int eq_batch_new(int64_t nscenes, const eq_scene_desc* scenes, int device, eq_ba
   eq_batch* b = new eq_batch();
   b->device = device;
   b->n = nscenes;
+  b->storage = storage;
+  b->esize = storage == 0 ? 4 : 2;
   auto bail = [&](int code, const char* what) {
     batch_free(b);
     return fail(code, what);
@@ -402,11 +428,11 @@ int eq_batch_new(int64_t nscenes, const eq_scene_desc* scenes, int device, eq_ba
       m[(size_t)i * S] = m[(size_t)i * S + S - 1] = 1;
     }
   }
-  b->arena_floats = foff;
+  b->arena_elems = foff;
   b->marena_bytes = moff;
-  if (cudaMalloc(&b->arena, foff * sizeof(float)) != cudaSuccess)
+  if (cudaMalloc(&b->arena, foff * b->esize) != cudaSuccess)
     return bail(EQ_ERR_OOM, "cudaMalloc (batch fields)");
-  if (cudaMemsetAsync(b->arena, 0, foff * sizeof(float), b->stream) != cudaSuccess)
+  if (cudaMemsetAsync(b->arena, 0, foff * b->esize, b->stream) != cudaSuccess)
     return bail(EQ_ERR_CUDA, "cudaMemsetAsync (batch fields)");
   if (cudaMalloc(&b->marena, moff) != cudaSuccess ||
       cudaMalloc(&b->d_desc, nscenes * sizeof(eqk::BScene)) != cudaSuccess ||
@@ -434,7 +460,12 @@ int eq_batch_new(int64_t nscenes, const eq_scene_desc* scenes, int device, eq_ba
     return bail(EQ_ERR_ARG, "the largest scene is too large for the block wavefront");
   {
     const int blocks = (int)std::min<int64_t>(nscenes, 4096);
-    k_batch_init<<<blocks, 256, 0, b->stream>>>(b->arena, b->d_desc, nscenes);
+    if (storage == EQ_STORE_F16)
+      k_batch_init<__half><<<blocks, 256, 0, b->stream>>>(static_cast<__half*>(b->arena), b->d_desc, nscenes);
+    else if (storage == EQ_STORE_BF16)
+      k_batch_init<__nv_bfloat16><<<blocks, 256, 0, b->stream>>>(static_cast<__nv_bfloat16*>(b->arena), b->d_desc, nscenes);
+    else
+      k_batch_init<float><<<blocks, 256, 0, b->stream>>>(static_cast<float*>(b->arena), b->d_desc, nscenes);
     if (cudaGetLastError() != cudaSuccess) return bail(EQ_ERR_CUDA, "k_batch_init");
     b->launches++;
   }
@@ -518,18 +549,32 @@ static int batch_field_copy(eq_batch* b, int64_t scene, int field, void* host, u
   const int S = d.S, P = d.P;
   if (n != (uint64_t)S * S) return fail(EQ_ERR_ARG, "element count must be size*size");
   if (!host) return fail(EQ_ERR_ARG, "null host buffer");
-  float* dev = b->arena + d.foff + (size_t)field * d.fstride;
-  std::vector<float> diag(d.fstride, 0.0f);
+  uint8_t* dev = static_cast<uint8_t*>(b->arena) + (d.foff + (size_t)field * d.fstride) * b->esize;
+  std::vector<uint8_t> diag(d.fstride * b->esize, 0);
   float* dense = static_cast<float*>(host);
+  auto get = [&](size_t q) -> float {
+    if (b->storage == EQ_STORE_F16) return __half2float(reinterpret_cast<const __half*>(diag.data())[q]);
+    if (b->storage == EQ_STORE_BF16)
+      return __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(diag.data())[q]);
+    return reinterpret_cast<const float*>(diag.data())[q];
+  };
+  auto put = [&](size_t q, float v) {
+    if (b->storage == EQ_STORE_F16)
+      reinterpret_cast<__half*>(diag.data())[q] = __float2half_rn(v);
+    else if (b->storage == EQ_STORE_BF16)
+      reinterpret_cast<__nv_bfloat16*>(diag.data())[q] = __float2bfloat16_rn(v);
+    else
+      reinterpret_cast<float*>(diag.data())[q] = v;
+  };
   if (to_host) {
-    EQ_CUDA(cudaMemcpyAsync(diag.data(), dev, d.fstride * 4, cudaMemcpyDeviceToHost, b->stream));
+    EQ_CUDA(cudaMemcpyAsync(diag.data(), dev, diag.size(), cudaMemcpyDeviceToHost, b->stream));
     EQ_CUDA(cudaStreamSynchronize(b->stream));
     for (int j = 0; j < S; ++j)
-      for (int i = 0; i < S; ++i) dense[(size_t)j * S + i] = diag[eqk::dg_at(i, j, P)];
+      for (int i = 0; i < S; ++i) dense[(size_t)j * S + i] = get(eqk::dg_at(i, j, P));
   } else {
     for (int j = 0; j < S; ++j)
-      for (int i = 0; i < S; ++i) diag[eqk::dg_at(i, j, P)] = dense[(size_t)j * S + i];
-    EQ_CUDA(cudaMemcpyAsync(dev, diag.data(), d.fstride * 4, cudaMemcpyHostToDevice, b->stream));
+      for (int i = 0; i < S; ++i) put(eqk::dg_at(i, j, P), dense[(size_t)j * S + i]);
+    EQ_CUDA(cudaMemcpyAsync(dev, diag.data(), diag.size(), cudaMemcpyHostToDevice, b->stream));
     EQ_CUDA(cudaStreamSynchronize(b->stream));
   }
   return EQ_OK;
@@ -562,7 +607,7 @@ int eq_batch_set_tuning(eq_batch* b, int sweeps_per_pass, int blocks_per_sm) {
     return rc;
   }
   int active = 0;
-  EQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, eqk::k_batch_run, L.threads,
+  EQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, eqk::k_batch_run<float>, L.threads,
                                                         L.smem));
   if (active < blocks_per_sm) {
     b->nwmax = onw;
@@ -727,10 +772,10 @@ int eq_batch_autotune(eq_batch* b, int trial_frames, double* ms_out, int cap, in
         cand.emplace_back(w, bps);
     }
   }
-  float* snap = nullptr;
-  if (cudaMalloc(&snap, b->arena_floats * sizeof(float)) != cudaSuccess)
+  void* snap = nullptr;
+  if (cudaMalloc(&snap, b->arena_elems * b->esize) != cudaSuccess)
     return fail(EQ_ERR_OOM, "cudaMalloc (autotune snapshot)");
-  EQ_CUDA(cudaMemcpyAsync(snap, b->arena, b->arena_floats * 4, cudaMemcpyDeviceToDevice,
+  EQ_CUDA(cudaMemcpyAsync(snap, b->arena, b->arena_elems * b->esize, cudaMemcpyDeviceToDevice,
                           b->stream));
   const int onw = b->nwmax, obps = b->bps;
   int best = -1;
@@ -752,8 +797,8 @@ int eq_batch_autotune(eq_batch* b, int trial_frames, double* ms_out, int cap, in
       float t = 0.f;
       EQ_CUDA(cudaEventElapsedTime(&t, e0, e1));
       ms = (double)t / trial_frames;
-      EQ_CUDA(cudaMemcpyAsync(b->arena, snap, b->arena_floats * 4, cudaMemcpyDeviceToDevice,
-                              b->stream));
+      EQ_CUDA(cudaMemcpyAsync(b->arena, snap, b->arena_elems * b->esize,
+                              cudaMemcpyDeviceToDevice, b->stream));
       if (best < 0 || ms < best_ms) {
         best = (int)q;
         best_ms = ms;

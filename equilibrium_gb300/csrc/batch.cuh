@@ -10,6 +10,7 @@
 #pragma once
 #include "common.cuh"
 #include "kernels.cuh"
+#include "store.cuh"
 #include "wave.cuh"
 
 namespace eqk {
@@ -27,7 +28,7 @@ struct BScene {
 };
 
 struct BatchArgs {
-  float* arena;
+  void* arena;  // fields in the storage format (FP32, FP16 or BF16)
   const uint8_t* marena;
   const BScene* scenes;
   const int* order;  // queue position -> scene index
@@ -61,25 +62,26 @@ __device__ __forceinline__ void dg_for_cells(int ilo, int ihi, int jlo, int jhi,
   }
 }
 
-__device__ __forceinline__ void blk_sources(const BatchArgs& A, const BScene& sc, float* de,
-                                            float* scr, float* vx, float* vy) {
+template <class ST>
+__device__ __forceinline__ void blk_sources(const BatchArgs& A, const BScene& sc, ST* de,
+                                            ST* scr, ST* vx, ST* vy) {
   if (threadIdx.x != 0 || sc.nsrc <= 0) return;
   const int S = sc.S, P = sc.P;
   for (int s = sc.src_off; s < sc.src_off + sc.nsrc; ++s) {  // array order, like k_sources
     const int x = A.src_x[s] > (uint32_t)(S - 1) ? S - 1 : (int)A.src_x[s];
     const int y = A.src_y[s] > (uint32_t)(S - 1) ? S - 1 : (int)A.src_y[s];
     const size_t q = dg_at(x, y, P);
-    de[q] = fadd(de[q], A.src_d[s]);
-    scr[q] = fadd(scr[q], A.src_d[s]);
-    vx[q] = fadd(vx[q], A.src_u[s]);
-    vy[q] = fadd(vy[q], A.src_v[s]);
+    hs(de, q, fadd(hl(de, q), A.src_d[s]));
+    hs(scr, q, fadd(hl(scr, q), A.src_d[s]));
+    hs(vx, q, fadd(hl(vx, q), A.src_u[s]));
+    hs(vy, q, fadd(hl(vy, q), A.src_v[s]));
   }
 }
 
 // set_boundaries (fluid.rs:252-272): the order-independent per-cell map of
 // k_set_boundaries, then the corners from post-pass frame values.
-template <int MODE>
-__device__ void blk_bnd(float* __restrict__ x, const uint8_t* __restrict__ code,
+template <int MODE, class ST>
+__device__ void blk_bnd(ST* __restrict__ x, const uint8_t* __restrict__ code,
                         const uint8_t* rowfl, const uint8_t* colfl, int S, int P) {
   const int N = S - 2;
   if (MODE == kPassive) {
@@ -87,7 +89,7 @@ __device__ void blk_bnd(float* __restrict__ x, const uint8_t* __restrict__ code,
       const int side = q / N, k = q - side * N + 1;
       const int i = side == 0 ? k : (side == 1 ? k : (side == 2 ? 0 : S - 1));
       const int j = side == 0 ? 0 : (side == 1 ? S - 1 : k);
-      x[dg_at(i, j, P)] = dg_frame_after_pass<kPassive>(x, rowfl, colfl, S, P, i, j);
+      hs(x, dg_at(i, j, P), dg_frame_after_pass<kPassive>(x, rowfl, colfl, S, P, i, j));
     }
   } else {
     // neighbours: (i+-1, j) at q +- P, (i, j+-1) at q +- (P + 1). Only fluid
@@ -102,28 +104,30 @@ __device__ void blk_bnd(float* __restrict__ x, const uint8_t* __restrict__ code,
 #pragma unroll
       for (int r = 0; r < kU; ++r) {
         const size_t q = (size_t)d * P + jb + 32 * r;
+        // (negation is exact in every storage format)
         if (MODE == kRow) {
           if (c[r] & kCodeRowRight)
-            x[q] = -x[q + P];
+            hs(x, q, -hl(x, q + P));
           else if (c[r] & kCodeRowLeft)
-            x[q] = -x[q - P];
+            hs(x, q, -hl(x, q - P));
         } else {
           if (c[r] & kCodeColUp)
-            x[q] = -x[q - P - 1];
+            hs(x, q, -hl(x, q - P - 1));
           else if (c[r] & kCodeColDown)
-            x[q] = -x[q + P + 1];
+            hs(x, q, -hl(x, q + P + 1));
         }
       }
     });
   }
   __syncthreads();
-  if (threadIdx.x == 0) dg_corners<MODE>(x, rowfl, colfl, S, P);
+  if (threadIdx.x == 0) dg_corners<MODE, ST>(x, rowfl, colfl, S, P);
   __syncthreads();
 }
 
 // project's divergence + zero pressure (fluid.rs:339-352).
-__device__ void blk_divergence(const float* __restrict__ vx, const float* __restrict__ vy,
-                               float* __restrict__ p, float* __restrict__ div, int S, int P) {
+template <class ST>
+__device__ void blk_divergence(const ST* __restrict__ vx, const ST* __restrict__ vy,
+                               ST* __restrict__ p, ST* __restrict__ div, int S, int P) {
   const int N = S - 2;
   dg_for_cells(1, N, 1, N, P, [&](int d, int jb, int j1) {
     float a[kU], b[kU], c[kU], e[kU];
@@ -131,10 +135,10 @@ __device__ void blk_divergence(const float* __restrict__ vx, const float* __rest
     for (int r = 0; r < kU; ++r) {
       const int j = jb + 32 * r;
       const size_t q = (size_t)d * P + (j <= j1 ? j : jb);
-      a[r] = vx[q + P];
-      b[r] = vx[q - P];
-      c[r] = vy[q + P + 1];
-      e[r] = vy[q - P - 1];
+      a[r] = hl(vx, q + P);
+      b[r] = hl(vx, q - P);
+      c[r] = hl(vy, q + P + 1);
+      e[r] = hl(vy, q - P - 1);
     }
 #pragma unroll
     for (int r = 0; r < kU; ++r) {
@@ -142,16 +146,17 @@ __device__ void blk_divergence(const float* __restrict__ vx, const float* __rest
       if (j > j1) continue;
       const size_t q = (size_t)d * P + j;
       const float inner = fsub(fadd(fsub(a[r], b[r]), c[r]), e[r]);
-      div[q] = fdiv(fmul(-0.5f, inner), (float)S);
-      p[q] = 0.0f;
+      hs(div, q, fdiv(fmul(-0.5f, inner), (float)S));
+      hs(p, q, 0.0f);
     }
   });
   __syncthreads();
 }
 
 // project's gradient subtraction (fluid.rs:364-371).
-__device__ void blk_gradient(float* __restrict__ vx, float* __restrict__ vy,
-                             const float* __restrict__ p, int S, int P) {
+template <class ST>
+__device__ void blk_gradient(ST* __restrict__ vx, ST* __restrict__ vy,
+                             const ST* __restrict__ p, int S, int P) {
   const int N = S - 2;
   const float sf = (float)S;
   dg_for_cells(1, N, 1, N, P, [&](int d, int jb, int j1) {
@@ -160,31 +165,32 @@ __device__ void blk_gradient(float* __restrict__ vx, float* __restrict__ vy,
     for (int r = 0; r < kU; ++r) {
       const int j = jb + 32 * r;
       const size_t q = (size_t)d * P + (j <= j1 ? j : jb);
-      x[r] = vx[q];
-      y[r] = vy[q];
-      pr[r] = p[q + P];
-      pl[r] = p[q - P];
-      pd[r] = p[q + P + 1];
-      pu[r] = p[q - P - 1];
+      x[r] = hl(vx, q);
+      y[r] = hl(vy, q);
+      pr[r] = hl(p, q + P);
+      pl[r] = hl(p, q - P);
+      pd[r] = hl(p, q + P + 1);
+      pu[r] = hl(p, q - P - 1);
     }
 #pragma unroll
     for (int r = 0; r < kU; ++r) {
       const int j = jb + 32 * r;
       if (j > j1) continue;
       const size_t q = (size_t)d * P + j;
-      vx[q] = fsub(x[r], fmul(fmul(0.5f, fsub(pr[r], pl[r])), sf));
-      vy[q] = fsub(y[r], fmul(fmul(0.5f, fsub(pd[r], pu[r])), sf));
+      hs(vx, q, fsub(x[r], fmul(fmul(0.5f, fsub(pr[r], pl[r])), sf)));
+      hs(vy, q, fsub(y[r], fmul(fmul(0.5f, fsub(pd[r], pu[r])), sf)));
     }
   });
   __syncthreads();
 }
 
-__device__ __forceinline__ float dg_bilerp(const Backtrace& b, const float* __restrict__ d0,
+template <class ST>
+__device__ __forceinline__ float dg_bilerp(const Backtrace& b, const ST* __restrict__ d0,
                                            int P) {
-  const float A = d0[dg_at(b.i0, b.j0, P)];
-  const float B = d0[dg_at(b.i0, b.j1, P)];
-  const float C = d0[dg_at(b.i1, b.j0, P)];
-  const float D = d0[dg_at(b.i1, b.j1, P)];
+  const float A = hl(d0, dg_at(b.i0, b.j0, P));
+  const float B = hl(d0, dg_at(b.i0, b.j1, P));
+  const float C = hl(d0, dg_at(b.i1, b.j0, P));
+  const float D = hl(d0, dg_at(b.i1, b.j1, P));
   return fadd(fmul(b.s0, fadd(fmul(b.t0, A), fmul(b.t1, B))),
               fmul(b.s1, fadd(fmul(b.t0, C), fmul(b.t1, D))));
 }
@@ -193,7 +199,8 @@ __device__ __forceinline__ float dg_bilerp(const Backtrace& b, const float* __re
 // backtrace reached size-1), as an atomic minimum per row. `brk` is block
 // scratch of >= S ints. A frame's two velocity advects share u, v and so
 // share this pass.
-__device__ void blk_advect_breaks(const float* __restrict__ u, const float* __restrict__ v,
+template <class ST>
+__device__ void blk_advect_breaks(const ST* __restrict__ u, const ST* __restrict__ v,
                                   int S, int P, float dt0, int* brk) {
   const int N = S - 2;
   for (int j = threadIdx.x; j < S; j += blockDim.x) brk[j] = N + 1;
@@ -204,8 +211,8 @@ __device__ void blk_advect_breaks(const float* __restrict__ u, const float* __re
     for (int r = 0; r < kU; ++r) {
       const int j = jb + 32 * r;
       const size_t q = (size_t)d * P + (j <= j1 ? j : jb);
-      uu[r] = u[q];
-      vv[r] = v[q];
+      uu[r] = hl(u, q);
+      vv[r] = hl(v, q);
     }
 #pragma unroll
     for (int r = 0; r < kU; ++r) {
@@ -219,8 +226,9 @@ __device__ void blk_advect_breaks(const float* __restrict__ u, const float* __re
 // advect's second pass (fluid.rs:378-432): the cells before the row's break
 // by bilinear interpolation, the break cell with its left neighbour's new
 // value (the old ghost when it is column 1); the cells after it untouched.
-__device__ void blk_advect_write(float* __restrict__ d, const float* __restrict__ d0,
-                                 const float* __restrict__ u, const float* __restrict__ v,
+template <class ST>
+__device__ void blk_advect_write(ST* __restrict__ d, const ST* __restrict__ d0,
+                                 const ST* __restrict__ u, const ST* __restrict__ v,
                                  int S, int P, float dt0, const int* brk) {
   const int N = S - 2;
   dg_for_cells(1, N, 1, N, P, [&](int dd, int jb, int j1) {
@@ -234,8 +242,8 @@ __device__ void blk_advect_write(float* __restrict__ d, const float* __restrict_
       bj[r] = brk[jj];
       // the break cell copies its left neighbour's value: backtrace (i-1, j)
       const size_t qc = (size_t)dd * P + jj - (i == bj[r] ? P : 0);
-      uu[r] = u[qc];
-      vv[r] = v[qc];
+      uu[r] = hl(u, qc);
+      vv[r] = hl(v, qc);
     }
     Backtrace bt[kU];
 #pragma unroll
@@ -254,17 +262,18 @@ __device__ void blk_advect_write(float* __restrict__ d, const float* __restrict_
       const int i = dd - j;
       if (j > j1 || i > bj[r]) continue;
       const size_t q = (size_t)dd * P + j;
-      if (i == bj[r] && i == 1) val[r] = d[q - P];  // d[0, j]: column 0 is never written here
-      d[q] = val[r];
+      if (i == bj[r] && i == 1) val[r] = hl(d, q - P);  // d[0, j]: column 0 is never written here
+      hs(d, q, val[r]);
     }
   });
   __syncthreads();
 }
 
 // scratch_space = density.clone() (fluid.rs:523) over every cell.
-__device__ void blk_copy(float* __restrict__ dst, const float* __restrict__ src, int S, int P) {
+template <class ST>
+__device__ void blk_copy(ST* __restrict__ dst, const ST* __restrict__ src, int S, int P) {
   dg_for_cells(0, S - 1, 0, S - 1, P, [&](int d, int jb, int j1) {
-    float t[kU];
+    ST t[kU];
 #pragma unroll
     for (int r = 0; r < kU; ++r) {
       const int j = jb + 32 * r;
@@ -310,11 +319,13 @@ struct BOpList {
   BOp op[kMaxOps];
 };
 
-__device__ __forceinline__ float* bfield(const BatchArgs& A, const BScene& sc, int f) {
-  return A.arena + sc.foff + (size_t)f * sc.fstride;
+template <class ST>
+__device__ __forceinline__ ST* bfield(const BatchArgs& A, const BScene& sc, int f) {
+  return static_cast<ST*>(A.arena) + sc.foff + (size_t)f * sc.fstride;
 }
 
 // One operation on the scene in shared memory.
+template <class ST>
 __device__ __forceinline__ void blk_op(const BatchArgs& A, const BScene* ssc, const BOp& op,
                                        const WBufs& Bf, int* brk) {
   const BScene& sc = *ssc;
@@ -323,7 +334,7 @@ __device__ __forceinline__ void blk_op(const BatchArgs& A, const BScene* ssc, co
   const uint8_t* rowfl = code + sc.fstride;
   const uint8_t* colfl = rowfl + S;
   const float dt0 = fmul(sc.dt, (float)(S - 2));
-  WGrid G;
+  WGrid<ST> G;
   G.code = code;
   G.rowfl = rowfl;
   G.colfl = colfl;
@@ -331,13 +342,13 @@ __device__ __forceinline__ void blk_op(const BatchArgs& A, const BScene* ssc, co
   G.P = P;
   switch (op.kind) {
     case kOpSources:
-      blk_sources(A, sc, bfield(A, sc, 1), bfield(A, sc, 0), bfield(A, sc, 2), bfield(A, sc, 3));
+      blk_sources(A, sc, bfield<ST>(A, sc, 1), bfield<ST>(A, sc, 0), bfield<ST>(A, sc, 2), bfield<ST>(A, sc, 3));
       __syncthreads();
       break;
     case kOpDiffuse:
     case kOpLinSolve: {
-      G.x = bfield(A, sc, op.f[0]);
-      G.x0 = bfield(A, sc, op.f[1]);
+      G.x = bfield<ST>(A, sc, op.f[0]);
+      G.x0 = bfield<ST>(A, sc, op.f[1]);
       float a, cr;
       if (op.kind == kOpDiffuse) {
         // diffuse (fluid.rs:276-298): a = ((dt*diff)*sf)*sf, c = 1 + 4a
@@ -350,36 +361,36 @@ __device__ __forceinline__ void blk_op(const BatchArgs& A, const BScene* ssc, co
         cr = fdiv(1.0f, op.c);
       }
       if (op.mode == kRow)
-        wave_lin_solve<kRow>(G, Bf, sc.K, A.nwmax, a, cr);
+        wave_lin_solve<kRow, ST>(G, Bf, sc.K, A.nwmax, a, cr);
       else if (op.mode == kCol)
-        wave_lin_solve<kCol>(G, Bf, sc.K, A.nwmax, a, cr);
+        wave_lin_solve<kCol, ST>(G, Bf, sc.K, A.nwmax, a, cr);
       else
-        wave_lin_solve<kPassive>(G, Bf, sc.K, A.nwmax, a, cr);
+        wave_lin_solve<kPassive, ST>(G, Bf, sc.K, A.nwmax, a, cr);
       break;
     }
     case kOpDivergence: {
-      float* p = bfield(A, sc, op.f[2]);
-      float* div = bfield(A, sc, op.f[3]);
-      blk_divergence(bfield(A, sc, op.f[0]), bfield(A, sc, op.f[1]), p, div, S, P);
+      ST* p = bfield<ST>(A, sc, op.f[2]);
+      ST* div = bfield<ST>(A, sc, op.f[3]);
+      blk_divergence(bfield<ST>(A, sc, op.f[0]), bfield<ST>(A, sc, op.f[1]), p, div, S, P);
       blk_bnd<kPassive>(div, code, rowfl, colfl, S, P);
       blk_bnd<kPassive>(p, code, rowfl, colfl, S, P);
       break;
     }
     case kOpGradient: {
-      float* vx = bfield(A, sc, op.f[0]);
-      float* vy = bfield(A, sc, op.f[1]);
-      blk_gradient(vx, vy, bfield(A, sc, op.f[2]), S, P);
+      ST* vx = bfield<ST>(A, sc, op.f[0]);
+      ST* vy = bfield<ST>(A, sc, op.f[1]);
+      blk_gradient(vx, vy, bfield<ST>(A, sc, op.f[2]), S, P);
       blk_bnd<kRow>(vx, code, rowfl, colfl, S, P);
       blk_bnd<kCol>(vy, code, rowfl, colfl, S, P);
       break;
     }
     case kOpAdvectBreaks:
-      blk_advect_breaks(bfield(A, sc, op.f[0]), bfield(A, sc, op.f[1]), S, P, dt0, brk);
+      blk_advect_breaks(bfield<ST>(A, sc, op.f[0]), bfield<ST>(A, sc, op.f[1]), S, P, dt0, brk);
       break;
     case kOpAdvectWrite: {
-      float* d = bfield(A, sc, op.f[0]);
-      blk_advect_write(d, bfield(A, sc, op.f[1]), bfield(A, sc, op.f[2]),
-                       bfield(A, sc, op.f[3]), S, P, dt0, brk);
+      ST* d = bfield<ST>(A, sc, op.f[0]);
+      blk_advect_write(d, bfield<ST>(A, sc, op.f[1]), bfield<ST>(A, sc, op.f[2]),
+                       bfield<ST>(A, sc, op.f[3]), S, P, dt0, brk);
       if (op.mode == kRow)
         blk_bnd<kRow>(d, code, rowfl, colfl, S, P);
       else if (op.mode == kCol)
@@ -389,7 +400,7 @@ __device__ __forceinline__ void blk_op(const BatchArgs& A, const BScene* ssc, co
       break;
     }
     case kOpBnd: {
-      float* x = bfield(A, sc, op.f[0]);
+      ST* x = bfield<ST>(A, sc, op.f[0]);
       if (op.mode == kRow)
         blk_bnd<kRow>(x, code, rowfl, colfl, S, P);
       else if (op.mode == kCol)
@@ -399,7 +410,7 @@ __device__ __forceinline__ void blk_op(const BatchArgs& A, const BScene* ssc, co
       break;
     }
     case kOpCopy:
-      blk_copy(bfield(A, sc, op.f[0]), bfield(A, sc, op.f[1]), S, P);
+      blk_copy(bfield<ST>(A, sc, op.f[0]), bfield<ST>(A, sc, op.f[1]), S, P);
       break;
     default:
       break;
@@ -418,6 +429,7 @@ __device__ __forceinline__ WBufs batch_bufs(const BatchArgs& A) {
 
 // The operation list on every scene: persistent blocks draining the scene
 // queue (one launch = one frame when L is the frame's list).
+template <class ST>
 __global__ void __launch_bounds__(672, 1) k_batch_run(BatchArgs A, BOpList L) {
   extern __shared__ __align__(16) float bsm[];
   __shared__ int s_next;
@@ -433,7 +445,7 @@ __global__ void __launch_bounds__(672, 1) k_batch_run(BatchArgs A, BOpList L) {
     __syncthreads();
     const int q = s_next;
     if (q >= A.nscenes) break;
-    for (int k = 0; k < L.n; ++k) blk_op(A, &s_sc, L.op[k], Bf, brk);
+    for (int k = 0; k < L.n; ++k) blk_op<ST>(A, &s_sc, L.op[k], Bf, brk);
     __syncthreads();
   }
 }

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -878,3 +879,6 @@ int eq_fluid_set_spin_limit(eq_fluid* h, int64_t iterations) {
 
 // The batched form (many scenes per launch).
 #include "batch.cu"
+
+// The precision form (half storage, refined pressure).
+#include "half.cu"

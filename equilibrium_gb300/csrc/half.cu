@@ -1,0 +1,479 @@
+// Host side of the precision form (include/eqfluid.h, "half-storage fluid").
+// Compiled in the same translation unit as eqfluid.cu: the diffusion solves
+// reuse the plain handle's lin_solve wavefront on FP32 staging grids (the
+// reference's lexicographic Gauss-Seidel, 20 sweeps in FP32 arithmetic), the
+// pressure solves run mixed-precision refinement (mg.cuh).
+#include "mg.cuh"
+
+struct eq_hfluid {
+  eq_fluid* plain = nullptr;  // stream, mask, codes, lin_solve state, FP32 staging grids
+  int storage = EQ_STORE_F16;
+  void* f[6] = {};            // stored fields (2 bytes per cell), pitched like the plain grids
+  void* fblock = nullptr;
+  float* p32 = nullptr;       // pressure (FP32, pitched, with ghosts)
+  float* b32 = nullptr;       // right-hand side: project's div (FP32)
+  float* r32 = nullptr;       // fine residual (FP32)
+  double* d_acc = nullptr;    // FP64 reduction slots
+  double* h_acc = nullptr;    // pinned
+  struct Level {
+    int n, pitch;
+    void* e;  // FP32 correction
+    void* r;  // right-hand side in the storage format (scaled by 4^-level)
+  };
+  std::vector<Level> lv;
+  void* lvblock = nullptr;
+  double rtol = 1e-5;
+  int max_ir = 30;
+  eq_hstats stats{};
+  std::vector<uint32_t> sx, sy;
+  std::vector<float> sd, su, sv;
+  uint8_t* d_src = nullptr;
+  size_t d_src_cap = 0;
+};
+
+namespace {
+
+dim3 h_grid(int nx, int ny) { return dim3((nx + 31) / 32, (ny + 7) / 8); }
+const dim3 kHBlk(32, 8);
+
+int h_check(eq_hfluid* h) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  EQ_CUDA(cudaSetDevice(h->plain->device));
+  return EQ_OK;
+}
+
+void hfree(eq_hfluid* h) {
+  if (!h) return;
+  if (h->plain) {
+    cudaSetDevice(h->plain->device);
+    cudaStreamSynchronize(h->plain->stream);
+  }
+  cudaFree(h->fblock);
+  cudaFree(h->p32);
+  cudaFree(h->b32);
+  cudaFree(h->r32);
+  cudaFree(h->d_acc);
+  cudaFree(h->lvblock);
+  cudaFree(h->d_src);
+  if (h->h_acc) cudaFreeHost(h->h_acc);
+  free_handle(h->plain);
+  delete h;
+}
+
+template <class T>
+int h_bnd(eq_hfluid* h, int mode, T* x) {
+  eq_fluid* pl = h->plain;
+  const int S = (int)pl->S;
+  const dim3 g = h_grid(S, S);
+  if (mode == eqk::kRow)
+    eqk::k_h_bnd<eqk::kRow, T><<<g, kHBlk, 0, pl->stream>>>(x, pl->code, pl->rowfl, pl->colfl, S, pl->P);
+  else if (mode == eqk::kCol)
+    eqk::k_h_bnd<eqk::kCol, T><<<g, kHBlk, 0, pl->stream>>>(x, pl->code, pl->rowfl, pl->colfl, S, pl->P);
+  else
+    eqk::k_h_bnd<eqk::kPassive, T><<<g, kHBlk, 0, pl->stream>>>(x, pl->code, pl->rowfl, pl->colfl, S, pl->P);
+  return check_launch(pl);
+}
+
+int h_blocks(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 8); }
+
+// diffuse (fluid.rs:276-298): the stored x (initial guess) and x0 widened
+// into the plain handle's FP32 grids, the reference's lin_solve there, x
+// narrowed back.
+template <class T>
+int h_diffuse(eq_hfluid* h, int mode, T* x, const T* x0, float diffusion) {
+  eq_fluid* pl = h->plain;
+  const size_t n = pl->grid_elems();
+  float* xs = pl->field[0];
+  float* x0s = pl->field[1];
+  eqk::k_h_widen<T><<<h_blocks(n), 256, 0, pl->stream>>>(xs, x, n);
+  eqk::k_h_widen<T><<<h_blocks(n), 256, 0, pl->stream>>>(x0s, x0, n);
+  int rc = check_launch(pl);
+  if (rc) return rc;
+  if ((rc = launch_diffuse(pl, mode, xs, x0s, diffusion))) return rc;
+  eqk::k_h_narrow<T><<<h_blocks(n), 256, 0, pl->stream>>>(x, xs, n);
+  return check_launch(pl);
+}
+
+template <class T>
+void h_vcycle(eq_hfluid* h, size_t l) {
+  cudaStream_t st = h->plain->stream;
+  const auto& L = h->lv[l];
+  h->plain->launches += (l + 1 == h->lv.size()) ? 1 : 10;
+  float* e = static_cast<float*>(L.e);
+  T* r = static_cast<T*>(L.r);
+  const float s4 = std::ldexp(1.0f, 2 * (int)l);  // 4^l
+  if (l + 1 == h->lv.size()) {
+    eqk::k_mg_coarse<T><<<1, 1024, 0, st>>>(e, r, L.n, L.pitch, s4, 64);
+    return;
+  }
+  const dim3 gs = h_grid((L.n + 1) / 2, L.n);
+  for (int s = 0; s < 2; ++s) {
+    eqk::k_mg_smooth<T><<<gs, kHBlk, 0, st>>>(e, r, L.n, L.pitch, 0, s4);
+    eqk::k_mg_smooth<T><<<gs, kHBlk, 0, st>>>(e, r, L.n, L.pitch, 1, s4);
+  }
+  const auto& C = h->lv[l + 1];
+  eqk::k_mg_restrict<T><<<h_grid(C.n, C.n), kHBlk, 0, st>>>(
+      e, r, L.n, L.pitch, s4, static_cast<T*>(C.r), static_cast<float*>(C.e), C.n, C.pitch);
+  h_vcycle<T>(h, l + 1);
+  eqk::k_mg_prolong<<<h_grid(L.n, L.n), kHBlk, 0, st>>>(e, L.n, L.pitch,
+                                                       static_cast<const float*>(C.e), C.n,
+                                                       C.pitch);
+  for (int s = 0; s < 2; ++s) {
+    eqk::k_mg_smooth<T><<<gs, kHBlk, 0, st>>>(e, r, L.n, L.pitch, 1, s4);
+    eqk::k_mg_smooth<T><<<gs, kHBlk, 0, st>>>(e, r, L.n, L.pitch, 0, s4);
+  }
+}
+
+// project (fluid.rs:330-375) with the pressure solved by mixed-precision
+// refinement; p and div are the stored arrays the reference aliases.
+template <class T>
+int h_project(eq_hfluid* h, int which, T* vx, T* vy, T* ps, T* divs) {
+  eq_fluid* pl = h->plain;
+  cudaStream_t st = pl->stream;
+  const int S = (int)pl->S, P = pl->P, N = S - 2;
+  const size_t n = pl->grid_elems();
+  int rc;
+  // pre-projection divergence (statistics)
+  EQ_CUDA(cudaMemsetAsync(h->d_acc, 0, 4 * sizeof(double), st));
+  eqk::k_h_div_norm<T><<<h_blocks((size_t)N * N), 256, 0, st>>>(vx, vy, S, P, h->d_acc + 2);
+  eqk::k_h_divergence<T><<<h_grid(N, N), kHBlk, 0, st>>>(vx, vy, h->b32, divs, S, P);
+  if ((rc = check_launch(pl))) return rc;
+  if ((rc = h_bnd<T>(h, eqk::kPassive, divs))) return rc;
+  // p: the stored array's values (its frame is the Dirichlet value where a
+  // row / column has no fluid cell), interior zeroed
+  eqk::k_h_widen<T><<<h_blocks(n), 256, 0, st>>>(h->p32, ps, n);
+  eqk::k_ir_zero<<<h_grid(N, N), kHBlk, 0, st>>>(h->p32, S, P);
+  if ((rc = check_launch(pl))) return rc;
+  const auto& L0 = h->lv[0];
+  double bnorm = 0.0, rel = 0.0, prev = 0.0;
+  int it = 0, slow = 0;
+  for (;; ++it) {
+    EQ_CUDA(cudaMemsetAsync(h->d_acc, 0, 2 * sizeof(double), st));
+    eqk::k_ir_residual<<<h_blocks((size_t)N * N), 256, 0, st>>>(h->p32, h->b32, S, P, pl->rowfl,
+                                                               pl->colfl, h->r32, h->d_acc);
+    if ((rc = check_launch(pl))) return rc;
+    EQ_CUDA(cudaMemcpyAsync(h->h_acc, h->d_acc, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    EQ_CUDA(cudaStreamSynchronize(st));
+    const double cnt = (double)N * N;
+    const double mean = h->h_acc[0] / cnt;
+    const double rn = std::sqrt(std::max(0.0, h->h_acc[1] - cnt * mean * mean));
+    if (it == 0) {
+      bnorm = rn;
+      h->stats.div_norm_before[which] = std::sqrt(h->h_acc[2]);
+    }
+    rel = bnorm > 0.0 ? rn / bnorm : 0.0;
+    if (rel <= h->rtol || it >= h->max_ir || rn == 0.0) break;
+    // FP32 floor: the residual of the FP32-rounded pressure (about
+    // eps32 * ||A|| * ||p||) can exceed rtol * ||div|| on large grids; stop
+    // once two rounds in a row gain less than a factor 2.
+    if (it > 0) slow = (rel > 0.5 * prev) ? slow + 1 : 0;
+    if (slow >= 2) break;
+    prev = rel;
+    const double scale = rn / std::sqrt(cnt);
+    eqk::k_ir_scale<T><<<h_grid(N, N), kHBlk, 0, st>>>(h->r32, S, P, (float)mean,
+                                                       (float)(1.0 / scale),
+                                                       static_cast<T*>(L0.r), L0.pitch);
+    EQ_CUDA(cudaMemsetAsync(L0.e, 0, (size_t)L0.pitch * L0.n * sizeof(float), st));
+    h_vcycle<T>(h, 0);
+    eqk::k_ir_update<<<h_grid(N, N), kHBlk, 0, st>>>(h->p32, S, P,
+                                                     static_cast<const float*>(L0.e), L0.pitch,
+                                                     (float)scale);
+    if ((rc = check_launch(pl))) return rc;
+  }
+  h->stats.ir_iterations[which] = it;
+  h->stats.rel_residual[which] = rel;
+  // zero-mean pressure where every frame neighbour is a Neumann copy (the
+  // operator's null space; a Dirichlet frame would fix the constant itself)
+  {
+    bool neumann = true;
+    const std::vector<uint8_t>& m = pl->host_cells;
+    for (int k = 1; k <= N && neumann; ++k) {
+      bool rf = false, cf = false;
+      for (int q = 1; q <= N; ++q) {
+        rf = rf || !m[(size_t)k * S + q];
+        cf = cf || !m[(size_t)q * S + k];
+      }
+      neumann = rf && cf;
+    }
+    if (neumann) {
+      EQ_CUDA(cudaMemsetAsync(h->d_acc, 0, 2 * sizeof(double), st));
+      eqk::k_ir_sum<<<h_blocks((size_t)N * N), 256, 0, st>>>(h->p32, S, P, h->d_acc);
+      eqk::k_ir_center<<<h_grid(N, N), kHBlk, 0, st>>>(h->p32, S, P, h->d_acc);
+      if ((rc = check_launch(pl))) return rc;
+    }
+  }
+  // p's frame by set_boundaries(Passive) (+ corners), stored into p's array
+  eqk::k_set_boundaries<eqk::kPassive><<<h_grid(S, S), kHBlk, 0, st>>>(h->p32, pl->code, pl->rowfl,
+                                                                      pl->colfl, S, P);
+  eqk::k_h_narrow<T><<<h_blocks(n), 256, 0, st>>>(ps, h->p32, n);
+  eqk::k_h_gradient<T><<<h_grid(N, N), kHBlk, 0, st>>>(vx, vy, h->p32, S, P);
+  if ((rc = check_launch(pl))) return rc;
+  if ((rc = h_bnd<T>(h, eqk::kRow, vx)) || (rc = h_bnd<T>(h, eqk::kCol, vy))) return rc;
+  EQ_CUDA(cudaMemsetAsync(h->d_acc + 3, 0, sizeof(double), st));
+  eqk::k_h_div_norm<T><<<h_blocks((size_t)N * N), 256, 0, st>>>(vx, vy, S, P, h->d_acc + 3);
+  EQ_CUDA(cudaMemcpyAsync(h->h_acc + 3, h->d_acc + 3, sizeof(double), cudaMemcpyDeviceToHost, st));
+  EQ_CUDA(cudaStreamSynchronize(st));
+  h->stats.div_norm[which] = std::sqrt(h->h_acc[3]);
+  return check_launch(pl);
+}
+
+template <class T>
+int h_advect(eq_hfluid* h, int mode, T* d, const T* d0, const T* u, const T* v) {
+  eq_fluid* pl = h->plain;
+  const int S = (int)pl->S, N = S - 2;
+  const float dt0 = pl->dt * (float)(S - 2);
+  const int threads = std::min(256, ((N + 31) / 32) * 32);
+  eqk::k_h_advect_rows<T><<<N, threads, 0, pl->stream>>>(d, d0, u, v, S, pl->P, dt0);
+  int rc = check_launch(pl);
+  if (rc) return rc;
+  return h_bnd<T>(h, mode, d);
+}
+
+template <class T>
+int h_step(eq_hfluid* h) {
+  eq_fluid* pl = h->plain;
+  int rc = upload_mask(pl);
+  if (rc) return rc;
+  T* sc = static_cast<T*>(h->f[EQ_FIELD_SCRATCH]);
+  T* de = static_cast<T*>(h->f[EQ_FIELD_DENSITY]);
+  T* vx = static_cast<T*>(h->f[EQ_FIELD_VX]);
+  T* vy = static_cast<T*>(h->f[EQ_FIELD_VY]);
+  T* vx0 = static_cast<T*>(h->f[EQ_FIELD_VX0]);
+  T* vy0 = static_cast<T*>(h->f[EQ_FIELD_VY0]);
+  const int64_t ns = (int64_t)h->sx.size();
+  if (ns > 0) {
+    const size_t bytes = (size_t)ns * 20;
+    if (bytes > h->d_src_cap) {
+      EQ_CUDA(cudaStreamSynchronize(pl->stream));
+      cudaFree(h->d_src);
+      h->d_src = nullptr;
+      h->d_src_cap = 0;
+      if (cudaMalloc(&h->d_src, bytes) != cudaSuccess) return fail(EQ_ERR_OOM, "cudaMalloc (sources)");
+      h->d_src_cap = bytes;
+    }
+    std::vector<uint8_t> buf(bytes);
+    std::memcpy(buf.data(), h->sx.data(), ns * 4);
+    std::memcpy(buf.data() + ns * 4, h->sy.data(), ns * 4);
+    std::memcpy(buf.data() + ns * 8, h->sd.data(), ns * 4);
+    std::memcpy(buf.data() + ns * 12, h->su.data(), ns * 4);
+    std::memcpy(buf.data() + ns * 16, h->sv.data(), ns * 4);
+    EQ_CUDA(cudaMemcpyAsync(h->d_src, buf.data(), bytes, cudaMemcpyHostToDevice, pl->stream));
+    const uint32_t* dx = reinterpret_cast<const uint32_t*>(h->d_src);
+    const float* dv = reinterpret_cast<const float*>(h->d_src + ns * 8);
+    eqk::k_h_sources<T><<<1, 1, 0, pl->stream>>>(de, sc, vx, vy, (int)pl->S, pl->P, ns, dx,
+                                                 dx + ns, dv, dv + ns, dv + 2 * ns);
+    if ((rc = check_launch(pl))) return rc;
+    EQ_CUDA(cudaStreamSynchronize(pl->stream));  // the staging vector goes out of scope
+    h->sx.clear();
+    h->sy.clear();
+    h->sd.clear();
+    h->su.clear();
+    h->sv.clear();
+  }
+  if ((rc = h_diffuse<T>(h, eqk::kRow, vx0, vx, pl->visc))) return rc;
+  if ((rc = h_diffuse<T>(h, eqk::kCol, vy0, vy, pl->visc))) return rc;
+  if ((rc = h_project<T>(h, 0, vx0, vy0, vx, vy))) return rc;
+  if ((rc = h_advect<T>(h, eqk::kRow, vx, vx0, vx0, vy0))) return rc;
+  if ((rc = h_advect<T>(h, eqk::kCol, vy, vy0, vx0, vy0))) return rc;
+  if ((rc = h_project<T>(h, 1, vx, vy, vx0, vy0))) return rc;
+  if ((rc = h_diffuse<T>(h, eqk::kPassive, sc, de, pl->diff))) return rc;
+  if ((rc = h_advect<T>(h, eqk::kPassive, de, sc, vx, vy))) return rc;
+  const size_t n = pl->grid_elems();
+  eqk::k_h_copy<T><<<h_blocks(n), 256, 0, pl->stream>>>(sc, de, n);
+  return check_launch(pl);
+}
+
+template <class T>
+int h_init(eq_hfluid* h) {
+  eq_fluid* pl = h->plain;
+  const int S = (int)pl->S;
+  eqk::k_h_init<T><<<h_grid(S, S), kHBlk, 0, pl->stream>>>(
+      static_cast<T*>(h->f[0]), static_cast<T*>(h->f[1]), static_cast<T*>(h->f[2]),
+      static_cast<T*>(h->f[3]), S, pl->P);
+  return check_launch(pl);
+}
+
+}  // namespace
+
+extern "C" {
+
+int eq_hfluid_new(const eq_fluid_configs* fluid, const eq_simulation_configs* sim, int storage,
+                  double pressure_rtol, int32_t max_refinements, int device, eq_hfluid** out) {
+  if (!fluid || !sim || !out) return fail(EQ_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (storage != EQ_STORE_F16 && storage != EQ_STORE_BF16)
+    return fail(EQ_ERR_ARG, "storage must be EQ_STORE_F16 or EQ_STORE_BF16");
+  if (sim->size < 20) return fail(EQ_ERR_ARG, "size must be >= 20 (fluid.rs:534 underflows)");
+  if (sim->size > 32768) return fail(EQ_ERR_ARG, "size too large");
+  if (sim->frames < 0) return fail(EQ_ERR_ARG, "frames must be >= 0");
+  if (!(pressure_rtol > 0.0) || max_refinements < 1)
+    return fail(EQ_ERR_ARG, "pressure_rtol must be > 0 and max_refinements >= 1");
+  eq_hfluid* h = new eq_hfluid();
+  h->storage = storage;
+  h->rtol = pressure_rtol;
+  h->max_ir = max_refinements;
+  int rc = alloc_handle(sim->size, device, &h->plain);
+  if (rc) {
+    delete h;
+    return rc;
+  }
+  eq_fluid* pl = h->plain;
+  pl->dt = sim->delta_t;
+  pl->frames = sim->frames;
+  pl->diff = fluid->diffusion;
+  pl->visc = fluid->viscousity;
+  pl->has_perlin_noise = fluid->has_perlin_noise;
+  const uint32_t S = sim->size;
+  for (uint32_t i = 0; i < S; ++i) {  // init_walls (fluid.rs:552-570)
+    pl->host_cells[i] = pl->host_cells[(size_t)(S - 1) * S + i] = 1;
+    pl->host_cells[(size_t)i * S] = pl->host_cells[(size_t)i * S + S - 1] = 1;
+  }
+  pl->mask_dirty = true;
+  const size_t g = pl->grid_elems();
+  auto bail = [&](int code, const char* what) {
+    hfree(h);
+    return fail(code, what);
+  };
+  if (cudaMalloc(&h->fblock, 6 * g * 2) != cudaSuccess ||
+      cudaMalloc(&h->p32, g * 4) != cudaSuccess || cudaMalloc(&h->b32, g * 4) != cudaSuccess ||
+      cudaMalloc(&h->r32, g * 4) != cudaSuccess ||
+      cudaMalloc(&h->d_acc, 4 * sizeof(double)) != cudaSuccess)
+    return bail(EQ_ERR_OOM, "cudaMalloc (half fields)");
+  if (cudaMallocHost(&h->h_acc, 4 * sizeof(double)) != cudaSuccess)
+    return bail(EQ_ERR_OOM, "cudaMallocHost");
+  for (int q = 0; q < 6; ++q) h->f[q] = static_cast<uint8_t*>(h->fblock) + (size_t)q * g * 2;
+  if (cudaMemsetAsync(h->fblock, 0, 6 * g * 2, pl->stream) != cudaSuccess ||
+      cudaMemsetAsync(h->p32, 0, g * 4, pl->stream) != cudaSuccess ||
+      cudaMemsetAsync(h->b32, 0, g * 4, pl->stream) != cudaSuccess ||
+      cudaMemsetAsync(h->r32, 0, g * 4, pl->stream) != cudaSuccess)
+    return bail(EQ_ERR_CUDA, "cudaMemsetAsync");
+  // multigrid levels: n, ceil(n/2), ... down to <= 4 cells per side
+  size_t bytes = 0;
+  for (int n = (int)S - 2;; n = (n + 1) / 2) {
+    eq_hfluid::Level L;
+    L.n = n;
+    L.pitch = ((n + 63) / 64) * 64;
+    L.e = L.r = nullptr;
+    h->lv.push_back(L);
+    bytes += (size_t)L.pitch * n * (4 + 2);
+    if (n <= 4) break;
+  }
+  if (cudaMalloc(&h->lvblock, bytes) != cudaSuccess) return bail(EQ_ERR_OOM, "cudaMalloc (levels)");
+  EQ_CUDA(cudaMemsetAsync(h->lvblock, 0, bytes, pl->stream));
+  uint8_t* base = static_cast<uint8_t*>(h->lvblock);
+  for (auto& L : h->lv) {
+    L.e = base;  // FP32 correction
+    base += (size_t)L.pitch * L.n * 4;
+    L.r = base;  // stored right-hand side
+    base += (size_t)L.pitch * L.n * 2;
+  }
+  rc = storage == EQ_STORE_F16 ? h_init<__half>(h) : h_init<__nv_bfloat16>(h);
+  if (rc) {
+    hfree(h);
+    return rc;
+  }
+  if (cudaStreamSynchronize(pl->stream) != cudaSuccess) return bail(EQ_ERR_CUDA, "init");
+  *out = h;
+  return EQ_OK;
+}
+
+int eq_hfluid_free(eq_hfluid* h) {
+  hfree(h);
+  return EQ_OK;
+}
+
+int eq_hfluid_fill_obstacle(eq_hfluid* h, int64_t x0, int64_t y0, int64_t x1, int64_t y1) {
+  int rc = h_check(h);
+  if (rc) return rc;
+  return eq_fluid_fill_obstacle(h->plain, x0, y0, x1, y1);
+}
+
+int eq_hfluid_add_sources(eq_hfluid* h, int64_t n, const uint32_t* x, const uint32_t* y,
+                          const float* density, const float* vx, const float* vy) {
+  int rc = h_check(h);
+  if (rc) return rc;
+  if (n < 0) return fail(EQ_ERR_ARG, "n must be >= 0");
+  if (n > 0 && (!x || !y)) return fail(EQ_ERR_ARG, "null coordinates");
+  for (int64_t s = 0; s < n; ++s) {
+    h->sx.push_back(x[s]);
+    h->sy.push_back(y[s]);
+    h->sd.push_back(density ? density[s] : 0.0f);
+    h->su.push_back(vx ? vx[s] : 0.0f);
+    h->sv.push_back(vy ? vy[s] : 0.0f);
+  }
+  return EQ_OK;
+}
+
+int eq_hfluid_step(eq_hfluid* h) {
+  int rc = h_check(h);
+  if (rc) return rc;
+  rc = h->storage == EQ_STORE_F16 ? h_step<__half>(h) : h_step<__nv_bfloat16>(h);
+  if (rc) return rc;
+  return read_err_word(h->plain);
+}
+
+int eq_hfluid_synchronize(eq_hfluid* h) {
+  int rc = h_check(h);
+  if (rc) return rc;
+  EQ_CUDA(cudaStreamSynchronize(h->plain->stream));
+  return read_err_word(h->plain);
+}
+
+static int hfield_copy(eq_hfluid* h, int field, float* host, uint64_t n, bool to_host) {
+  int rc = h_check(h);
+  if (rc) return rc;
+  if ((rc = check_field(field))) return rc;
+  eq_fluid* pl = h->plain;
+  if (n != (uint64_t)pl->S * pl->S) return fail(EQ_ERR_ARG, "element count must be size*size");
+  if (!host) return fail(EQ_ERR_ARG, "null host buffer");
+  const size_t g = pl->grid_elems();
+  float* stage = pl->field[2];  // FP32 staging grid of the plain handle
+  const size_t w = (size_t)pl->S * sizeof(float);
+  if (to_host) {
+    if (h->storage == EQ_STORE_F16)
+      eqk::k_h_widen<__half><<<h_blocks(g), 256, 0, pl->stream>>>(stage, static_cast<__half*>(h->f[field]), g);
+    else
+      eqk::k_h_widen<__nv_bfloat16><<<h_blocks(g), 256, 0, pl->stream>>>(stage, static_cast<__nv_bfloat16*>(h->f[field]), g);
+    if ((rc = check_launch(pl))) return rc;
+    EQ_CUDA(cudaMemcpy2DAsync(host, w, stage, (size_t)pl->P * 4, w, pl->S, cudaMemcpyDeviceToHost,
+                              pl->stream));
+  } else {
+    EQ_CUDA(cudaMemcpy2DAsync(stage, (size_t)pl->P * 4, host, w, w, pl->S, cudaMemcpyHostToDevice,
+                              pl->stream));
+    if (h->storage == EQ_STORE_F16)
+      eqk::k_h_narrow<__half><<<h_blocks(g), 256, 0, pl->stream>>>(static_cast<__half*>(h->f[field]), stage, g);
+    else
+      eqk::k_h_narrow<__nv_bfloat16><<<h_blocks(g), 256, 0, pl->stream>>>(static_cast<__nv_bfloat16*>(h->f[field]), stage, g);
+    if ((rc = check_launch(pl))) return rc;
+  }
+  EQ_CUDA(cudaStreamSynchronize(pl->stream));
+  return EQ_OK;
+}
+
+int eq_hfluid_read_field(eq_hfluid* h, int field, float* host, uint64_t n) {
+  return hfield_copy(h, field, host, n, true);
+}
+
+int eq_hfluid_write_field(eq_hfluid* h, int field, const float* host, uint64_t n) {
+  return hfield_copy(h, field, const_cast<float*>(host), n, false);
+}
+
+int eq_hfluid_stats(const eq_hfluid* h, eq_hstats* out) {
+  if (!h || !out) return fail(EQ_ERR_ARG, "null argument");
+  *out = h->stats;
+  return EQ_OK;
+}
+
+int eq_hfluid_get_stream(eq_hfluid* h, void** stream) {
+  if (!h || !stream) return fail(EQ_ERR_ARG, "null argument");
+  *stream = (void*)h->plain->stream;
+  return EQ_OK;
+}
+
+int eq_hfluid_launch_count(const eq_hfluid* h, uint64_t* count) {
+  if (!h || !count) return fail(EQ_ERR_ARG, "null argument");
+  *count = h->plain->launches;
+  return EQ_OK;
+}
+
+}  // extern "C"

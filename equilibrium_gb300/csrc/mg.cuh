@@ -1,0 +1,250 @@
+// Mixed-precision iterative refinement for project's pressure equation
+// (fluid.rs:353-362 solves it with a fixed 20 Gauss-Seidel sweeps; the
+// precision form solves it to a relative residual instead).
+//
+// The equation is lin_solve(Passive, p, div, 1, 4) at its fixed point:
+//   4 p(i,j) - (p(i-1,j) + p(i+1,j) + p(i,j-1) + p(i,j+1)) = div(i,j)
+// on the N x N interior, with set_boundaries(Passive)'s ghost rule: a frame
+// neighbour equals the adjacent interior cell where its row / column holds a
+// fluid cell (Neumann), else it keeps its stored value (Dirichlet). Obstacles
+// do not enter it (the Passive pass ignores them, fluid.rs:252-272).
+//
+// Refinement: p (FP32) starts at 0; each round computes the FP32 residual
+// r = div - A p with FP64 sums (mean and norm), stops when the mean-free norm
+// is below rtol times the first one (the mean is in the null space of the
+// pure-Neumann operator, so no solver can remove it), else scales r to unit
+// RMS, stores it in the low-precision format and runs one multigrid V-cycle
+// for the correction e (low-precision storage, FP32 arithmetic), p += s e.
+//
+// Multigrid: cell-centred, coarsening by 2, red-black Gauss-Seidel smoothing
+// with the Neumann rule solved locally (e = (r + sum of inside neighbours) /
+// (number of inside neighbours)), bilinear prolongation with reflection at the
+// walls, the coarsest level solved by one block in shared memory. The
+// right-hand sides of every level are STORED in the low-precision format; a
+// coarse cell holds the AVERAGE of its 2 x 2 children's residuals (the sum,
+// which the coarse 5-point stencil needs, divided by 4 per level so that the
+// stored values stay O(1) in FP16's range), and level l multiplies its stored
+// right-hand side by 4^l when it uses it. The corrections e stay FP32: a
+// Poisson correction's smooth part exceeds its rough part by up to N^2 / pi^2
+// (about 2^19 at N = 2048), more than an FP16 or BF16 significand holds, so a
+// low-precision e would round the rough part away.
+#pragma once
+#include "half.cuh"
+
+namespace eqk {
+
+// One red-black colour of Gauss-Seidel on A e = rs * s4 (level of n x n
+// cells, rs stored, s4 = 4^level).
+template <class T>
+__global__ void k_mg_smooth(float* __restrict__ e, const T* __restrict__ r, int n, int pitch,
+                            int color, float s4) {
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int I2 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int I = 2 * I2 + ((J + color) & 1);
+  if (I >= n || J >= n) return;
+  const size_t q = (size_t)J * pitch + I;
+  float sum = 0.0f;
+  int nin = 0;
+  if (I > 0) { sum += e[q - 1]; ++nin; }
+  if (I < n - 1) { sum += e[q + 1]; ++nin; }
+  if (J > 0) { sum += e[q - pitch]; ++nin; }
+  if (J < n - 1) { sum += e[q + pitch]; ++nin; }
+  e[q] = (hl(r, q) * s4 + sum) / (float)nin;
+}
+
+// (r * s4 - A e) at one cell.
+template <class T>
+__device__ __forceinline__ float mg_resid(const float* e, const T* r, int I, int J, int n,
+                                          int pitch, float s4) {
+  const size_t q = (size_t)J * pitch + I;
+  const float c = e[q];
+  float sum = 0.0f;
+  int nin = 0;
+  if (I > 0) { sum += e[q - 1]; ++nin; }
+  if (I < n - 1) { sum += e[q + 1]; ++nin; }
+  if (J > 0) { sum += e[q - pitch]; ++nin; }
+  if (J < n - 1) { sum += e[q + pitch]; ++nin; }
+  return hl(r, q) * s4 - ((float)nin * c - sum);
+}
+
+// rc = (sum over the 2 x 2 children of the residual) / (4 s4) (the stored
+// form of the coarse right-hand side); ec = 0.
+template <class T>
+__global__ void k_mg_restrict(const float* __restrict__ e, const T* __restrict__ r, int n,
+                              int pitch, float s4, T* __restrict__ rc, float* __restrict__ ec,
+                              int nc, int pitchc) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  if (I >= nc || J >= nc) return;
+  float s = 0.0f;
+#pragma unroll
+  for (int b = 0; b < 2; ++b)
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+      const int i = 2 * I + a, j = 2 * J + b;
+      if (i < n && j < n) s += mg_resid(e, r, i, j, n, pitch, s4);
+    }
+  hs(rc, (size_t)J * pitchc + I, s / (4.0f * s4));
+  ec[(size_t)J * pitchc + I] = 0.0f;
+}
+
+// e += bilinear interpolation of the coarse correction (weights 9/16, 3/16,
+// 3/16, 1/16; a coarse neighbour beyond the wall reflects to the parent).
+__global__ void k_mg_prolong(float* __restrict__ e, int n, int pitch, const float* __restrict__ ec,
+                             int nc, int pitchc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= n || j >= n) return;
+  const int I = i >> 1, J = j >> 1;
+  int In = I + ((i & 1) ? 1 : -1), Jn = J + ((j & 1) ? 1 : -1);
+  if (In < 0 || In >= nc) In = I;
+  if (Jn < 0 || Jn >= nc) Jn = J;
+  const float v = 0.5625f * ec[(size_t)J * pitchc + I] + 0.1875f * ec[(size_t)J * pitchc + In] +
+                  0.1875f * ec[(size_t)Jn * pitchc + I] + 0.0625f * ec[(size_t)Jn * pitchc + In];
+  e[(size_t)j * pitch + i] += v;
+}
+
+// The coarsest level (n <= 32) by one block of 1024 threads in shared memory:
+// `iters` red-black sweeps from e = 0, then the mean removed (the pure
+// Neumann problem determines e only up to a constant).
+template <class T>
+__global__ void __launch_bounds__(1024) k_mg_coarse(float* __restrict__ e, const T* __restrict__ r,
+                                                    int n, int pitch, float s4, int iters) {
+  __shared__ float se[32][33], sr[32][33];
+  __shared__ float ssum[32];
+  const int I = threadIdx.x & 31, J = threadIdx.x >> 5;
+  const bool in = I < n && J < n;
+  se[J][I] = 0.0f;
+  sr[J][I] = in ? hl(r, (size_t)J * pitch + I) * s4 : 0.0f;
+  __syncthreads();
+  for (int it = 0; it < iters; ++it) {
+    for (int color = 0; color < 2; ++color) {
+      if (in && ((I + J) & 1) == color) {
+        float sum = 0.0f;
+        int nin = 0;
+        if (I > 0) { sum += se[J][I - 1]; ++nin; }
+        if (I < n - 1) { sum += se[J][I + 1]; ++nin; }
+        if (J > 0) { sum += se[J - 1][I]; ++nin; }
+        if (J < n - 1) { sum += se[J + 1][I]; ++nin; }
+        se[J][I] = (sr[J][I] + sum) / (float)nin;
+      }
+      __syncthreads();
+    }
+  }
+  float v = in ? se[J][I] : 0.0f;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (I == 0) ssum[J] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+    for (int w = 0; w < 32; ++w) t += ssum[w];
+    ssum[0] = t / (float)(n * n);
+  }
+  __syncthreads();
+  if (in) e[(size_t)J * pitch + I] = se[J][I] - ssum[0];
+}
+
+// ---- refinement on the fine grid (f32 pressure, pitched like the fields) ----
+
+__device__ __forceinline__ void block_add_f64x2(double a, double b, double* out) {
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  __shared__ double pa[32], pb[32];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    pa[w] = a;
+    pb[w] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0.0, tb = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      ta += pa[k];
+      tb += pb[k];
+    }
+    atomicAdd(out, ta);
+    atomicAdd(out + 1, tb);
+  }
+}
+
+// r = b - A p on the interior (FP32), with FP64 sums of r and r^2.
+__global__ void k_ir_residual(const float* __restrict__ p, const float* __restrict__ b, int S,
+                              int P, const uint8_t* __restrict__ rowfl,
+                              const uint8_t* __restrict__ colfl, float* __restrict__ r,
+                              double* __restrict__ acc) {
+  const int N = S - 2;
+  double s1 = 0.0, s2 = 0.0;
+  const size_t n = (size_t)N * N;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(k / N) + 1, i = (int)(k % N) + 1;
+    const size_t q = (size_t)j * P + i;
+    const float c = p[q];
+    const float L = (i == 1) ? (rowfl[j] ? c : p[q - 1]) : p[q - 1];
+    const float R = (i == N) ? (rowfl[j] ? c : p[q + 1]) : p[q + 1];
+    const float U = (j == 1) ? (colfl[i] ? c : p[q - P]) : p[q - P];
+    const float D = (j == N) ? (colfl[i] ? c : p[q + P]) : p[q + P];
+    const float res = b[q] - (4.0f * c - (((L + R) + U) + D));
+    r[q] = res;
+    s1 += res;
+    s2 += (double)res * res;
+  }
+  block_add_f64x2(s1, s2, acc);
+}
+
+// Level-0 right-hand side: (r - mean) / scale in the storage format.
+template <class T>
+__global__ void k_ir_scale(const float* __restrict__ r, int S, int P, float mean, float inv_scale,
+                           T* __restrict__ r0, int pitch0) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int N = S - 2;
+  if (I >= N || J >= N) return;
+  hs(r0, (size_t)J * pitch0 + I, (r[(size_t)(J + 1) * P + I + 1] - mean) * inv_scale);
+}
+
+// p += scale * e0 on the interior.
+__global__ void k_ir_update(float* __restrict__ p, int S, int P, const float* __restrict__ e0,
+                            int pitch0, float scale) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int N = S - 2;
+  if (I >= N || J >= N) return;
+  const size_t q = (size_t)(J + 1) * P + I + 1;
+  p[q] += scale * e0[(size_t)J * pitch0 + I];
+}
+
+// Sum of p over the interior (FP64) into acc[0].
+__global__ void k_ir_sum(const float* __restrict__ p, int S, int P, double* __restrict__ acc) {
+  const int N = S - 2;
+  double s1 = 0.0;
+  const size_t n = (size_t)N * N;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(k / N) + 1, i = (int)(k % N) + 1;
+    s1 += p[(size_t)j * P + i];
+  }
+  block_add_f64x2(s1, 0.0, acc);
+}
+
+// p -= mean(p) on the interior: the pure-Neumann solution's free constant is
+// fixed at zero mean.
+__global__ void k_ir_center(float* __restrict__ p, int S, int P, const double* __restrict__ acc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int N = S - 2;
+  if (i > N || j > N) return;
+  p[(size_t)j * P + i] -= (float)(acc[0] / ((double)N * N));
+}
+
+// p = 0 on the interior (project's `p[idx] = 0.0`, fluid.rs:349).
+__global__ void k_ir_zero(float* __restrict__ p, int S, int P) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > S - 2 || j > S - 2) return;
+  p[(size_t)j * P + i] = 0.0f;
+}
+
+}  // namespace eqk

@@ -43,6 +43,7 @@
 #pragma once
 #include "common.cuh"
 #include "kernels.cuh"
+#include "store.cuh"
 
 namespace eqk {
 
@@ -59,31 +60,31 @@ __host__ __device__ inline size_t dg_size(int S, int P) { return (size_t)(2 * S 
 
 // set_boundaries' corners (fluid.rs:254-271) on a diagonal-layout grid, from
 // the post-pass values of the frame (the rest of the pass is done).
-template <int MODE>
-__device__ __forceinline__ float dg_frame_after_pass(const float* x, const uint8_t* rowfl,
+template <int MODE, class ST>
+__device__ __forceinline__ float dg_frame_after_pass(const ST* x, const uint8_t* rowfl,
                                                      const uint8_t* colfl, int S, int P, int i,
                                                      int j) {
   if (MODE == kPassive) {
-    if (j == 0 && colfl[i]) return x[dg_at(i, 1, P)];
-    if (j == S - 1 && colfl[i]) return x[dg_at(i, S - 2, P)];
-    if (i == 0 && rowfl[j]) return x[dg_at(1, j, P)];
-    if (i == S - 1 && rowfl[j]) return x[dg_at(S - 2, j, P)];
+    if (j == 0 && colfl[i]) return hl(x, dg_at(i, 1, P));
+    if (j == S - 1 && colfl[i]) return hl(x, dg_at(i, S - 2, P));
+    if (i == 0 && rowfl[j]) return hl(x, dg_at(1, j, P));
+    if (i == S - 1 && rowfl[j]) return hl(x, dg_at(S - 2, j, P));
   }
-  return x[dg_at(i, j, P)];
+  return hl(x, dg_at(i, j, P));
 }
 
-template <int MODE>
-__device__ __forceinline__ void dg_corners(float* x, const uint8_t* rowfl, const uint8_t* colfl,
+template <int MODE, class ST>
+__device__ __forceinline__ void dg_corners(ST* x, const uint8_t* rowfl, const uint8_t* colfl,
                                            int S, int P) {
   auto f = [&](int i, int j) { return dg_frame_after_pass<MODE>(x, rowfl, colfl, S, P, i, j); };
   const float c00 = fmul(0.5f, fadd(f(1, 0), f(0, 1)));
   const float c0S = fmul(0.5f, fadd(f(1, S - 1), f(0, S - 2)));
   const float cS0 = fmul(0.5f, fadd(f(S - 2, 0), f(S - 1, 1)));
   const float cSS = fmul(0.5f, fadd(f(S - 2, S - 1), f(S - 1, S - 2)));
-  x[dg_at(0, 0, P)] = c00;
-  x[dg_at(0, S - 1, P)] = c0S;
-  x[dg_at(S - 1, 0, P)] = cS0;
-  x[dg_at(S - 1, S - 1, P)] = cSS;
+  hs(x, dg_at(0, 0, P), c00);
+  hs(x, dg_at(0, S - 1, P), c0S);
+  hs(x, dg_at(S - 1, 0, P), cS0);
+  hs(x, dg_at(S - 1, S - 1, P), cSS);
 }
 
 // Shared-memory accesses through 32-bit shared-window addresses (half the
@@ -97,10 +98,12 @@ __device__ __forceinline__ void sts_f32(uint32_t a, float v) {
   asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
 }
 
-// One scene grid as the block solver sees it (diagonal layout).
+// One scene grid as the block solver sees it (diagonal layout; fields in
+// storage format ST, arithmetic in FP32).
+template <class ST>
 struct WGrid {
-  float* x;
-  const float* x0;
+  ST* x;
+  const ST* x0;
   const uint8_t* code;   // boundary codes, diagonal layout
   const uint8_t* rowfl;  // [S]
   const uint8_t* colfl;  // [S]
@@ -138,10 +141,11 @@ struct WLaneState {
 // Per-task, per-lane constants. Grid rows of the diagonal layout are given as
 // a base with column i at base[i * P]; shared rows are 32-bit shared-window
 // byte addresses, column- or slot-indexed with stride 4 bytes.
+template <class ST>
 struct WTask {
-  float* gout;        // last sweep: x row j, global
-  float* gfix;        // last sweep: x row j-1 (AdjustColumn fix-up), global
-  const float* x0row;
+  ST* gout;        // last sweep: x row j, global
+  ST* gfix;           // last sweep: x row j-1 (AdjustColumn fix-up), global
+  const ST* x0row;
   const uint8_t* crow;
   uint32_t sr, sd;    // other sweeps: R / D source (ring lane, slot-indexed, or carry row)
   uint32_t sout;      // other sweeps: this lane's ring row (slot-indexed)
@@ -154,10 +158,10 @@ struct WTask {
 
 // x0 and codes of columns ib..ib+kWG-1 of this lane's row (EDGE: only the
 // ones inside the grid).
-template <bool EDGE>
-__device__ __forceinline__ void wave_prefetch(const WTask& T, int ib, int S, int P,
+template <bool EDGE, class ST>
+__device__ __forceinline__ void wave_prefetch(const WTask<ST>& T, int ib, int S, int P,
                                               float (&x)[kWG], uint32_t (&c)[kWG]) {
-  const float* px = T.x0row + (ptrdiff_t)ib * P;
+  const ST* px = T.x0row + (ptrdiff_t)ib * P;
   const uint8_t* pc = T.crow + (ptrdiff_t)ib * P;
 #pragma unroll
   for (int r = 0; r < kWG; ++r) {
@@ -166,14 +170,14 @@ __device__ __forceinline__ void wave_prefetch(const WTask& T, int ib, int S, int
       x[r] = 0.0f;
       c[r] = 0u;
     } else {
-      x[r] = __ldg(px + (ptrdiff_t)r * P);
+      x[r] = Store<ST>::ld(px + (ptrdiff_t)r * P);
       c[r] = __ldg(pc + (ptrdiff_t)r * P);
     }
   }
 }
 
-template <int MODE, bool EDGE, bool LAST>
-__device__ __forceinline__ void wave_chunk(const WTask& T, WLaneState& st, int lane, int tau0,
+template <int MODE, bool EDGE, bool LAST, class ST>
+__device__ __forceinline__ void wave_chunk(const WTask<ST>& T, WLaneState& st, int lane, int tau0,
                                            int half, int S, int P, float a, float cr,
                                            bool next_in_task, bool next_edge) {
   const unsigned FULL = 0xffffffffu;
@@ -182,7 +186,7 @@ __device__ __forceinline__ void wave_chunk(const WTask& T, WLaneState& st, int l
   // R / D / out streams at q = 0
   const uint32_t sR = T.sr + 4u * (uint32_t)(T.rring ? half : ib + 1);
   const uint32_t sD = T.sd + 4u * (uint32_t)(T.dring ? half : ib);
-  float* gO = LAST ? T.gout + (ptrdiff_t)(ib - 1) * P : nullptr;
+  ST* gO = LAST ? T.gout + (ptrdiff_t)(ib - 1) * P : nullptr;
   const uint32_t sO = T.sout + 4u * (uint32_t)half;
   float xa[kWG];
   uint32_t ca[kWG];
@@ -246,7 +250,7 @@ __device__ __forceinline__ void wave_chunk(const WTask& T, WLaneState& st, int l
       }
       const bool colok = EDGE ? (i - 1 >= 0 && i - 1 <= S - 1) : true;
       if (LAST) {
-        if (T.valid && colok) gO[(ptrdiff_t)q * P] = val;
+        if (T.valid && colok) hs(gO, (ptrdiff_t)q * P, val);
       } else {
         if (colok) sts_f32(sO + 4u * q, val);
         if (T.scarry && colok) {
@@ -267,7 +271,7 @@ __device__ __forceinline__ void wave_chunk(const WTask& T, WLaneState& st, int l
       if (MODE == kCol && lane == 0 && T.valid && (Cv[r] & kCodeAboveDown) &&
           (EDGE ? (i >= 1 && i <= N) : true)) {
         if (LAST)
-          T.gfix[(ptrdiff_t)i * P] = -g;
+          hs(T.gfix, (ptrdiff_t)i * P, -g);
         else
           sts_f32(T.sfix + 4u * (uint32_t)i, -g);
       }
@@ -281,8 +285,8 @@ __device__ __forceinline__ void wave_chunk(const WTask& T, WLaneState& st, int l
   }
 }
 
-template <int MODE, bool LAST>
-__device__ __forceinline__ void wave_chunk_any(const WTask& T, WLaneState& st, int lane, int c,
+template <int MODE, bool LAST, class ST>
+__device__ __forceinline__ void wave_chunk_any(const WTask<ST>& T, WLaneState& st, int lane, int c,
                                                int NCH, int half, int S, int P, float a,
                                                float cr) {
   const int N = S - 2;
@@ -291,19 +295,19 @@ __device__ __forceinline__ void wave_chunk_any(const WTask& T, WLaneState& st, i
   const bool next_in_task = c + 1 < NCH;
   const bool next_edge = !((tau0 + kWQ >= 32) && (tau0 + 2 * kWQ <= N));
   if (fast)
-    wave_chunk<MODE, false, LAST>(T, st, lane, tau0, half, S, P, a, cr, next_in_task,
-                                  next_edge);
+    wave_chunk<MODE, false, LAST, ST>(T, st, lane, tau0, half, S, P, a, cr, next_in_task,
+                                      next_edge);
   else
-    wave_chunk<MODE, true, LAST>(T, st, lane, tau0, half, S, P, a, cr, next_in_task,
-                                 next_edge);
+    wave_chunk<MODE, true, LAST, ST>(T, st, lane, tau0, half, S, P, a, cr, next_in_task,
+                                     next_edge);
 }
 
 // `K` sweeps of lin_solve on grid G by the whole block (blockDim.x = 32 *
 // (nwmax + 1): a loader warp and one warp per sweep of a pass), passes of at
 // most nwmax sweeps. Ends with a block barrier; the result (corners included)
 // is in G.x.
-template <int MODE>
-__device__ __noinline__ void wave_lin_solve(const WGrid G, const WBufs Bf, int K, int nwmax,
+template <int MODE, class ST>
+__device__ __noinline__ void wave_lin_solve(const WGrid<ST> G, const WBufs Bf, int K, int nwmax,
                                             float a, float cr) {
   if (K <= 0) return;
   extern __shared__ __align__(16) float wave_smem[];
@@ -331,11 +335,11 @@ __device__ __noinline__ void wave_lin_solve(const WGrid G, const WBufs Bf, int K
         const int j = 32 * t + lane;
         const bool rowok = j >= 0 && j <= S - 1;
         const int jc = rowok ? j : 0;
-        const float* base = G.x + (size_t)jc * P + jc;
+        const ST* base = G.x + (size_t)jc * P + jc;
 #pragma unroll
         for (int q = 0; q < kWQ; ++q) {
           const int is = c * kWQ + q - lane;
-          xs[q] = (rowok && is >= 0 && is <= S - 1) ? base[(ptrdiff_t)is * P] : 0.0f;
+          xs[q] = (rowok && is >= 0 && is <= S - 1) ? hl(base, (ptrdiff_t)is * P) : 0.0f;
         }
       };
       load_chunk(0);
@@ -373,7 +377,7 @@ __device__ __noinline__ void wave_lin_solve(const WGrid G, const WBufs Bf, int K
       WLaneState st;
       st.g1 = st.g2 = st.u1 = st.rm1 = st.h0 = st.h1 = 0.0f;
       st.c1 = 0u;
-      WTask T;
+      WTask<ST> T;
       for (int s = 0; s < nsup; ++s) {
         const int g = s - warp;
         if (sw < nw && g >= 0 && g < ntask) {
@@ -419,9 +423,9 @@ __device__ __noinline__ void wave_lin_solve(const WGrid G, const WBufs Bf, int K
           }
           const int half = (g & 1) * kWQ;
           if (last)
-            wave_chunk_any<MODE, true>(T, st, lane, c, NCH, half, S, P, a, cr);
+            wave_chunk_any<MODE, true, ST>(T, st, lane, c, NCH, half, S, P, a, cr);
           else
-            wave_chunk_any<MODE, false>(T, st, lane, c, NCH, half, S, P, a, cr);
+            wave_chunk_any<MODE, false, ST>(T, st, lane, c, NCH, half, S, P, a, cr);
           if (c == NCH - 1 && T.scarry) {
             sts_f32(T.scarry, st.h0);
             if (lane == 30) sts_f32(T.scarry + 4u, st.h1);
@@ -431,7 +435,7 @@ __device__ __noinline__ void wave_lin_solve(const WGrid G, const WBufs Bf, int K
       }
     }
   }
-  if (threadIdx.x == 0) dg_corners<MODE>(G.x, G.rowfl, G.colfl, S, P);
+  if (threadIdx.x == 0) dg_corners<MODE, ST>(G.x, G.rowfl, G.colfl, S, P);
   __syncthreads();
 }
 

@@ -222,6 +222,13 @@ typedef struct eq_batch eq_batch; /* opaque; owns device state */
 /* Creates `nscenes` scenes, each in the Fluid::new state (fluid.rs:93-110:
  * init() once, frame = DefaultWall). `device` < 0 = current device. */
 int eq_batch_new(int64_t nscenes, const eq_scene_desc* scenes, int device, eq_batch** out);
+/* The same with the fields STORED in FP16 or BF16 (storage EQ_STORE_F16 /
+ * EQ_STORE_BF16, defined with the precision form below; 0 = FP32): every
+ * phase computes exactly as the FP32 batch on the widened values and rounds
+ * once on store, so the per-scene results differ from the reference's only by
+ * those roundings (and their propagation). */
+int eq_batch_new_storage(int64_t nscenes, const eq_scene_desc* scenes, int storage, int device,
+                         eq_batch** out);
 int eq_batch_free(eq_batch* b); /* accepts NULL */
 int eq_batch_scene_count(const eq_batch* b, int64_t* n);
 /* Sum over scenes of (size-2)^2: the interior cells one frame advances. */
@@ -281,6 +288,51 @@ int eq_batch_autotune(eq_batch* b, int trial_frames, double* ms_out, int cap, in
 
 int eq_batch_get_stream(eq_batch* b, void** stream);
 int eq_batch_launch_count(const eq_batch* b, uint64_t* count);
+
+/* ---- the precision form: half-storage fluid ------------------------------ */
+
+/* One scene whose six fields are STORED in FP16 or BF16 (half the bytes of
+ * every field access) while every operation computes in FP32 on the widened
+ * values. The frame keeps the reference's phases, order and array aliasing
+ * (fluid.rs:437-524); the diffusion solves keep its lexicographic Gauss-Seidel
+ * (`frames` sweeps, FP32 arithmetic). The two pressure solves (fluid.rs:
+ * 353-362) are solved to a relative residual instead of a fixed sweep count:
+ * mixed-precision iterative refinement with an FP32 residual, FP64 norms and a
+ * multigrid correction stored in the half format. The solution's constant
+ * (the pure-Neumann null space) is the one the refinement reaches from p = 0.
+ * Results differ from the reference's by design; eq_hfluid_stats reports the
+ * refinement and the post-projection divergence of the last frame. */
+#define EQ_STORE_F16 1
+#define EQ_STORE_BF16 2
+
+typedef struct eq_hstats {
+  int32_t ir_iterations[2];  /* refinement rounds of the frame's two projects */
+  double rel_residual[2];    /* final mean-free relative residual of each */
+  double div_norm_before[2]; /* ||div v||_2 entering each project (FP64) */
+  double div_norm[2];        /* ||div v||_2 after each project (FP64) */
+} eq_hstats;
+
+typedef struct eq_hfluid eq_hfluid; /* opaque */
+
+/* Fluid::new (init() once, frame = DefaultWall) in half storage. Refinement
+ * stops at a relative residual <= pressure_rtol or after max_refinements
+ * rounds. */
+int eq_hfluid_new(const eq_fluid_configs* fluid, const eq_simulation_configs* sim, int storage,
+                  double pressure_rtol, int32_t max_refinements, int device, eq_hfluid** out);
+int eq_hfluid_free(eq_hfluid* h); /* accepts NULL */
+int eq_hfluid_fill_obstacle(eq_hfluid* h, int64_t x0, int64_t y0, int64_t x1, int64_t y1);
+/* Sources applied at the start of the next step (add_density / add_velocity
+ * order, fluid.rs:120-131). */
+int eq_hfluid_add_sources(eq_hfluid* h, int64_t n, const uint32_t* x, const uint32_t* y,
+                          const float* density, const float* vx, const float* vy);
+int eq_hfluid_step(eq_hfluid* h); /* synchronises (the refinement loop reads its norms) */
+int eq_hfluid_synchronize(eq_hfluid* h);
+/* Dense size*size FP32 copies of a stored field (widened / rounded). */
+int eq_hfluid_read_field(eq_hfluid* h, int field, float* host, uint64_t n);
+int eq_hfluid_write_field(eq_hfluid* h, int field, const float* host, uint64_t n);
+int eq_hfluid_stats(const eq_hfluid* h, eq_hstats* out);
+int eq_hfluid_get_stream(eq_hfluid* h, void** stream);
+int eq_hfluid_launch_count(const eq_hfluid* h, uint64_t* count);
 
 /* ---- lin_solve that allocates nothing ----------------------------------- */
 

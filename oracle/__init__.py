@@ -68,6 +68,11 @@ def lib():
             "eqo_step_f64": (None, [P, P, u32, f64, i64, f64, f64]),
             "eqo_run_f64": (None, [P, P, u32, f64, i64, f64, f64, i64, i64, P, P, P, P, P]),
             "eqo_new_f64": (None, [u32, P, P]),
+            "eqo_set_boundaries_f64": (None, [ci, P, u32, P]),
+            "eqo_diffuse_f64": (None, [ci, P, P, f64, u32, f64, i64, P]),
+            "eqo_advect_f64": (None, [ci, P, P, P, P, u32, f64, P]),
+            "eqo_project_div_f64": (None, [P, P, P, P, u32, P]),
+            "eqo_project_grad_f64": (None, [P, P, P, u32, P]),
             "eqo_fill_obstacle": (None, [P, u32, i64, i64, i64, i64]),
             "eqo_rectangle_valid": (ci, [i64, i64, i64, i64, i64]),
         }
@@ -171,3 +176,71 @@ def fill_obstacle(cells, size, x0, y0, x1, y1):
 
 def rectangle_valid(dl, ur, size) -> bool:
     return bool(lib().eqo_rectangle_valid(dl[0], dl[1], ur[0], ur[1], size))
+
+
+# ---- f64 reference step with a converged pressure solve --------------------
+# Used to measure the precision form (which solves project's pressure equation
+# to a relative residual instead of a fixed sweep count) against a reference
+# whose only difference is that solve. The pressure equation
+#   4 p - (sum of the 4 neighbours) = div,  frame neighbour = adjacent cell
+# (set_boundaries(Passive) where every interior row and column holds a fluid
+# cell) is the pure-Neumann 5-point Laplacian, which the orthonormal DCT-II
+# diagonalises exactly: eigenvalues 4 - 2 cos(pi k / N) - 2 cos(pi l / N). The
+# constant mode (zero eigenvalue) is set to zero: zero-mean pressure.
+
+
+def neumann_pressure_f64(div_interior: np.ndarray) -> np.ndarray:
+    from scipy.fft import dctn, idctn
+    n = div_interior.shape[0]
+    k = np.arange(n)
+    lam1 = 2.0 - 2.0 * np.cos(np.pi * k / n)
+    lam = lam1[:, None] + lam1[None, :]
+    bh = dctn(div_interior, type=2, norm="ortho")
+    lam[0, 0] = 1.0
+    ph = bh / lam
+    ph[0, 0] = 0.0
+    return idctn(ph, type=2, norm="ortho")
+
+
+def _all_rows_cols_fluid(cells: np.ndarray, size: int) -> bool:
+    m = cells.reshape(size, size)[1:-1, 1:-1] == 0
+    return bool(m.any(axis=1).all() and m.any(axis=0).all())
+
+
+def converged_step_f64(of: "OracleFluid"):
+    """One f64 frame of the reference (fluid.rs:437-524, same aliasing) with both
+    pressure solves replaced by the exact pure-Neumann solve."""
+    assert of.dtype == np.float64
+    S = of.size
+    if not _all_rows_cols_fluid(of.cells, S):
+        raise ValueError("a fully walled interior row or column makes the frame Dirichlet")
+    L = lib()
+    sc, de, vx, vy, vx0, vy0 = of.fields
+    c = _ptr(of.cells)
+
+    def project(u, v, p, div):
+        L.eqo_project_div_f64(_ptr(u), _ptr(v), _ptr(p), _ptr(div), S, c)
+        pin = neumann_pressure_f64(div.reshape(S, S)[1:-1, 1:-1].T.copy()).T
+        p.reshape(S, S)[1:-1, 1:-1] = pin
+        L.eqo_set_boundaries_f64(PASSIVE, _ptr(p), S, c)
+        L.eqo_project_grad_f64(_ptr(u), _ptr(v), _ptr(p), S, c)
+
+    dt, K = float(of.delta_t), int(of.frames)
+    L.eqo_diffuse_f64(ADJUST_ROW, _ptr(vx0), _ptr(vx), float(of.viscousity), S, dt, K, c)
+    L.eqo_diffuse_f64(ADJUST_COLUMN, _ptr(vy0), _ptr(vy), float(of.viscousity), S, dt, K, c)
+    project(vx0, vy0, vx, vy)
+    L.eqo_advect_f64(ADJUST_ROW, _ptr(vx), _ptr(vx0), _ptr(vx0), _ptr(vy0), S, dt, c)
+    L.eqo_advect_f64(ADJUST_COLUMN, _ptr(vy), _ptr(vy0), _ptr(vx0), _ptr(vy0), S, dt, c)
+    project(vx, vy, vx0, vy0)
+    L.eqo_diffuse_f64(PASSIVE, _ptr(sc), _ptr(de), float(of.diffusion), S, dt, K, c)
+    L.eqo_advect_f64(PASSIVE, _ptr(de), _ptr(sc), _ptr(vx), _ptr(vy), S, dt, c)
+    sc[:] = de
+
+
+def add_sources(of: "OracleFluid", xs, ys, d, u, v):
+    """add_density / add_velocity (fluid.rs:120-131) in array order, idx!-clamped."""
+    S = of.size
+    for x, y, dd, uu, vv in zip(xs, ys, d, u, v):
+        q = min(int(x), S - 1) + min(int(y), S - 1) * S
+        for f, a in ((1, dd), (0, dd), (2, uu), (3, vv)):
+            of.fields[f][q] = of.fields[f][q] + of.dtype.type(np.float32(a))

@@ -119,6 +119,26 @@ void eqo_run_f64(double* const f[6], const uint8_t* cells, uint32_t size, double
 void eqo_new_f64(uint32_t size, double* const f[6], uint8_t* cells) {
   fluid_init_arrays<double>(size, f, cells);
 }
+// The phases of the f64 step, for a step composed with another pressure solve.
+void eqo_set_boundaries_f64(int mode, double* x, uint32_t size, const uint8_t* cells) {
+  set_boundaries<double>((Mode)mode, x, size, cells);
+}
+void eqo_diffuse_f64(int mode, double* x, const double* x0, double diff, uint32_t size,
+                     double dt, int64_t iters, const uint8_t* cells) {
+  diffuse<double>((Mode)mode, x, x0, diff, size, dt, iters, cells);
+}
+void eqo_advect_f64(int mode, double* d, const double* d0, const double* u, const double* v,
+                    uint32_t size, double dt, const uint8_t* cells) {
+  advect<double>((Mode)mode, d, d0, u, v, size, dt, cells);
+}
+void eqo_project_div_f64(double* vx, double* vy, double* p, double* div, uint32_t size,
+                         const uint8_t* cells) {
+  project_divergence<double>(vx, vy, p, div, size, cells);
+}
+void eqo_project_grad_f64(double* vx, double* vy, const double* p, uint32_t size,
+                          const uint8_t* cells) {
+  project_gradient<double>(vx, vy, p, size, cells);
+}
 
 // ---- mask / obstacles -----------------------------------------------------
 void eqo_fill_obstacle(uint8_t* cells, uint32_t size, int64_t x0, int64_t y0, int64_t x1,

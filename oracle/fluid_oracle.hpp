@@ -132,10 +132,12 @@ inline void diffuse(Mode m, T* x, const T* x0, T diffusion, uint32_t size,
 }
 
 // project (fluid.rs:330-375). Note the divergence and gradient scale by
-// `size` (ghost frame included), not by size-2.
+// `size` (ghost frame included), not by size-2. Split in its divergence part
+// (fluid.rs:339-352), the pressure solve and its gradient part (fluid.rs:
+// 364-374) so that a step can be composed with another pressure solve.
 template <class T>
-inline void project(T* vx, T* vy, T* p, T* div, uint32_t size, int64_t frames,
-                    const uint8_t* cells) {
+inline void project_divergence(T* vx, T* vy, T* p, T* div, uint32_t size,
+                               const uint8_t* cells) {
   const int64_t S = size;
   const T sf = (T)size;
   for (int64_t j = 1; j < S - 1; ++j) {
@@ -148,6 +150,30 @@ inline void project(T* vx, T* vy, T* p, T* div, uint32_t size, int64_t frames,
   }
   set_boundaries<T>(Passive, div, size, cells);
   set_boundaries<T>(Passive, p, size, cells);
+}
+
+template <class T>
+inline void project_gradient(T* vx, T* vy, const T* p, uint32_t size, const uint8_t* cells) {
+  const int64_t S = size;
+  const T sf = (T)size;
+  for (int64_t j = 1; j < S - 1; ++j) {
+    for (int64_t i = 1; i < S - 1; ++i) {
+      vx[idx(i, j, S)] = vx[idx(i, j, S)] -
+                         ((T)0.5 * (p[idx(i + 1, j, S)] - p[idx(i - 1, j, S)])) * sf;
+      vy[idx(i, j, S)] = vy[idx(i, j, S)] -
+                         ((T)0.5 * (p[idx(i, j + 1, S)] - p[idx(i, j - 1, S)])) * sf;
+    }
+  }
+  set_boundaries<T>(AdjustRow, vx, size, cells);
+  set_boundaries<T>(AdjustColumn, vy, size, cells);
+}
+
+template <class T>
+inline void project(T* vx, T* vy, T* p, T* div, uint32_t size, int64_t frames,
+                    const uint8_t* cells) {
+  const int64_t S = size;
+  const T sf = (T)size;
+  project_divergence<T>(vx, vy, p, div, size, cells);
   lin_solve<T>(Passive, p, div, (T)1.0, (T)4.0, size, frames, cells);
   for (int64_t j = 1; j < S - 1; ++j) {
     for (int64_t i = 1; i < S - 1; ++i) {

@@ -192,3 +192,40 @@ def test_batch_rejects_bad_arguments(eqlib):
     with pytest.raises(_lib.EqError):
         b.lin_solve(PAS, 1, 1, 1.0, 4.0)
     b.close()
+
+
+# Per-scene tolerances on the density after 3 frames: the first two scenes
+# amplify any rounding quickly (the reference's own FP32 step drifts from its
+# FP64 step by a factor ~40 in 3 frames there, and rounding to FP16 once per
+# frame alone gives 6e-3 / 2e-3), the third is diffusion-dominated.
+HALF_TOL = {"f16": (0.1, 0.05, 2e-3), "bf16": (0.5, 0.3, 2e-2)}
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+def test_batch_half_storage_vs_f64(eqlib, storage):
+    """FP16 / BF16 storage, FP32 arithmetic, the reference's method: each
+    scene's density stays close to the f64 reference step (relative L2 over
+    the interior)."""
+    from equilibrium_gb300.precision import rel_l2
+    rng = np.random.default_rng(12)
+    cfgs = [SceneConfig(66, 0.1, 20, 1e-4, 1e-4), SceneConfig(130, 0.05, 20, 1e-5, 1e-5),
+            SceneConfig(41, 0.1, 7, 1e-3, 1e-3)]
+    rects = [[(20, 30, 30, 45)], random_rects(rng, 130, 3), []]
+    b = Batch(cfgs, storage=storage)
+    refs = []
+    for s, (c, rr) in enumerate(zip(cfgs, rects)):
+        r = oracle.OracleFluid(c.size, c.delta_t, c.frames, c.diffusion, c.viscousity,
+                               dtype=np.float64)
+        for rc in rr:
+            r.fill_obstacle(*rc)
+            b.fill_obstacle(s, *rc)
+        refs.append(r)
+    b.step(3)
+    for r in refs:
+        for _ in range(3):
+            r.step()
+    for s, r in enumerate(refs):
+        err = rel_l2(b.read_field(s, DE), r.fields[DE])
+        tol = HALF_TOL[storage][s]
+        assert np.isfinite(err) and err < tol, f"scene {s}: density rel L2 {err:.2e} >= {tol}"
+    b.close()

@@ -1,0 +1,102 @@
+"""The precision form (eq_hfluid_*): FP16 / BF16 storage, FP32 arithmetic,
+project's pressure by mixed-precision iterative refinement.
+
+Checked against two FP64 references built from the oracle: the reference step
+itself (20 Gauss-Seidel sweeps for the pressure) and the same step with both
+pressure solves converged exactly (oracle.converged_step_f64, a DCT solve of
+the pure-Neumann equation). The form changes the pressure method, so it is
+compared for accuracy with the second; the first is reported in the bench.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from equilibrium_gb300 import _lib
+from equilibrium_gb300.precision import HalfFluid, max_abs, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+S, DT, K, DIFF, VISC = 66, 0.1, 20, 1e-4, 1e-4
+RECT = (S // 3, S // 4, S // 3 + S // 8, S // 4 + S // 6)
+
+
+def rounded(a, storage):
+    import torch
+    t = torch.from_numpy(np.asarray(a, dtype=np.float32))
+    return t.to(torch.float16 if storage == "f16" else torch.bfloat16).float().numpy()
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+def test_init_and_field_roundtrip(eqlib, storage):
+    g = HalfFluid(S, DT, K, DIFF, VISC, storage)
+    r = oracle.OracleFluid(S, DT, K, DIFF, VISC)
+    for f in range(6):
+        np.testing.assert_array_equal(g.read_field(f), rounded(r.fields[f], storage))
+    vals = np.random.default_rng(0).uniform(-300, 300, S * S).astype(np.float32)
+    g.write_field(2, vals)
+    np.testing.assert_array_equal(g.read_field(2), rounded(vals, storage))
+    g.close()
+
+
+# Frame-1 accuracy against the converged FP64 step (measured: FP16 3.2e-3
+# density, 5.5e-3 velocity; BF16 0.12 / 0.05) with margin.
+TOL = {"f16": (1e-2, 2e-2), "bf16": (0.3, 0.15)}
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+def test_first_frame_vs_converged_f64(eqlib, storage):
+    rng = np.random.default_rng(1)
+    g = HalfFluid(S, DT, K, DIFF, VISC, storage)
+    conv = oracle.OracleFluid(S, DT, K, DIFF, VISC, dtype=np.float64)
+    g.fill_obstacle(*RECT)
+    conv.fill_obstacle(*RECT)
+    xs = rng.integers(S // 2 - 2, S // 2 + 3, 25)
+    ys = rng.integers(S // 2 - 2, S // 2 + 3, 25)
+    d = rng.uniform(0, 100, 25).astype(np.float32)
+    u = rng.uniform(-5, 5, 25).astype(np.float32)
+    v = rng.uniform(-5, 5, 25).astype(np.float32)
+    g.add_sources(xs, ys, d, u, v)
+    g.step()
+    oracle.add_sources(conv, xs, ys, d, u, v)
+    oracle.converged_step_f64(conv)
+    dens_tol, vel_tol = TOL[storage]
+    assert rel_l2(g.read_field(1), conv.fields[1]) < dens_tol
+    assert max(max_abs(g.read_field(2), conv.fields[2]),
+               max_abs(g.read_field(3), conv.fields[3])) < vel_tol
+    st = g.stats()
+    for w in range(2):
+        # refinement reached its FP32 floor or the tolerance, well below the start
+        assert st["rel_residual"][w] < 1e-4
+        assert 1 <= st["ir_iterations"][w] <= 30
+        assert np.isfinite(st["div_norm"][w])
+    g.close()
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+def test_projection_lowers_divergence(eqlib, storage):
+    g = HalfFluid(130, 0.05, 20, 1e-5, 1e-5, storage)
+    g.fill_obstacle(40, 30, 60, 70)
+    rng = np.random.default_rng(2)
+    for _ in range(3):
+        xs = rng.integers(60, 70, 8)
+        ys = rng.integers(60, 70, 8)
+        g.add_sources(xs, ys, rng.uniform(0, 50, 8), rng.normal(0, 3, 8), rng.normal(0, 3, 8))
+        g.step()
+        st = g.stats()
+        # The reference's project solves the compact 5-point equation and then
+        # subtracts a central-difference gradient, so even a converged pressure
+        # does not zero the central-difference divergence it measures (and the
+        # wall reflections add some back); it only lowers it.
+        assert np.isfinite(st["div_norm"][1])
+        assert st["div_norm"][1] < st["div_norm_before"][1]
+        assert st["rel_residual"][1] < 1e-4
+    g.close()
+
+
+def test_rejects_bad_arguments(eqlib):
+    with pytest.raises(_lib.EqError):
+        HalfFluid(19, DT, K, DIFF, VISC)
+    with pytest.raises(KeyError):
+        HalfFluid(S, DT, K, DIFF, VISC, "f8")
+    with pytest.raises(_lib.EqError):
+        HalfFluid(S, DT, K, DIFF, VISC, pressure_rtol=0.0)
