@@ -44,6 +44,7 @@ SIZE, DT, DIFF, VISC, ITERS, NSRC, SEED = 1026, 0.05, 1e-5, 1e-5, 20, 8, 2
 N = SIZE - 2
 BYTES_PER_CELL_LINSOLVE = 13  # read x0, read x, write x (f32) + mask byte, per S^2 cell
 BYTES_PER_CELL_FRAME = 164    # fused-phase compulsory traffic per S^2 cell per frame
+BYTES_PER_CELL_FRAME_HALF = 86  # the same with FP16 / BF16 fields: (164 - 8) / 2 + 8
 
 
 def baseline_metric():
@@ -106,7 +107,8 @@ def batch_workload(n=BATCH_SCENES, seed=BATCH_SEED, nmin=32, nmax=512):
     return cfgs, rects
 
 
-def run_batched_form(local_rank: int, frames: int, plain_sample: int = 12):
+def run_batched_form(local_rank: int, frames: int, plain_sample: int = 12, storage: str = "f32",
+                     autotune: bool = True, err_sample: int = 0):
     """The batched form on the many-scene workload: one persistent launch per
     frame (graph-replayed), autotuned; timed with CUDA events on the batch's
     stream (inputs ~4.6 GB, far larger than L2). Also the plain kernels looped
@@ -117,12 +119,12 @@ def run_batched_form(local_rank: int, frames: int, plain_sample: int = 12):
     from equilibrium_gb300.simulation import Fluid, FluidConfigs, SimulationConfigs
     L = _lib.load()
     cfgs, rects = batch_workload()
-    b = Batch([SceneConfig(*c) for c in cfgs], device=local_rank)
+    b = Batch([SceneConfig(*c) for c in cfgs], device=local_rank, storage=storage)
     for sidx, rr in enumerate(rects):
         for r in rr:
             b.fill_obstacle(sidx, *r)
     cells = b.cell_count()
-    tune_ms = b.autotune(trial_frames=1)
+    tune_ms = b.autotune(trial_frames=1) if autotune else None
     nw, bps = b.tuning()
     sp = ctypes.c_void_p()
     _lib.check(L.eq_batch_get_stream(b.handle, ctypes.byref(sp)))
@@ -141,51 +143,199 @@ def run_batched_form(local_rank: int, frames: int, plain_sample: int = 12):
     launches = b.launch_count() - c0
     ms = statistics.mean(a.elapsed_time(e) for a, e in ev)
     value = cells / (ms / 1e3)
-    # end to end: one frame through the C ABI, then every scene's three pub
-    # fields read back to host memory
-    t0 = time.perf_counter()
-    b.step(1)
-    d2h = 0
-    for sidx, c in enumerate(cfgs):
-        for f in (_lib.FIELD_DENSITY, _lib.FIELD_VX, _lib.FIELD_VY):
-            d2h += b.read_field(sidx, f).nbytes
-    e2e_s = time.perf_counter() - t0
+    out = {"value": cells / (ms / 1e3), "unit": "cell-steps/s", "ms_per_frame": ms,
+           "frames_timed": frames, "scenes": len(cfgs), "interior_cells": cells,
+           "dtype": "f32" if storage == "f32" else f"{storage} storage, f32 arithmetic",
+           "workload": f"{len(cfgs)} scenes, N log-uniform in [32, 512], dt U[0.02, 0.2], "
+                       "diffusion and viscosity log-uniform [1e-6, 1e-3], 20 sweeps, 0-8 "
+                       "seeded rectangles each, no sources (seed 3)",
+           "tuning": {"sweeps_per_pass": nw, "blocks_per_sm": bps,
+                      "autotune_ms_per_frame": tune_ms},
+           "gpu_launches": int(launches),
+           "roofline": {"bound": "hbm",
+                        "achieved": (BYTES_PER_CELL_FRAME if storage == "f32" else
+                                     BYTES_PER_CELL_FRAME_HALF) * cells / (ms / 1e3) / 1e9,
+                        "unit": "GB/s",
+                        "bytes_per_cell_frame": (BYTES_PER_CELL_FRAME if storage == "f32"
+                                                 else BYTES_PER_CELL_FRAME_HALF)}}
+    if storage == "f32":
+        # end to end: one frame through the C ABI, then every scene's three pub
+        # fields read back to host memory
+        t0 = time.perf_counter()
+        b.step(1)
+        d2h = 0
+        for sidx, c in enumerate(cfgs):
+            for f in (_lib.FIELD_DENSITY, _lib.FIELD_VX, _lib.FIELD_VY):
+                d2h += b.read_field(sidx, f).nbytes
+        e2e_s = time.perf_counter() - t0
+        out["e2e"] = {"value": cells / e2e_s, "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
+                      "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3}
+        out["bit_exact"] = "per scene, vs the reference step (tests/test_gpu_batch.py)"
     b.close()
-    # the plain (eq_fluid) kernels looped over a sample of the same scenes
-    rng = np.random.default_rng(7)
-    pick = rng.choice(len(cfgs), size=plain_sample, replace=False)
-    pcells, pms = 0, 0.0
-    for q in pick:
-        size, dt, k, dif, vis = cfgs[q]
-        g = Fluid(FluidConfigs(dif, vis, False), SimulationConfigs(dt, k, size), device=local_rank)
-        for r in rects[q]:
-            _lib.check(L.eq_fluid_fill_obstacle(g.handle, *r))
-        g.step()
-        g.synchronize()
-        t = time.perf_counter()
-        g.step()
-        g.step()
-        g.synchronize()
-        pms += (time.perf_counter() - t) / 2 * 1e3
-        pcells += (size - 2) ** 2
+    if err_sample:
+        out["density_rel_l2_vs_f64"] = batch_half_errors(storage, err_sample, local_rank)
+    if plain_sample:
+        # the plain (eq_fluid) kernels looped over a sample of the same scenes
+        rng = np.random.default_rng(7)
+        pick = rng.choice(len(cfgs), size=plain_sample, replace=False)
+        pcells, pms = 0, 0.0
+        for q in pick:
+            size, dt, k, dif, vis = cfgs[q]
+            g = Fluid(FluidConfigs(dif, vis, False), SimulationConfigs(dt, k, size),
+                      device=local_rank)
+            for r in rects[q]:
+                _lib.check(L.eq_fluid_fill_obstacle(g.handle, *r))
+            g.step()
+            g.synchronize()
+            t = time.perf_counter()
+            g.step()
+            g.step()
+            g.synchronize()
+            pms += (time.perf_counter() - t) / 2 * 1e3
+            pcells += (size - 2) ** 2
+            g.close()
+        out["plain_looped"] = {"value": pcells / (pms / 1e3), "unit": "cell-steps/s",
+                               "sample": f"{plain_sample} scenes of the workload stepped one by "
+                                         "one through eq_fluid (host clock, 2 frames each)"}
+    return out
+
+
+def batch_half_errors(storage: str, nsample: int, local_rank: int, frames=(1, 3)):
+    """Relative L2 density error of half-storage batch scenes against the f64
+    reference step (the oracle built with f64), for a seeded sample of the
+    workload's scenes: the median and maximum over the sample per frame."""
+    import oracle
+    from equilibrium_gb300.batch import Batch, SceneConfig
+    from equilibrium_gb300.precision import rel_l2
+    cfgs, rects = batch_workload()
+    rng = np.random.default_rng(11)
+    pick = [int(q) for q in rng.choice(len(cfgs), size=nsample, replace=False)
+            if cfgs[int(q)][0] <= 258][:nsample]
+    b = Batch([SceneConfig(*cfgs[q]) for q in pick], device=local_rank, storage=storage)
+    refs = []
+    for k, q in enumerate(pick):
+        size, dt, K, dif, vis = cfgs[q]
+        r = oracle.OracleFluid(size, dt, K, dif, vis, dtype=np.float64)
+        for rc in rects[q]:
+            r.fill_obstacle(*rc)
+            b.fill_obstacle(k, *rc)
+        refs.append(r)
+    res, done = {}, 0
+    for fr in frames:
+        b.step(fr - done)
+        for r in refs:
+            for _ in range(fr - done):
+                r.step()
+        done = fr
+        errs = [rel_l2(b.read_field(k, _lib_field_density()), r.fields[1])
+                for k, r in enumerate(refs)]
+        res[f"frame_{fr}"] = {"median": float(np.median(errs)), "max": float(np.max(errs))}
+    b.close()
+    res["scenes"] = f"{len(pick)} seeded scenes of the workload with size <= 258"
+    return res
+
+
+def _lib_field_density():
+    from equilibrium_gb300 import _lib
+    return _lib.FIELD_DENSITY
+
+
+# ---- the precision form's workload: one N = 2048 scene in half storage
+PREC_SIZE, PREC_DT, PREC_DIFF, PREC_VISC, PREC_RTOL = 2050, 0.05, 1e-5, 1e-5, 1e-5
+
+
+def precision_scene(size, seed=4, nframes=1):
+    """Obstacles and sources seeded as the N = 1024 plain workload, scaled to
+    `size` (4 rectangles of 2-8 % of the area, 8 source cells per frame)."""
+    n = size - 2
+    rng = np.random.default_rng(seed)
+    rects = []
+    while len(rects) < 4:
+        frac = rng.uniform(0.02, 0.08)
+        aspect = rng.uniform(0.5, 2.0)
+        w = int(round(math.sqrt(frac * n * n * aspect)))
+        h = int(round(frac * n * n / max(w, 1)))
+        if w < 2 or h < 2 or w > n - 2 or h > n - 2:
+            continue
+        x0 = int(rng.integers(1, size - 1 - w))
+        y0 = int(rng.integers(1, size - 1 - h))
+        rects.append((x0, y0, x0 + w, y0 + h))
+    cells = rng.integers(1, size - 1, size=(NSRC, 2))
+    u1 = rng.uniform(size=(nframes, NSRC, 2))
+    u2 = rng.uniform(size=(nframes, NSRC, 2))
+    gauss = np.sqrt(-2.0 * np.log(np.maximum(u1, 1e-12))) * np.cos(2 * np.pi * u2) * 3.0
+    dens = rng.uniform(0.0, 50.0, size=(nframes, NSRC))
+    return (rects, cells[:, 0].astype(np.uint32), cells[:, 1].astype(np.uint32),
+            dens.astype(np.float32), gauss[..., 0].astype(np.float32),
+            gauss[..., 1].astype(np.float32))
+
+
+def run_precision_form(local_rank: int, frames: int, size: int = PREC_SIZE,
+                       err_frames=(1,), storages=("f16", "bf16")):
+    """The precision form on one scene: throughput of `frames` timed frames per
+    storage format, its refinement statistics, and at `err_frames` the relative
+    L2 density error, max-abs velocity error and post-projection divergence
+    against two f64 references run on the host: the reference step itself and
+    the same step with both pressure solves converged exactly."""
+    import torch
+    import oracle
+    from equilibrium_gb300.precision import HalfFluid, max_abs, rel_l2
+    nmax = max(err_frames) if err_frames else 0
+    total = max(frames + 1, nmax)
+    rects, sx, sy, sd, su, sv = precision_scene(size, nframes=total)
+    refs = {}
+    if err_frames:
+        for kind in ("f64_reference", "f64_converged_pressure"):
+            r = oracle.OracleFluid(size, PREC_DT, ITERS, PREC_DIFF, PREC_VISC, dtype=np.float64)
+            for rc in rects:
+                r.fill_obstacle(*rc)
+            refs[kind] = (r, {})
+        for fr in range(nmax):
+            for kind, (r, snaps) in refs.items():
+                oracle.add_sources(r, sx, sy, sd[fr], su[fr], sv[fr])
+                if kind == "f64_reference":
+                    r.step()
+                else:
+                    oracle.converged_step_f64(r)
+                if fr + 1 in err_frames:
+                    snaps[fr + 1] = (r.fields[1].copy(), r.fields[2].copy(), r.fields[3].copy())
+    out = {"workload": f"one scene, N = {size - 2} interior, dt {PREC_DT}, diffusion = viscosity "
+                       f"= {PREC_DIFF}, 20 sweeps per diffusion solve, pressure refined to a "
+                       f"relative residual of {PREC_RTOL}, 4 seeded rectangles, {NSRC} seeded "
+                       "sources per frame"}
+    for storage in storages:
+        g = HalfFluid(size, PREC_DT, ITERS, PREC_DIFF, PREC_VISC, storage, PREC_RTOL, 30,
+                      device=local_rank)
+        for rc in rects:
+            g.fill_obstacle(*rc)
+        errs = {}
+        ms, launches = [], []
+        for fr in range(max(total, frames + 1)):
+            g.add_sources(sx, sy, sd[fr % total], su[fr % total], sv[fr % total])
+            torch.cuda.synchronize()
+            c0 = g.launch_count()
+            t0 = time.perf_counter()
+            g.step()
+            ms.append((time.perf_counter() - t0) * 1e3)
+            launches.append(g.launch_count() - c0)
+            if fr + 1 in err_frames:
+                de, vx, vy = g.read_field(1), g.read_field(2), g.read_field(3)
+                st = g.stats()
+                errs[f"frame_{fr + 1}"] = {
+                    kind: {"density_rel_l2": rel_l2(de, snaps[fr + 1][0]),
+                           "velocity_max_abs": max(max_abs(vx, snaps[fr + 1][1]),
+                                                   max_abs(vy, snaps[fr + 1][2]))}
+                    for kind, (_, snaps) in refs.items()}
+                errs[f"frame_{fr + 1}"]["post_projection_divergence_l2"] = st["div_norm"]
+        timed = ms[1:frames + 1]
+        t = statistics.mean(timed)
+        out[storage] = {"value": (size - 2) ** 2 / (t / 1e3), "unit": "cell-steps/s",
+                        "ms_per_frame": t, "frames_timed": len(timed),
+                        "clock": "host, per frame (the refinement loop reads its norms)",
+                        "stats_last_frame": g.stats(), "errors": errs,
+                        "gpu_launches_per_frame": statistics.mean(launches[1:frames + 1])}
         g.close()
-    plain_looped = pcells / (pms / 1e3)
-    return {"value": value, "unit": "cell-steps/s", "ms_per_frame": ms, "frames_timed": frames,
-            "scenes": len(cfgs), "interior_cells": cells, "dtype": "f32",
-            "workload": f"{len(cfgs)} scenes, N log-uniform in [32, 512], dt U[0.02, 0.2], "
-                        "diffusion and viscosity log-uniform [1e-6, 1e-3], 20 sweeps, 0-8 "
-                        "seeded rectangles each, no sources (seed 3)",
-            "tuning": {"sweeps_per_pass": nw, "blocks_per_sm": bps,
-                       "autotune_ms_per_frame": tune_ms},
-            "gpu_launches": int(launches),
-            "roofline": {"bound": "hbm", "achieved": BYTES_PER_CELL_FRAME * cells / (ms / 1e3) / 1e9,
-                         "unit": "GB/s", "bytes_per_cell_frame": BYTES_PER_CELL_FRAME},
-            "e2e": {"value": cells / e2e_s, "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
-            "plain_looped": {"value": plain_looped, "unit": "cell-steps/s",
-                             "sample": f"{plain_sample} scenes of the workload stepped one by "
-                                       "one through eq_fluid (host clock, 2 frames each)"},
-            "bit_exact": "per scene, vs the reference step (tests/test_gpu_batch.py)"}
+    return out
 
 
 def replicas_value(local_seconds: float, steps: int, world: int, reduce_max=None):
@@ -459,14 +609,25 @@ def run_ours(args):
                "sample": f"failed: {e}"}
     forms = {}
     if args.forms:
-        try:
-            bf = run_batched_form(local_rank, args.batch_frames)
-            bf["roofline"]["peak"] = hbm
-            bf["roofline"]["frac"] = bf["roofline"]["achieved"] / hbm
-            bf["vs_plain"] = bf["value"] / value
-        except Exception as e:  # reported, never silently replaced
-            bf = {"error": f"{type(e).__name__}: {e}"}
-        forms["batched"] = bf
+        def form(name, fn):
+            try:
+                r = fn()
+                if "roofline" in r:
+                    r["roofline"]["peak"] = hbm
+                    r["roofline"]["frac"] = r["roofline"]["achieved"] / hbm
+                if "value" in r:
+                    r["vs_plain"] = r["value"] / value
+            except Exception as e:  # reported, never silently replaced
+                r = {"error": f"{type(e).__name__}: {e}"}
+            forms[name] = r
+
+        form("batched", lambda: run_batched_form(local_rank, args.batch_frames))
+        form("batched_f16", lambda: run_batched_form(local_rank, args.batch_frames, 0, "f16",
+                                                     autotune=False, err_sample=24))
+        form("precision", lambda: run_precision_form(local_rank, args.precision_frames))
+        for k in ("f16", "bf16"):
+            if "precision" in forms and k in forms["precision"]:
+                forms["precision"][k]["vs_plain"] = forms["precision"][k]["value"] / value
     line = {"metric": baseline_metric(), "value": value, "unit": "cell-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -491,12 +652,23 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-frames", type=int, default=12)
     ap.add_argument("--batch-frames", type=int, default=5)
+    ap.add_argument("--precision-frames", type=int, default=4)
+    ap.add_argument("--precision-study", action="store_true",
+                    help="only the precision form's error study: N=512, errors at frames 1, "
+                         "50 and 200 against both f64 references")
     ap.add_argument("--no-forms", dest="forms", action="store_false",
                     help="skip the batched / half-storage forms")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.precision_study:
+        import torch
+        from equilibrium_gb300 import build as eqbuild
+        eqbuild.build()
+        torch.cuda.set_device(0)
+        print(json.dumps({"precision_study": run_precision_form(
+            0, 3, size=514, err_frames=(1, 50, 200))}), flush=True)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
