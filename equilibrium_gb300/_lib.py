@@ -43,6 +43,11 @@ class HStatsC(ctypes.Structure):
                 ("div_norm_before", ctypes.c_double * 2), ("div_norm", ctypes.c_double * 2)]
 
 
+class RenderColorsC(ctypes.Structure):
+    _fields_ = [("fluid", ctypes.c_uint8 * 4), ("world", ctypes.c_uint8 * 4),
+                ("obstacles", ctypes.c_uint8 * 4)]
+
+
 class FluidConfigsC(ctypes.Structure):
     _fields_ = [("diffusion", ctypes.c_float), ("viscousity", ctypes.c_float),
                 ("has_perlin_noise", ctypes.c_int32)]
@@ -113,6 +118,12 @@ def load(path: str = LIB_PATH):
         "eq_fluid_set_profiling": (i32, [H, i32]),
         "eq_fluid_kernel_stats": (i32, [H, i32, ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_uint64)]),
+        "eq_fluid_render_rgba": (i32, [H, ctypes.POINTER(RenderColorsC), P, u64]),
+        "eq_fluid_render_rgba_device": (i32, [H, ctypes.POINTER(RenderColorsC), P]),
+        "eq_fluid_add_noise": (i32, [H, u64]),
+        "eq_noise_angle": (ctypes.c_double, [f32]),
+        "eq_fluid_fill_obstacle_device": (i32, [H, i64, i64, i64, i64]),
+        "eq_fluid_step_graph": (i32, [H, i64, i32, u64]),
         "eq_batch_new": (i32, [i64, ctypes.POINTER(SceneDescC), i32, PP]),
         "eq_batch_new_storage": (i32, [i64, ctypes.POINTER(SceneDescC), i32, i32, PP]),
         "eq_batch_free": (i32, [H]),

@@ -81,6 +81,18 @@ struct eq_fluid {
   bool profiling = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ls_events;
 
+  // around the step: noise counter, rendered image, captured frame loop
+  unsigned long long* noise_counter = nullptr;
+  void* rgba = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int64_t gframes = -1, gK = -1;
+  bool gnoise = false;
+  uint64_t gseed = 0;
+  float gdt = 0.f, gdiff = 0.f, gvisc = 0.f;
+  uint64_t glaunches = 0;
+  bool graph_mode = false;  // lin_solve clears its tagged buffers (graph replay)
+
   size_t grid_elems() const { return (size_t)P * S; }
 };
 
@@ -195,6 +207,13 @@ int launch_lin_solve(eq_fluid* h, int mode, float* x, const float* x0, float a, 
   const int S = (int)h->S;
   for (int64_t done = 0; done < K; done += kMaxSweepsPerLaunch) {
     const int Kc = (int)std::min<int64_t>(kMaxSweepsPerLaunch, K - done);
+    if (h->graph_mode) {
+      // A captured frame replays with the same tags: clear what a previous
+      // replay left so that no stale word carries a current tag.
+      EQ_CUDA(cudaMemsetAsync(h->wt, 0, 2 * h->grid_elems() * 8, h->stream));
+      EQ_CUDA(cudaMemsetAsync(h->edge, 0, (size_t)h->B * kMaxSweepsPerLaunch * h->P * 8,
+                              h->stream));
+    }
     if (h->tag > 0xF0000000u) {  // tags would wrap: restart from clean buffers
       EQ_CUDA(cudaMemsetAsync(h->wt, 0, 2 * h->grid_elems() * 8, h->stream));
       EQ_CUDA(cudaMemsetAsync(h->edge, 0, (size_t)h->B * kMaxSweepsPerLaunch * h->P * 8,
@@ -348,6 +367,10 @@ void free_handle(eq_fluid* h) {
     cudaEventDestroy(e.first);
     cudaEventDestroy(e.second);
   }
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  cudaFree(h->noise_counter);
+  cudaFree(h->rgba);
   cudaFree(h->block);
   cudaFree(h->cells);
   cudaFree(h->code);
@@ -882,3 +905,6 @@ int eq_fluid_set_spin_limit(eq_fluid* h, int64_t iterations) {
 
 // The precision form (half storage, refined pressure).
 #include "half.cu"
+
+// Around the step: image, noise, device obstacles, graph-captured frames.
+#include "frame.cu"

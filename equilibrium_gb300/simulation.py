@@ -189,31 +189,42 @@ class Fluid:
         ptr = [None if a is None else a.ctypes.data for a in arrs]
         check(self._L.eq_fluid_add_sources(self._h, n, xs.ctypes.data, ys.ctypes.data, *ptr))
 
-    def add_noise(self, rng: Optional[random.Random] = None):
-        """fluid.rs:575-599: a velocity impulse at the centre whose direction is
-        the segment centre->(random cell) rotated by an angle from gradient
-        noise at (dt, dt). The reference's angle comes from the `noise` crate's
-        Perlin and its cell from `thread_rng`; this mirror uses its own
-        seeded gradient noise and RNG, so it matches in distribution only."""
-        rng = rng or random.Random()
-        size = self.simulation_configs.size
-        dt = float(self.simulation_configs.delta_t)
-        angle = _gradient_noise_2d(dt, dt) * 6.28 * 2.0
-        rx, ry = rng.randrange(size), rng.randrange(size)
-        cx = cy = float(size // 2)
-        # rotate (rx, ry) around (cx, cy) by `angle` degrees (geo's rotate_around_point)
-        rad = math.radians(angle)
-        ox, oy = rx - cx, ry - cy
-        px = cx + ox * math.cos(rad) - oy * math.sin(rad)
-        py = cy + ox * math.sin(rad) + oy * math.cos(rad)
-        self.add_velocity(int(cx), int(cy), float(np.float32(px)) * 2.0,
-                          float(np.float32(py)) * 2.0)
+    def add_noise(self, seed: Optional[int] = None):
+        """fluid.rs:575-599 on the device: a velocity impulse at the centre whose
+        value is twice a uniformly drawn cell rotated about the centre by the
+        gradient-noise angle at (dt, dt) (eq_noise_angle). The reference's angle
+        comes from the `noise` crate's Perlin and its cell from `thread_rng`,
+        so this matches it in distribution only. `seed` None draws one."""
+        if seed is None:
+            seed = random.getrandbits(64)
+        check(self._L.eq_fluid_add_noise(self._h, int(seed) & (2**64 - 1)))
+
+    def step_graph(self, nframes: int, with_noise: bool = False, seed: int = 0):
+        """`nframes` frames (optional device noise, then step) replayed from one
+        captured CUDA graph: the frame loop without a host sync per frame."""
+        check(self._L.eq_fluid_step_graph(self._h, int(nframes), int(bool(with_noise)),
+                                          int(seed) & (2**64 - 1)))
+
+    def render_rgba(self, colors=None) -> np.ndarray:
+        """render_image's pixels (renderer_helpers.rs:115-180) as (size, size, 4) RGBA8,
+        row y, column x. `colors` = (fluid, world, obstacles) RGBA tuples or None."""
+        n = int(self.simulation_configs.size)
+        out = np.empty((n, n, 4), dtype=np.uint8)
+        c = None
+        if colors is not None:
+            c = _lib.RenderColorsC((ctypes.c_uint8 * 4)(*colors[0]), (ctypes.c_uint8 * 4)(*colors[1]),
+                                   (ctypes.c_uint8 * 4)(*colors[2]))
+        check(self._L.eq_fluid_render_rgba(self._h, ctypes.byref(c) if c is not None else None,
+                                           out.ctypes.data, out.nbytes))
+        return out
 
     # -- obstacles ------------------------------------------------------------
     def fill_obstacle(self, obstacle: Rectangle):
-        """fluid.rs:610-619."""
+        """fluid.rs:610-619, rasterised on the device (mask and boundary codes
+        updated in place)."""
         p = obstacle.get_approximate_points()
-        check(self._L.eq_fluid_fill_obstacle(self._h, p[0][0], p[0][1], p[1][0], p[1][1]))
+        check(self._L.eq_fluid_fill_obstacle_device(self._h, p[0][0], p[0][1], p[1][0],
+                                                    p[1][1]))
 
     # -- the pub fields -----------------------------------------------------------
     def _n(self) -> int:
@@ -331,3 +342,22 @@ class CurrentSimulation:
                 self.fluid.add_noise()
             self.fluid.step()
             tx(FluidStep(self.fluid.clone(), i))
+
+
+def write_png(path: str, rgba: np.ndarray):
+    """A frame image (H, W, 4) RGBA8 as a PNG file (stdlib zlib; the reference
+    saves JPEGs through the `image` crate, renderer_helpers.rs:166-179)."""
+    import struct
+    import zlib
+    h, w = rgba.shape[:2]
+    raw = b"".join(b"\x00" + rgba[y].tobytes() for y in range(h))
+
+    def chunk(tag, data):
+        return (struct.pack(">I", len(data)) + tag + data +
+                struct.pack(">I", zlib.crc32(tag + data) & 0xffffffff))
+
+    with open(path, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n")
+        f.write(chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)))
+        f.write(chunk(b"IDAT", zlib.compress(raw, 6)))
+        f.write(chunk(b"IEND", b""))

@@ -179,6 +179,49 @@ int eq_fluid_write_field_async(eq_fluid* h, int field, const float* host, uint64
 int eq_fluid_read_cells(eq_fluid* h, uint8_t* host, uint64_t n);
 int eq_fluid_write_cells(eq_fluid* h, const uint8_t* host, uint64_t n);
 
+/* ---- around the step --------------------------------------------------- */
+
+/* RGBA colours of render_image (renderer_helpers.rs:115-180): FluidConfigs'
+ * fluid_color and world_color (configs.rs:37-60) and the listener's
+ * obstacles_color. NULL selects the defaults (208,88,157,220), (94,146,162,128)
+ * and red (255,0,0,255). */
+typedef struct eq_render_colors {
+  uint8_t fluid[4];
+  uint8_t world[4];
+  uint8_t obstacles[4];
+} eq_render_colors;
+
+/* The frame's image, size x size RGBA8 pixels (x fastest, pixel (x, y) =
+ * cell idx(x, y)), by render_image's rule: a wall in the obstacles colour, a
+ * fluid cell with density != 0 as ((density*fluid.r) as u8, fluid.g,
+ * density as u8, 1) with Rust's saturating casts, any other cell in the world
+ * colour. The host form synchronises; the device form writes a caller's
+ * device buffer on the handle's stream (a headless frame buffer). */
+int eq_fluid_render_rgba(eq_fluid* h, const eq_render_colors* colors, uint8_t* host_rgba,
+                         uint64_t nbytes);
+int eq_fluid_render_rgba_device(eq_fluid* h, const eq_render_colors* colors, void* d_rgba);
+
+/* add_noise (fluid.rs:575-599) on the device: a velocity impulse at the
+ * centre cell equal to twice the point (rx, ry) rotated about the centre by
+ * eq_noise_angle(delta_t) degrees, (rx, ry) uniform over the grid from a
+ * counter-based generator seeded by `seed` (the handle's noise counter
+ * advances each call). The reference draws (rx, ry) from thread_rng and the
+ * angle from the `noise` crate's Perlin, so results match it in distribution
+ * only. */
+int eq_fluid_add_noise(eq_fluid* h, uint64_t seed);
+double eq_noise_angle(float delta_t); /* gradient noise at (dt, dt) * 6.28 * 2 */
+
+/* fill_obstacle (fluid.rs:610-619) rasterised on the device: the device mask
+ * and the boundary codes are updated in place (no host upload); the host copy
+ * of cells_type is kept current. */
+int eq_fluid_fill_obstacle_device(eq_fluid* h, int64_t x0, int64_t y0, int64_t x1, int64_t y1);
+
+/* The frame loop of CurrentSimulation::simulate (renderer_helpers.rs:52-72)
+ * without a host synchronisation per frame: `nframes` frames of (optional
+ * device add_noise, then step) captured once into a CUDA graph (kept for the
+ * next call with the same arguments and configs) and replayed. Asynchronous. */
+int eq_fluid_step_graph(eq_fluid* h, int64_t nframes, int32_t with_noise, uint64_t seed);
+
 /* ---- single phases (the reference's private functions), on fields ------- */
 
 /* set_boundaries (fluid.rs:252-272) on one field. */

@@ -244,3 +244,26 @@ def add_sources(of: "OracleFluid", xs, ys, d, u, v):
         q = min(int(x), S - 1) + min(int(y), S - 1) * S
         for f, a in ((1, dd), (0, dd), (2, uu), (3, vv)):
             of.fields[f][q] = of.fields[f][q] + of.dtype.type(np.float32(a))
+
+
+def render_rgba(density: np.ndarray, cells: np.ndarray, size: int,
+                fluid=(208, 88, 157, 220), world=(94, 146, 162, 128),
+                obstacles=(255, 0, 0, 255)) -> np.ndarray:
+    """render_image's per-pixel rule (renderer_helpers.rs:147-164) in numpy:
+    wall -> obstacles colour; density != 0 on a fluid cell ->
+    ((density * fluid.r) as u8, fluid.g, density as u8, 1) with Rust's
+    saturating float-to-u8 casts; otherwise the world colour."""
+    def as_u8(v):
+        v = np.where(np.isnan(v), 0.0, v)
+        return np.clip(np.trunc(v), 0, 255).astype(np.uint8)
+    d = np.asarray(density, dtype=np.float32).reshape(size, size)
+    w = np.asarray(cells).reshape(size, size) != 0
+    out = np.empty((size, size, 4), dtype=np.uint8)
+    out[:] = np.array(world, dtype=np.uint8)
+    fl = (~w) & (d != 0.0)
+    out[fl, 0] = as_u8(d[fl] * np.float32(fluid[0]))
+    out[fl, 1] = fluid[1]
+    out[fl, 2] = as_u8(d[fl])
+    out[fl, 3] = 1
+    out[w] = np.array(obstacles, dtype=np.uint8)
+    return out

@@ -146,3 +146,25 @@ def test_f64_oracle_tracks_f32():
         f.step()
     d32, d64 = a.field("density").astype(np.float64), b.field("density")
     assert np.linalg.norm(d32 - d64) / np.linalg.norm(d64) < 1e-5
+
+
+def test_render_rule_restatement():
+    """render_image's rule on a 3x3 grid: wall, zero density, saturating casts."""
+    d = np.array([0.0, 1.5, 300.0, -2.0, np.nan, 0.5, 2.0, 0.0, 1.0], dtype=np.float32)
+    cells = np.array([1, 0, 0, 0, 0, 0, 0, 0, 1], dtype=np.uint8)
+    img = oracle.render_rgba(d, cells, 3)
+    assert tuple(img[0, 0]) == (255, 0, 0, 255) and tuple(img[2, 2]) == (255, 0, 0, 255)
+    assert tuple(img[0, 1]) == (255, 88, 1, 1)            # 1.5 * 208 saturates
+    assert tuple(img[1, 2]) == (104, 88, 0, 1)            # 0.5 * 208 truncates
+    assert tuple(img[0, 2]) == (255, 88, 255, 1)
+    assert tuple(img[1, 0]) == (0, 88, 0, 1)          # negative saturates to 0
+    assert tuple(img[1, 1]) == (0, 88, 0, 1)          # NaN != 0, casts to 0
+    assert tuple(img[2, 1]) == (94, 146, 162, 128)    # zero density: world colour
+
+
+def test_noise_angle_is_deterministic_and_bounded():
+    from equilibrium_gb300 import _lib
+    L = _lib.load()
+    a = [L.eq_noise_angle(np.float32(dt)) for dt in (0.02, 0.05, 0.1, 0.02)]
+    assert a[0] == a[3]
+    assert all(abs(x) <= 6.28 * 2 * 1.5 for x in a)
