@@ -338,6 +338,41 @@ def run_precision_form(local_rank: int, frames: int, size: int = PREC_SIZE,
     return out
 
 
+def run_case(case: str):
+    """Small, self-contained runs of one form, for kernel profiles."""
+    import torch
+    from equilibrium_gb300 import build as eqbuild
+    eqbuild.build()
+    torch.cuda.set_device(0)
+    if case.startswith("batch256"):
+        from equilibrium_gb300.batch import Batch, SceneConfig
+        cfgs, rects = batch_workload(n=256)
+        b = Batch([SceneConfig(*c) for c in cfgs], storage="f16" if case.endswith("f16") else "f32")
+        for sidx, rr in enumerate(rects):
+            for r in rr:
+                b.fill_obstacle(sidx, *r)
+        b.step(1, graph=False)
+        b.synchronize()
+        t = time.perf_counter()
+        b.step(1, graph=False)
+        b.synchronize()
+        print(json.dumps({"case": case, "ms": (time.perf_counter() - t) * 1e3,
+                          "cells": b.cell_count()}))
+        b.close()
+    else:
+        from equilibrium_gb300.precision import HalfFluid
+        size = 1026
+        rects, sx, sy, sd, su, sv = precision_scene(size, nframes=2)
+        g = HalfFluid(size, PREC_DT, ITERS, PREC_DIFF, PREC_VISC, "f16", PREC_RTOL, 30)
+        for r in rects:
+            g.fill_obstacle(*r)
+        for fr in range(2):
+            g.add_sources(sx, sy, sd[fr], su[fr], sv[fr])
+            g.step()
+        print(json.dumps({"case": case, "stats": g.stats()}))
+        g.close()
+
+
 def replicas_value(local_seconds: float, steps: int, world: int, reduce_max=None):
     """Whole-job cell-steps/s of `world` independent replicas: every rank ran
     `steps` frames; the job time is the slowest rank's (max over ranks)."""
@@ -653,6 +688,11 @@ def main():
     ap.add_argument("--cpu-frames", type=int, default=12)
     ap.add_argument("--batch-frames", type=int, default=5)
     ap.add_argument("--precision-frames", type=int, default=4)
+    ap.add_argument("--case", default=None,
+                    choices=["batch256", "batch256_f16", "precision1024"],
+                    help="one small run for profiling: 'batch256' = one frame of 256 scenes of "
+                         "the batched workload (after one warm-up frame), 'precision1024' = two "
+                         "frames of the precision form at N = 1024 (FP16)")
     ap.add_argument("--precision-study", action="store_true",
                     help="only the precision form's error study: N=512, errors at frames 1, "
                          "50 and 200 against both f64 references")
@@ -661,7 +701,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.precision_study:
+    if args.case:
+        run_case(args.case)
+    elif args.precision_study:
         import torch
         from equilibrium_gb300 import build as eqbuild
         eqbuild.build()
