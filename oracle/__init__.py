@@ -21,7 +21,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libeqoracle.so")
-SOURCES = [os.path.join(HERE, "fluid_oracle.cpp"), os.path.join(HERE, "fluid_oracle.hpp")]
+SOURCES = [os.path.join(HERE, "fluid_oracle.cpp"), os.path.join(HERE, "fluid_oracle.hpp"),
+           os.path.join(HERE, "adjoint.hpp")]
 
 # Modes (fluid.rs:21-29) and field order (fluid.rs:59-77).
 ADJUST_ROW, ADJUST_COLUMN, PASSIVE = 0, 1, 2
@@ -73,6 +74,10 @@ def lib():
             "eqo_advect_f64": (None, [ci, P, P, P, P, u32, f64, P]),
             "eqo_project_div_f64": (None, [P, P, P, P, u32, P]),
             "eqo_project_grad_f64": (None, [P, P, P, u32, P]),
+            "eqo_adjoint_problem_f64": (f64, [P, u32, f64, i64, f64, f64, i64, P, P, P, P, P,
+                                              P, P]),
+            "eqo_lin_solve_adj_f64": (None, [ci, P, P, f64, f64, u32, i64, P]),
+            "eqo_set_boundaries_adj_f64": (None, [ci, P, u32, P]),
             "eqo_fill_obstacle": (None, [P, u32, i64, i64, i64, i64]),
             "eqo_rectangle_valid": (ci, [i64, i64, i64, i64, i64]),
         }
@@ -267,3 +272,43 @@ def render_rgba(density: np.ndarray, cells: np.ndarray, size: int,
     out[fl, 3] = 1
     out[w] = np.array(obstacles, dtype=np.uint8)
     return out
+
+
+# ---- the differentiable problem (f64 tape adjoint) ---------------------------
+
+
+def adjoint_problem_f64(cells, size, dt, iters, diff, visc, init, src, target, grads=True):
+    """Loss 0.5*sum_interior(density - target)^2 after len(src) frames of
+    (density/scratch += src[f]; step) from `init` (six arrays); returns
+    (loss, signature, g_vx, g_vy, g_src) with the adjoints of the initial vx,
+    vy and of every source field (None when grads=False)."""
+    n = size * size
+    init = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) for a in init]
+    src = np.ascontiguousarray(src, dtype=np.float64).reshape(-1, n)
+    target = np.ascontiguousarray(target, dtype=np.float64).reshape(-1)
+    ptrs = (ctypes.c_void_p * 6)(*[_ptr(a) for a in init])
+    sig = ctypes.c_uint64()
+    if grads:
+        gvx, gvy = np.zeros(n), np.zeros(n)
+        gsrc = np.zeros_like(src)
+        loss = lib().eqo_adjoint_problem_f64(_ptr(cells), size, dt, iters, diff, visc,
+                                             src.shape[0], ptrs, _ptr(src), _ptr(target),
+                                             _ptr(gvx), _ptr(gvy), _ptr(gsrc), ctypes.byref(sig))
+        return loss, sig.value, gvx, gvy, gsrc
+    loss = lib().eqo_adjoint_problem_f64(_ptr(cells), size, dt, iters, diff, visc,
+                                         src.shape[0], ptrs, _ptr(src), _ptr(target), None, None,
+                                         None, ctypes.byref(sig))
+    return loss, sig.value, None, None, None
+
+
+def gaussian_target(size, nblobs=6, sigma=(8.0, 24.0), seed=0, amplitude=1.0):
+    """A seeded target density: the sum of `nblobs` Gaussians with sigma
+    uniform in `sigma` (cells), centres uniform over the interior."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:size, 0:size].astype(np.float64)
+    t = np.zeros((size, size))
+    for _ in range(nblobs):
+        cx, cy = rng.uniform(1, size - 1, 2)
+        sg = rng.uniform(*sigma)
+        t += amplitude * np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2 * sg * sg))
+    return t.reshape(-1)

@@ -5,6 +5,7 @@
 // Field order everywhere: scratch, density, vx, vy, vx0, vy0 (fluid.rs:59-77).
 // Mask: one byte per cell, 1 = DefaultWall, 0 = NoWall (fluid.rs:12-17).
 #include "fluid_oracle.hpp"
+#include "adjoint.hpp"
 
 #include <chrono>
 
@@ -138,6 +139,23 @@ void eqo_project_div_f64(double* vx, double* vy, double* p, double* div, uint32_
 void eqo_project_grad_f64(double* vx, double* vy, const double* p, uint32_t size,
                           const uint8_t* cells) {
   project_gradient<double>(vx, vy, p, size, cells);
+}
+
+// ---- adjoint (the f64 tape adjoint the GPU adjoint is checked against) ----
+double eqo_adjoint_problem_f64(const uint8_t* cells, uint32_t size, double dt, int64_t iters,
+                               double diff, double visc, int64_t nframes,
+                               const double* const init[6], const double* src,
+                               const double* target, double* g_vx, double* g_vy, double* g_src,
+                               uint64_t* sig) {
+  return adjoint_problem<double>(cells, size, dt, iters, diff, visc, nframes, init, src, target,
+                                 g_vx, g_vy, g_src, sig);
+}
+void eqo_lin_solve_adj_f64(int mode, double* xb, double* x0b, double a, double c,
+                           uint32_t size, int64_t iters, const uint8_t* cells) {
+  lin_solve_adj<double>((Mode)mode, xb, x0b, a, c, size, iters, cells);
+}
+void eqo_set_boundaries_adj_f64(int mode, double* xb, uint32_t size, const uint8_t* cells) {
+  set_boundaries_adj<double>((Mode)mode, xb, size, cells);
 }
 
 // ---- mask / obstacles -----------------------------------------------------
