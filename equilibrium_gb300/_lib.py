@@ -161,6 +161,20 @@ def load(path: str = LIB_PATH):
         "eq_hfluid_get_stream": (i32, [H, PP]),
         "eq_hfluid_launch_count": (i32, [H, ctypes.POINTER(ctypes.c_uint64)]),
         "eq_batch_launch_count": (i32, [H, ctypes.POINTER(ctypes.c_uint64)]),
+        "eq_grad_new": (i32, [H, i64, i64, PP]),
+        "eq_grad_free": (i32, [H]),
+        "eq_grad_forward": (i32, [H, i64, P, u64]),
+        "eq_grad_forward_device": (i32, [H, i64, P]),
+        "eq_grad_l2_loss": (i32, [H, P, u64, ctypes.POINTER(ctypes.c_double), P]),
+        "eq_grad_backward": (i32, [H, P, u64, P, u64, P, u64]),
+        "eq_grad_backward_device": (i32, [H, P, P, P]),
+        "eq_grad_frames": (i32, [H, ctypes.POINTER(ctypes.c_int64)]),
+        "eq_grad_set_wavefront_storage": (i32, [H, i32]),
+        "eq_grad_launch_count": (i32, [H, ctypes.POINTER(ctypes.c_uint64)]),
+        "eq_grad_set_boundaries_adj": (i32, [H, i32, P, u64]),
+        "eq_grad_lin_solve_adj": (i32, [H, i32, P, P, f32, f32, u64]),
+        "eq_grad_advect_adj": (i32, [H, i32, P, P, P, P, P, P, P, u64]),
+        "eq_grad_project_adj": (i32, [H, P, P, P, P, u64]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)

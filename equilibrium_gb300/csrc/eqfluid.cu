@@ -908,3 +908,6 @@ int eq_fluid_set_spin_limit(eq_fluid* h, int64_t iterations) {
 
 // Around the step: image, noise, device obstacles, graph-captured frames.
 #include "frame.cu"
+
+// The differentiation form (recorded forward, adjoint kernels, backward).
+#include "adjoint.cu"

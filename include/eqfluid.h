@@ -377,6 +377,63 @@ int eq_hfluid_stats(const eq_hfluid* h, eq_hstats* out);
 int eq_hfluid_get_stream(eq_hfluid* h, void** stream);
 int eq_hfluid_launch_count(const eq_hfluid* h, uint64_t* count);
 
+/* ---- the differentiation form: adjoint of the frame step --------------- */
+
+/* No counterpart in the reference (its step has no derivative). A recorded
+ * forward run of a plain handle and its reverse-mode derivative. The forward
+ * is the handle's own bit-exact step: for f in [0, nframes), src[f] (a dense
+ * size x size field, x fastest) is added to density and scratch at every cell
+ * (add_density at each cell, fluid.rs:120-124), then step() (fluid.rs:437-524).
+ * The state at every `checkpoint_every`-th frame is kept on the device;
+ * backward() recomputes each segment from its checkpoint with the fields
+ * every advect reads saved, and undoes it frame by frame with the adjoint
+ * kernels (set_boundaries^T, reverse Gauss-Seidel sweeps, the transposed
+ * bilinear scatter of advect, project^T), FP32 arithmetic. Gradients are
+ * those of the reference's f32 step, including its discrete choices (advect's
+ * row breaks and clamps) as the recorded run took them. The handle's configs
+ * and mask must not change between forward and backward (EQ_ERR_STATE);
+ * backward leaves the handle in the forward's final state. */
+typedef struct eq_grad eq_grad; /* opaque; binds one eq_fluid */
+
+int eq_grad_new(eq_fluid* h, int64_t max_frames, int64_t checkpoint_every, eq_grad** out);
+int eq_grad_free(eq_grad* g); /* accepts NULL */
+/* Runs nframes (<= max_frames) recorded frames from the handle's state.
+ * src: nframes * size * size floats (host), or NULL for no sources (n = 0). */
+int eq_grad_forward(eq_grad* g, int64_t nframes, const float* src, uint64_t n);
+int eq_grad_forward_device(eq_grad* g, int64_t nframes, const float* d_src);
+/* loss = 0.5 * sum over the interior of (density - target)^2 at the recorded
+ * run's end (FP64 sum); seeds backward() with its adjoint. adj_density
+ * (optional, host, size * size) receives density - target (0 on the frame). */
+int eq_grad_l2_loss(eq_grad* g, const float* target, uint64_t n, double* loss,
+                    float* adj_density);
+/* adj_final: the adjoints of the six arrays after the run (6 * size * size,
+ * EQ_FIELD_* order), or NULL to use the seed of eq_grad_l2_loss. Outputs
+ * (each optional): grad_init, the adjoints of the six arrays before the run
+ * (6 * size * size); grad_src, of every frame's source field
+ * (nframes * size * size). Host pointers; synchronises. */
+int eq_grad_backward(eq_grad* g, const float* adj_final, uint64_t n_adj, float* grad_init,
+                     uint64_t n_init, float* grad_src, uint64_t n_src);
+int eq_grad_backward_device(eq_grad* g, const float* d_adj_final, float* d_grad_init,
+                            float* d_grad_src);
+int eq_grad_frames(const eq_grad* g, int64_t* recorded);
+/* Caps where the transposed Gauss-Seidel wavefront keeps its band of live
+ * diagonals: 2 = y and its running sum in shared memory (the default where
+ * they fit), 1 = y only, 0 = global memory; -1 restores the default. */
+int eq_grad_set_wavefront_storage(eq_grad* g, int max_store);
+int eq_grad_launch_count(const eq_grad* g, uint64_t* count);
+/* The adjoint of one phase on host size x size arrays (in/out), at the bound
+ * handle's mask and configs: set_boundaries, lin_solve (x_b -> adjoint before
+ * the solve, x0_b accumulates), advect (at the forward state d0, u, v; d_b ->
+ * adjoint of the old d; d0_b, u_b, v_b accumulate; distinct arrays), project
+ * (p and div the aliased arrays, as in step()). */
+int eq_grad_set_boundaries_adj(eq_grad* g, int mode, float* xb, uint64_t n);
+int eq_grad_lin_solve_adj(eq_grad* g, int mode, float* xb, float* x0b, float a, float c,
+                          uint64_t n);
+int eq_grad_advect_adj(eq_grad* g, int mode, float* db, float* d0b, float* ub, float* vb,
+                       const float* d0, const float* u, const float* v, uint64_t n);
+int eq_grad_project_adj(eq_grad* g, float* vxb, float* vyb, float* pb, float* divb,
+                        uint64_t n);
+
 /* ---- lin_solve that allocates nothing ----------------------------------- */
 
 /* No counterpart in the reference. lin_solve (the same kernels, the same

@@ -78,6 +78,10 @@ def lib():
                                               P, P]),
             "eqo_lin_solve_adj_f64": (None, [ci, P, P, f64, f64, u32, i64, P]),
             "eqo_set_boundaries_adj_f64": (None, [ci, P, u32, P]),
+            "eqo_advect_adj_f32": (None, [ci, P, P, P, P, P, P, P, u32, f32, P]),
+            "eqo_project_adj_f64": (None, [P, P, P, P, u32, i64, P]),
+            "eqo_adjoint_problem_f32": (f32, [P, u32, f32, i64, f32, f32, i64, P, P, P, P, P,
+                                              P, P]),
             "eqo_fill_obstacle": (None, [P, u32, i64, i64, i64, i64]),
             "eqo_rectangle_valid": (ci, [i64, i64, i64, i64, i64]),
         }
@@ -299,6 +303,50 @@ def adjoint_problem_f64(cells, size, dt, iters, diff, visc, init, src, target, g
                                          src.shape[0], ptrs, _ptr(src), _ptr(target), None, None,
                                          None, ctypes.byref(sig))
     return loss, sig.value, None, None, None
+
+
+def adjoint_problem_f32(cells, size, dt, iters, diff, visc, init, src, target):
+    """adjoint_problem_f64 with the f32 forward and f32 adjoint arithmetic:
+    (loss, signature, g_vx, g_vy, g_src)."""
+    n = size * size
+    init = [np.ascontiguousarray(a, dtype=np.float32).reshape(-1) for a in init]
+    src = np.ascontiguousarray(src, dtype=np.float32).reshape(-1, n)
+    target = np.ascontiguousarray(target, dtype=np.float32).reshape(-1)
+    ptrs = (ctypes.c_void_p * 6)(*[_ptr(a) for a in init])
+    sig = ctypes.c_uint64()
+    gvx, gvy = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    gsrc = np.zeros_like(src)
+    loss = lib().eqo_adjoint_problem_f32(_ptr(cells), size, dt, iters, diff, visc, src.shape[0],
+                                         ptrs, _ptr(src), _ptr(target), _ptr(gvx), _ptr(gvy),
+                                         _ptr(gsrc), ctypes.byref(sig))
+    return loss, sig.value, gvx, gvy, gsrc
+
+
+def set_boundaries_adj_f64(mode, xb, size, cells):
+    x = np.ascontiguousarray(xb, dtype=np.float64).copy()
+    lib().eqo_set_boundaries_adj_f64(mode, _ptr(x), size, _ptr(cells))
+    return x
+
+
+def lin_solve_adj_f64(mode, xb, x0b, a, c, size, iters, cells):
+    x = np.ascontiguousarray(xb, dtype=np.float64).copy()
+    x0 = np.ascontiguousarray(x0b, dtype=np.float64).copy()
+    lib().eqo_lin_solve_adj_f64(mode, _ptr(x), _ptr(x0), a, c, size, iters, _ptr(cells))
+    return x, x0
+
+
+def advect_adj_f32(mode, db, d0b, ub, vb, d0, u, v, size, dt, cells):
+    io = [np.ascontiguousarray(a, dtype=np.float32).copy() for a in (db, d0b, ub, vb)]
+    ins = [np.ascontiguousarray(a, dtype=np.float32) for a in (d0, u, v)]
+    lib().eqo_advect_adj_f32(mode, *[_ptr(a) for a in io], *[_ptr(a) for a in ins], size, dt,
+                             _ptr(cells))
+    return io
+
+
+def project_adj_f64(vxb, vyb, pb, divb, size, iters, cells):
+    io = [np.ascontiguousarray(a, dtype=np.float64).copy() for a in (vxb, vyb, pb, divb)]
+    lib().eqo_project_adj_f64(*[_ptr(a) for a in io], size, iters, _ptr(cells))
+    return io
 
 
 def gaussian_target(size, nblobs=6, sigma=(8.0, 24.0), seed=0, amplitude=1.0):

@@ -157,6 +157,25 @@ void eqo_lin_solve_adj_f64(int mode, double* xb, double* x0b, double a, double c
 void eqo_set_boundaries_adj_f64(int mode, double* xb, uint32_t size, const uint8_t* cells) {
   set_boundaries_adj<double>((Mode)mode, xb, size, cells);
 }
+// advect^T in f32: the same discrete choices (row breaks, clamps) as the f32
+// forward that recorded d0, u, v.
+void eqo_advect_adj_f32(int mode, float* db, float* d0b, float* ub, float* vb, const float* d0,
+                        const float* u, const float* v, uint32_t size, float dt,
+                        const uint8_t* cells) {
+  advect_adj<float>((Mode)mode, db, d0b, ub, vb, d0, u, v, size, dt, cells);
+}
+void eqo_project_adj_f64(double* vxb, double* vyb, double* pb, double* divb, uint32_t size,
+                         int64_t iters, const uint8_t* cells) {
+  project_adj<double>(vxb, vyb, pb, divb, size, iters, cells);
+}
+// The same problem with the f32 forward (the tape the GPU adjoint records).
+float eqo_adjoint_problem_f32(const uint8_t* cells, uint32_t size, float dt, int64_t iters,
+                              float diff, float visc, int64_t nframes,
+                              const float* const init[6], const float* src, const float* target,
+                              float* g_vx, float* g_vy, float* g_src, uint64_t* sig) {
+  return adjoint_problem<float>(cells, size, dt, iters, diff, visc, nframes, init, src, target,
+                                g_vx, g_vy, g_src, sig);
+}
 
 // ---- mask / obstacles -----------------------------------------------------
 void eqo_fill_obstacle(uint8_t* cells, uint32_t size, int64_t x0, int64_t y0, int64_t x1,
