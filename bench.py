@@ -338,6 +338,266 @@ def run_precision_form(local_rank: int, frames: int, size: int = PREC_SIZE,
     return out
 
 
+# ---- the differentiation form ------------------------------------------------
+DIFF_SIZE, DIFF_FRAMES, DIFF_EVERY, DIFF_SEED = 258, 64, 8, 11
+DIFF_DT, DIFF_NU = 0.1, 1e-4
+
+
+def diff_problem(size=DIFF_SIZE, frames=DIFF_FRAMES, seed=DIFF_SEED):
+    """The differentiable workload: Fluid::new's density (the 0.9 block),
+    an initial velocity that is divergence-free and smooth (the curl of a
+    stream function of four seeded Gaussian vortices, sigma U[10, 30] cells,
+    scaled to max |v| = 0.3, i.e. backtraces of up to 7.7 cells a frame), two
+    seeded rectangle obstacles, per-frame density source fields (three
+    Gaussian puffs a frame, amplitude U[0, 2], sigma U[3, 10] cells) and a
+    target density of six Gaussian blobs (sigma U[8, 24] cells). Returns
+    (rects, cells, init (6 f32 arrays), src (frames, n) f32, target f32)."""
+    import oracle
+    rng = np.random.default_rng(seed)
+    n = size * size
+    rects = []
+    while len(rects) < 2:
+        w, h = (int(v) for v in rng.integers(size // 10, size // 5, 2))
+        x0, y0 = (int(v) for v in rng.integers(2, size - 2 - max(w, h), 2))
+        rects.append((x0, y0, x0 + w, y0 + h))
+    of = oracle.OracleFluid(size, DIFF_DT, ITERS, DIFF_NU, DIFF_NU)
+    for r in rects:
+        of.fill_obstacle(*r)
+    init = [f.copy() for f in of.fields]
+    y, x = np.mgrid[0:size, 0:size].astype(np.float64)
+    psi = np.zeros((size, size))
+    for _ in range(4):
+        cx, cy = rng.uniform(size * 0.2, size * 0.8, 2)
+        sg, sgn = rng.uniform(10, 30), rng.choice([-1.0, 1.0])
+        psi += sgn * sg * np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2 * sg * sg))
+    vx, vy = np.gradient(psi, axis=0), -np.gradient(psi, axis=1)
+    vmax = max(np.abs(vx).max(), np.abs(vy).max())
+    init[2] = (vx * (0.3 / vmax)).reshape(-1).astype(np.float32)
+    init[3] = (vy * (0.3 / vmax)).reshape(-1).astype(np.float32)
+    init[4] = np.zeros(n, np.float32)
+    init[5] = np.zeros(n, np.float32)
+    src = np.zeros((frames, size, size))
+    for fr in range(frames):
+        for _ in range(3):
+            cx, cy = rng.uniform(size * 0.2, size * 0.8, 2)
+            sg, amp = rng.uniform(3, 10), rng.uniform(0, 2)
+            src[fr] += amp * np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2 * sg * sg))
+    target = oracle.gaussian_target(size, 6, (8.0, 24.0), seed=seed + 1)
+    return (rects, of.cells.copy(), init, src.reshape(frames, n).astype(np.float32),
+            target.astype(np.float32))
+
+
+_FD_CACHE = {}
+
+
+def _fd_direction(k, n, nsrc):
+    d = np.random.default_rng(1000 + k).standard_normal(2 * n + nsrc)
+    return d / np.linalg.norm(d)
+
+
+def _fd_task(task):
+    """Central differences of the f64 forward of the differentiable workload
+    along seeded random unit direction k: plain runs, or runs that replay the
+    unperturbed run's advect choices (frozen). Runs in a spawned worker (the
+    oracle only)."""
+    import oracle
+    k, hs, frozen, size, frames = task
+    key = (size, frames)
+    if key not in _FD_CACHE:
+        _, cells, init, src, target = diff_problem(size, frames)
+        _FD_CACHE[key] = (cells, [a.astype(np.float64) for a in init], src.astype(np.float64),
+                          target.astype(np.float64))
+    cells, init, src, target = _FD_CACHE[key]
+    d = _fd_direction(k, size * size, src.size)
+    return oracle.fd_direction_f64(cells, size, DIFF_DT, ITERS, DIFF_NU, DIFF_NU, init, src,
+                                   target, d, hs, frozen=frozen)
+
+
+def fd_check(grads, size, frames, ndirs=32, h=1e-3, workers=None):
+    """Central differences of the f64 forward (step h) along `ndirs` seeded
+    random unit directions over (initial vx, vy, every source field) against
+    each gradient's directional derivative (grads: name -> flat gradient).
+    'plain': ordinary runs; the forward is only piecewise smooth (advect's
+    cell choice, clamps and row breaks), so a direction whose runs cross a
+    bilinear cell boundary differs by the kink. 'frozen_path': the perturbed
+    runs replay the unperturbed run's choices, the derivative the adjoint
+    computes (O(h^2) agreement)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    n = size * size
+    tasks = [(k, (h,), frozen, size, frames) for k in range(ndirs) for frozen in (False, True)]
+    workers = workers or max(1, min(len(tasks), os.cpu_count() or 1))
+    t0 = time.perf_counter()
+    with cf.ProcessPoolExecutor(workers, mp_context=mp.get_context("spawn")) as ex:
+        res = list(ex.map(_fd_task, tasks))
+    out = {"directions": ndirs, "h": h, "workers": workers,
+           "seconds": time.perf_counter() - t0,
+           "metric": "per direction d: |fd - g.d| / rms, rms = |g|_2 / sqrt(dim) (the typical "
+                     "size of g.d over random unit d); 'rel_to_fd' = |fd - g.d| / |fd|"}
+    nsrc = frames * n
+    for name, gv in grads.items():
+        gv = gv.astype(np.float64)
+        rms = np.linalg.norm(gv) / np.sqrt(gv.size)
+        for kind, fz in (("plain", False), ("frozen_path", True)):
+            e_rms, e_fd = [], []
+            for k in range(ndirs):
+                (lp, lm), = res[2 * k + (1 if fz else 0)]
+                fd = (lp - lm) / (2 * h)
+                diff = abs(fd - gv @ _fd_direction(k, n, nsrc))
+                e_rms.append(diff / rms)
+                e_fd.append(diff / max(abs(fd), 1e-300))
+            out[f"{name}_vs_{kind}"] = {"median": float(np.median(e_rms)),
+                                        "max": float(np.max(e_rms)),
+                                        "rel_to_fd_median": float(np.median(e_fd))}
+    return out
+
+
+def run_diff_form(local_rank: int, reps: int = 2, fd_dirs: int = 32, size: int = DIFF_SIZE,
+                  frames: int = DIFF_FRAMES):
+    """The differentiation form: one gradient evaluation = `frames` recorded
+    frames + the L2 loss + backward() (checkpoints every 8 frames, the
+    segment recomputed, the adjoint kernels); cell-steps/s counts the
+    differentiated frames' interior cells. Checked against the f32 and f64
+    tape adjoints and by central differences of the f64 forward."""
+    import torch
+    import oracle
+    from equilibrium_gb300 import _lib
+    from equilibrium_gb300.adjoint import Recorder
+    from equilibrium_gb300.simulation import Fluid, FluidConfigs, SimulationConfigs
+    L = _lib.load()
+    rects, cells, init, src, target = diff_problem(size, frames)
+    n = size * size
+    f = Fluid(FluidConfigs(DIFF_NU, DIFF_NU, False), SimulationConfigs(DIFF_DT, ITERS, size),
+              device=local_rank)
+    for r in rects:
+        _lib.check(L.eq_fluid_fill_obstacle(f.handle, *r))
+    g = Recorder(f, frames, DIFF_EVERY)
+    sp = ctypes.c_void_p()
+    _lib.check(L.eq_fluid_get_stream(f.handle, ctypes.byref(sp)))
+    stream = torch.cuda.ExternalStream(sp.value)
+    dev = torch.device("cuda", local_rank)
+    d_src = torch.from_numpy(src).to(dev)
+    d_gi = torch.empty(6 * n, dtype=torch.float32, device=dev)
+    d_gs = torch.empty(frames * n, dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def reset():
+        for k in range(6):
+            f.write_field(k, init[k])
+
+    # device-resident: sources and gradients stay on the GPU
+    dev_ms, fwd_ms, bwd_ms, launches = [], [], [], []
+    gs_ms, gs_n = ctypes.c_double(), ctypes.c_uint64()
+    for rep in range(reps + 1):
+        reset()
+        with torch.cuda.stream(stream):
+            flush.fill_(float(rep))
+        torch.cuda.synchronize()
+        if rep == reps:
+            _lib.check(L.eq_grad_set_profiling(g.handle, 1))
+        c0 = g.launch_count()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record(stream)
+        _lib.check(L.eq_grad_forward_device(g.handle, frames, d_src.data_ptr()))
+        g.nframes = frames
+        e[1].record(stream)
+        g.l2_loss(target)
+        _lib.check(L.eq_grad_backward_device(g.handle, None, d_gi.data_ptr(), d_gs.data_ptr()))
+        e[2].record(stream)
+        torch.cuda.synchronize()
+        if rep > 0:
+            dev_ms.append(e[0].elapsed_time(e[2]))
+            fwd_ms.append(e[0].elapsed_time(e[1]))
+            bwd_ms.append(e[1].elapsed_time(e[2]))
+            launches.append(g.launch_count() - c0)
+    _lib.check(L.eq_grad_kernel_stats(g.handle, ctypes.byref(gs_ms), ctypes.byref(gs_n)))
+    _lib.check(L.eq_grad_set_profiling(g.handle, 0))
+    gi = d_gi.view(6, n).cpu().numpy()
+    gsrc = d_gs.view(frames, n).cpu().numpy()
+    # end to end through the C ABI with host buffers
+    e2e_ms = []
+    for rep in range(reps):
+        reset()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.forward(src)
+        loss = g.l2_loss(target)
+        h_gi, h_gs = g.backward()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    # advect^T scatters with float atomics: runs agree to rounding, not bit for bit
+    rerun = max(float(np.linalg.norm(h_gi - gi) / np.linalg.norm(gi)),
+                float(np.linalg.norm(h_gs - gsrc) / np.linalg.norm(gsrc)))
+    assert rerun < 1e-4, rerun
+    t = statistics.mean(dev_ms)
+    cells_steps = (size - 2) ** 2 * frames
+    out = {"workload": f"one scene, N = {size - 2} interior, dt {DIFF_DT}, diffusion = viscosity "
+                       f"= {DIFF_NU}, 20 sweeps, {frames} frames, 2 seeded rectangles, a seeded "
+                       "density source field per frame, loss = 0.5 * L2^2 to a 6-blob Gaussian "
+                       f"target; gradient w.r.t. the initial velocity and every source field, "
+                       f"checkpoints every {DIFF_EVERY} frames",
+           "value": cells_steps / (t / 1e3), "unit": "cell-steps/s (differentiated frames)",
+           "ms_per_gradient": t, "ms_forward": statistics.mean(fwd_ms),
+           "ms_loss_and_backward": statistics.mean(bwd_ms), "reps_timed": len(dev_ms),
+           "gpu_launches_per_gradient": statistics.mean(launches),
+           "clock": "CUDA events on the scene's stream, L2 flushed before each gradient",
+           "e2e": {"value": cells_steps / (statistics.mean(e2e_ms) / 1e3),
+                   "unit": "cell-steps/s", "ms_per_gradient": statistics.mean(e2e_ms),
+                   "h2d_bytes_per_gradient": frames * n * 4 + n * 4,
+                   "d2h_bytes_per_gradient": (6 + frames) * n * 4 + 8},
+           "loss": loss, "rerun_rel_diff": rerun}
+    avg_gs = gs_ms.value / max(gs_n.value, 1)
+    store, blocks = g.wavefront_storage()
+    # the adjoint wavefront: per cell and sweep it reads 2 + 2 (+ sum) values
+    # and writes 2 on chip; its DRAM traffic is the incoming adjoint, the
+    # codes and the outputs (13 B per cell), so it is bound by the SM, not HBM
+    out["roofline"] = {"bound": "hbm", "kernel": ("k_gs_adj_cl (transposed Gauss-Seidel "
+                       f"wavefront over a cluster of {blocks} blocks, distributed shared memory)"
+                       if store == 3 else f"k_gs_adj (transposed Gauss-Seidel wavefront, one "
+                       f"block, storage form {store})"),
+                       "achieved": 13 * size * size / (avg_gs / 1e3) / 1e9 if avg_gs > 0 else None,
+                       "unit": "GB/s", "avg_launch_ms": avg_gs, "launches": int(gs_n.value),
+                       "share_of_gradient": gs_ms.value / statistics.mean(dev_ms[-1:]),
+                       "cell_sweeps_per_s": size * size * ITERS / (avg_gs / 1e3) if avg_gs else None,
+                       "traffic": None}
+    # accuracy against the tape adjoints (host, 1 core) and finite differences
+    t0 = time.perf_counter()
+    l32, s32, vx32, vy32, src32 = oracle.adjoint_problem_f32(
+        cells, size, DIFF_DT, ITERS, DIFF_NU, DIFF_NU, init, src, target)
+    t32 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    l64, s64, vx64, vy64, src64 = oracle.adjoint_problem_f64(
+        cells, size, DIFF_DT, ITERS, DIFF_NU, DIFF_NU, [a.astype(np.float64) for a in init],
+        src.astype(np.float64), target.astype(np.float64))
+    t64 = time.perf_counter() - t0
+
+    def rel(a, b):
+        return float(np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b))
+    out["errors"] = {
+        "vs_f32_tape": {"g_vx": rel(gi[2], vx32), "g_vy": rel(gi[3], vy32),
+                        "g_src": rel(gsrc, src32), "loss_rel": abs(loss - l32) / abs(l32)},
+        "vs_f64_tape": {"g_vx": rel(gi[2], vx64), "g_vy": rel(gi[3], vy64),
+                        "g_src": rel(gsrc, src64), "same_discrete_path": s32 == s64},
+        "f32_tape_vs_f64_tape": {"g_vx": rel(vx32, vx64), "g_vy": rel(vy32, vy64),
+                                 "g_src": rel(src32, src64)},
+        "metric": "relative L2 norm of the difference"}
+    out["cpu_baseline"] = {"value": cells_steps / t64, "unit": "cell-steps/s", "cores": 1,
+                           "kind": "port",
+                           "sample": f"the f64 tape adjoint of the oracle, forward + backward, "
+                                     f"the full workload ({t64:.1f} s); the f32 tape: "
+                                     f"{cells_steps / t32:.3g} cell-steps/s"}
+    if fd_dirs:
+        try:
+            flat = lambda a, b, c: np.concatenate([a.reshape(-1), b.reshape(-1), c.reshape(-1)])
+            out["finite_differences"] = fd_check(
+                {"gpu": flat(gi[2], gi[3], gsrc), "f64_tape": flat(vx64, vy64, src64)},
+                size, frames, fd_dirs)
+        except Exception as e:  # reported, never silently replaced
+            out["finite_differences"] = {"error": f"{type(e).__name__}: {e}"}
+    g.close()
+    f.close()
+    return out
+
+
 def run_case(case: str):
     """Small, self-contained runs of one form, for kernel profiles."""
     import torch
@@ -359,6 +619,27 @@ def run_case(case: str):
         print(json.dumps({"case": case, "ms": (time.perf_counter() - t) * 1e3,
                           "cells": b.cell_count()}))
         b.close()
+    elif case == "diff256":
+        from equilibrium_gb300 import _lib
+        from equilibrium_gb300.adjoint import Recorder
+        from equilibrium_gb300.simulation import Fluid, FluidConfigs, SimulationConfigs
+        frames = 4
+        rects, cells, init, src, target = diff_problem(DIFF_SIZE, frames)
+        f = Fluid(FluidConfigs(DIFF_NU, DIFF_NU, False),
+                  SimulationConfigs(DIFF_DT, ITERS, DIFF_SIZE))
+        for r in rects:
+            _lib.check(_lib.load().eq_fluid_fill_obstacle(f.handle, *r))
+        for k in range(6):
+            f.write_field(k, init[k])
+        g = Recorder(f, frames, frames)
+        t = time.perf_counter()
+        g.forward(src)
+        loss = g.l2_loss(target)
+        gi, gs = g.backward()
+        print(json.dumps({"case": case, "ms": (time.perf_counter() - t) * 1e3, "loss": loss,
+                          "launches": g.launch_count()}))
+        g.close()
+        f.close()
     else:
         from equilibrium_gb300.precision import HalfFluid
         size = 1026
@@ -660,6 +941,7 @@ def run_ours(args):
         form("batched_f16", lambda: run_batched_form(local_rank, args.batch_frames, 0, "f16",
                                                      autotune=False, err_sample=24))
         form("precision", lambda: run_precision_form(local_rank, args.precision_frames))
+        form("differentiation", lambda: run_diff_form(local_rank, fd_dirs=args.fd_dirs))
         for k in ("f16", "bf16"):
             if "precision" in forms and k in forms["precision"]:
                 forms["precision"][k]["vs_plain"] = forms["precision"][k]["value"] / value
@@ -688,11 +970,16 @@ def main():
     ap.add_argument("--cpu-frames", type=int, default=12)
     ap.add_argument("--batch-frames", type=int, default=5)
     ap.add_argument("--precision-frames", type=int, default=4)
+    ap.add_argument("--fd-dirs", type=int, default=32,
+                    help="random directions of the differentiation form's finite-difference check")
+    ap.add_argument("--diff-only", action="store_true",
+                    help="only the differentiation form (N=256, 64 frames)")
     ap.add_argument("--case", default=None,
-                    choices=["batch256", "batch256_f16", "precision1024"],
+                    choices=["batch256", "batch256_f16", "precision1024", "diff256"],
                     help="one small run for profiling: 'batch256' = one frame of 256 scenes of "
                          "the batched workload (after one warm-up frame), 'precision1024' = two "
-                         "frames of the precision form at N = 1024 (FP16)")
+                         "frames of the precision form at N = 1024 (FP16), 'diff256' = one "
+                         "gradient of the differentiation workload at N = 256 over 4 frames")
     ap.add_argument("--precision-study", action="store_true",
                     help="only the precision form's error study: N=512, errors at frames 1, "
                          "50 and 200 against both f64 references")
@@ -710,6 +997,12 @@ def main():
         torch.cuda.set_device(0)
         print(json.dumps({"precision_study": run_precision_form(
             0, 3, size=514, err_frames=(1, 50, 200))}), flush=True)
+    elif args.diff_only:
+        import torch
+        from equilibrium_gb300 import build as eqbuild
+        eqbuild.build()
+        torch.cuda.set_device(0)
+        print(json.dumps({"differentiation": run_diff_form(0, fd_dirs=args.fd_dirs)}), flush=True)
     elif args.impl == "reference":
         run_reference(args)
     else:

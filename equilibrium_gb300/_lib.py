@@ -170,6 +170,11 @@ def load(path: str = LIB_PATH):
         "eq_grad_backward_device": (i32, [H, P, P, P]),
         "eq_grad_frames": (i32, [H, ctypes.POINTER(ctypes.c_int64)]),
         "eq_grad_set_wavefront_storage": (i32, [H, i32]),
+        "eq_grad_get_wavefront_storage": (i32, [H, ctypes.POINTER(ctypes.c_int),
+                                                ctypes.POINTER(ctypes.c_int)]),
+        "eq_grad_set_profiling": (i32, [H, i32]),
+        "eq_grad_kernel_stats": (i32, [H, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_uint64)]),
         "eq_grad_launch_count": (i32, [H, ctypes.POINTER(ctypes.c_uint64)]),
         "eq_grad_set_boundaries_adj": (i32, [H, i32, P, u64]),
         "eq_grad_lin_solve_adj": (i32, [H, i32, P, P, f32, f32, u64]),

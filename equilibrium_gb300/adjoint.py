@@ -99,6 +99,13 @@ class Recorder:
     def set_wavefront_storage(self, max_store: int):
         check(self._L.eq_grad_set_wavefront_storage(self.handle, int(max_store)))
 
+    def wavefront_storage(self):
+        """(store, blocks) of the last transposed solve (see the C header)."""
+        st, cl = ctypes.c_int(), ctypes.c_int()
+        check(self._L.eq_grad_get_wavefront_storage(self.handle, ctypes.byref(st),
+                                                    ctypes.byref(cl)))
+        return st.value, cl.value
+
     def launch_count(self) -> int:
         c = ctypes.c_uint64()
         check(self._L.eq_grad_launch_count(self.handle, ctypes.byref(c)))

@@ -21,6 +21,7 @@ struct eq_grad {
   float* ckpt = nullptr;        // nseg x 6 pitched grids
   float* final_state = nullptr; // 6 pitched grids
   float* tape = nullptr;        // every x 5 pitched grids (vx0, vy0, vx, vy, sc)
+  int64_t tape_seg = -1;        // the segment whose frames the tape holds
   float* src = nullptr;         // max_frames x S x S dense
   bool have_src = false;
   float* adj = nullptr;         // the six adjoint grids (anti-diagonal)
@@ -32,8 +33,11 @@ struct eq_grad {
   float* pstage = nullptr;      // 3 pitched grids (per-phase advect inputs)
   double* d_loss = nullptr;
   uint64_t launches = 0;
+  bool profiling = false;  // event pairs around every adjoint wavefront launch
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> gs_events;
   int gs_store = 0;   // where the adjoint wavefront keeps its band (see gs_adj_smem_bytes)
-  int gs_force = -1;  // cap on gs_store (tests of the global-memory forms)
+  int gs_force = -1;  // cap on gs_store (tests of the other forms)
+  int gs_cluster = 8; // blocks per cluster (gs_store == 3)
 };
 
 namespace {
@@ -82,22 +86,71 @@ int adj_bnd(eq_grad* g, int mode, float* x) {
   return EQ_OK;
 }
 
+// Threads of one cluster block: a warp per (sweep, 32-position chunk) task,
+// at most 32 warps.
+int gs_cl_threads(int S, int K, int C) {
+  const int J = (S - 2 + C - 1) / C;
+  return 32 * std::min(32, K * ((J + 31) / 32));
+}
+
 template <int MODE>
 int launch_gs_adj(eq_grad* g, const eqk::GsAdjArgs& A) {
   const int store = g->gs_store;
   const size_t smem = eqk::gs_adj_smem_bytes(store, A.S, A.K);
   cudaStream_t s = g->h->stream;
+  if (store == 3) {  // a cluster of g->gs_cluster blocks
+    cudaEvent_t c0 = nullptr, c1 = nullptr;
+    if (g->profiling) {
+      EQ_CUDA(cudaEventCreate(&c0));
+      EQ_CUDA(cudaEventCreate(&c1));
+      EQ_CUDA(cudaEventRecord(c0, s));
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(g->gs_cluster);
+    cfg.blockDim = dim3(gs_cl_threads(A.S, A.K, g->gs_cluster));
+    cfg.dynamicSmemBytes = eqk::gs_cl_layout(A.S, A.K, g->gs_cluster).total;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = g->gs_cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_gs_adj_cl<MODE>, A));
+    int rc = gcheck(g);
+    if (rc) return rc;
+    if (g->profiling) {
+      EQ_CUDA(cudaEventRecord(c1, s));
+      g->gs_events.emplace_back(c0, c1);
+    }
+    return EQ_OK;
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (g->profiling) {
+    EQ_CUDA(cudaEventCreate(&e0));
+    EQ_CUDA(cudaEventCreate(&e1));
+    EQ_CUDA(cudaEventRecord(e0, s));
+  }
   if (store == 2)
     eqk::k_gs_adj<MODE, 2><<<1, 1024, smem, s>>>(A);
   else if (store == 1)
     eqk::k_gs_adj<MODE, 1><<<1, 1024, smem, s>>>(A);
   else
     eqk::k_gs_adj<MODE, 0><<<1, 1024, 0, s>>>(A);
-  return gcheck(g);
+  int rc = gcheck(g);
+  if (rc) return rc;
+  if (g->profiling) {
+    EQ_CUDA(cudaEventRecord(e1, s));
+    g->gs_events.emplace_back(e0, e1);
+  }
+  return EQ_OK;
 }
 
-// The storage form of the wavefront for this size and sweep count: shared
-// memory when the band fits (the attribute is raised once per kernel).
+// The storage form of the wavefront for this size and sweep count: a cluster
+// when every block keeps >= 16 positions, its share fits and the device can
+// hold the cluster, else one block with shared memory where the band fits
+// (the kernels' attributes are raised once).
 int pick_gs_store(eq_grad* g, int S, int K) {
   static bool raised = false;
   int dev = g->h->device, optin = 0;
@@ -106,19 +159,58 @@ int pick_gs_store(eq_grad* g, int S, int K) {
     auto raise = [&](const void* fn) {
       return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     };
+    auto nonportable = [&](const void* fn) {
+      return cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    };
     if (raise((const void*)eqk::k_gs_adj<eqk::kRow, 1>) != cudaSuccess ||
         raise((const void*)eqk::k_gs_adj<eqk::kRow, 2>) != cudaSuccess ||
         raise((const void*)eqk::k_gs_adj<eqk::kCol, 1>) != cudaSuccess ||
         raise((const void*)eqk::k_gs_adj<eqk::kCol, 2>) != cudaSuccess ||
         raise((const void*)eqk::k_gs_adj<eqk::kPassive, 1>) != cudaSuccess ||
-        raise((const void*)eqk::k_gs_adj<eqk::kPassive, 2>) != cudaSuccess)
+        raise((const void*)eqk::k_gs_adj<eqk::kPassive, 2>) != cudaSuccess ||
+        raise((const void*)eqk::k_gs_adj_cl<eqk::kRow>) != cudaSuccess ||
+        raise((const void*)eqk::k_gs_adj_cl<eqk::kCol>) != cudaSuccess ||
+        raise((const void*)eqk::k_gs_adj_cl<eqk::kPassive>) != cudaSuccess ||
+        nonportable((const void*)eqk::k_gs_adj_cl<eqk::kRow>) != cudaSuccess ||
+        nonportable((const void*)eqk::k_gs_adj_cl<eqk::kCol>) != cudaSuccess ||
+        nonportable((const void*)eqk::k_gs_adj_cl<eqk::kPassive>) != cudaSuccess)
       return fail(EQ_ERR_CUDA, "cudaFuncSetAttribute (adjoint wavefront)");
     raised = true;
   }
-  g->gs_store = eqk::gs_adj_smem_bytes(2, S, K) <= (size_t)optin   ? 2
-                : eqk::gs_adj_smem_bytes(1, S, K) <= (size_t)optin ? 1
-                                                                   : 0;
-  if (g->gs_force >= 0) g->gs_store = std::min(g->gs_store, g->gs_force);
+  bool ok[4];
+  ok[0] = true;
+  ok[1] = eqk::gs_adj_smem_bytes(1, S, K) <= (size_t)optin;
+  ok[2] = eqk::gs_adj_smem_bytes(2, S, K) <= (size_t)optin;
+  ok[3] = false;
+  const int C = (S - 2) >= 384 ? 16 : 8;
+  const size_t cl_bytes = eqk::gs_cl_layout(S, K, C).total;
+  if ((S - 2) / C >= 16 && cl_bytes <= (size_t)optin) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(gs_cl_threads(S, K, C));
+    cfg.dynamicSmemBytes = cl_bytes;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    ok[3] = cudaOccupancyMaxActiveClusters(&nclusters, eqk::k_gs_adj_cl<eqk::kRow>, &cfg) ==
+                cudaSuccess &&
+            nclusters >= 1;
+    cudaGetLastError();  // a refused query leaves the single-block forms
+  }
+  const int cap = g->gs_force >= 0 ? g->gs_force : 3;
+  int store = 0;
+  for (int k = cap; k >= 0; --k)
+    if (ok[k]) {
+      store = k;
+      break;
+    }
+  g->gs_store = store;
+  g->gs_cluster = C;
   return EQ_OK;
 }
 
@@ -304,11 +396,19 @@ int run_forward(eq_grad* g, int64_t nframes) {
   g->visc = h->visc;
   g->K = h->frames;
   g->cells = h->host_cells;
+  // The last segment's frames keep their tape as they run: backward starts
+  // there without recomputing it.
+  const int64_t last = (nframes - 1) / g->every;
+  const size_t tstride = (size_t)kTapeFields * g->grid;
   for (int64_t f = 0; f < nframes; ++f) {
     if (f % g->every == 0)
       if ((rc = copy_state(g, g->ckpt + (size_t)(f / g->every) * 6 * g->grid, h->block))) return rc;
-    if ((rc = add_frame_source(g, f)) || (rc = launch_step(h))) return rc;
+    if ((rc = add_frame_source(g, f))) return rc;
+    rc = (f / g->every == last) ? step_taped(g, g->tape + (size_t)(f - last * g->every) * tstride)
+                                : launch_step(h);
+    if (rc) return rc;
   }
+  g->tape_seg = last;
   if ((rc = copy_state(g, g->final_state, h->block))) return rc;
   g->nframes = nframes;
   g->recorded = true;
@@ -344,10 +444,15 @@ int run_backward(eq_grad* g, const float* d_adj_final, float* d_grad_init, float
   const size_t tstride = (size_t)kTapeFields * g->grid;
   for (int64_t seg = nseg - 1; seg >= 0; --seg) {
     const int64_t f0 = seg * g->every, f1 = std::min(f0 + g->every, g->nframes);
-    if ((rc = copy_state(g, h->block, g->ckpt + (size_t)seg * 6 * g->grid))) return rc;
-    for (int64_t f = f0; f < f1; ++f)
-      if ((rc = add_frame_source(g, f)) || (rc = step_taped(g, g->tape + (size_t)(f - f0) * tstride)))
-        return rc;
+    if (g->tape_seg != seg) {  // recompute the segment from its checkpoint
+      g->tape_seg = -1;
+      if ((rc = copy_state(g, h->block, g->ckpt + (size_t)seg * 6 * g->grid))) return rc;
+      for (int64_t f = f0; f < f1; ++f)
+        if ((rc = add_frame_source(g, f)) ||
+            (rc = step_taped(g, g->tape + (size_t)(f - f0) * tstride)))
+          return rc;
+      g->tape_seg = seg;
+    }
     for (int64_t f = f1 - 1; f >= f0; --f) {
       if ((rc = adj_step(g, g->tape + (size_t)(f - f0) * tstride))) return rc;
       if (d_grad_src && (rc = to_dense(g, gadj(g, EQ_FIELD_DENSITY), gadj(g, EQ_FIELD_SCRATCH),
@@ -366,6 +471,10 @@ int run_backward(eq_grad* g, const float* d_adj_final, float* d_grad_init, float
 void free_grad(eq_grad* g) {
   if (!g) return;
   if (g->h) cudaSetDevice(g->h->device);
+  for (auto& e : g->gs_events) {
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
   cudaFree(g->ckpt);
   cudaFree(g->final_state);
   cudaFree(g->tape);
@@ -566,10 +675,42 @@ int eq_grad_launch_count(const eq_grad* g, uint64_t* count) {
   return EQ_OK;
 }
 
+int eq_grad_set_profiling(eq_grad* g, int enable) {
+  if (!g) return fail(EQ_ERR_ARG, "null handle");
+  g->profiling = enable != 0;
+  return EQ_OK;
+}
+
+int eq_grad_kernel_stats(eq_grad* g, double* total_ms, uint64_t* launches) {
+  if (!g || !total_ms || !launches) return fail(EQ_ERR_ARG, "null argument");
+  int rc = select_device(g->h);
+  if (rc) return rc;
+  EQ_CUDA(cudaStreamSynchronize(g->h->stream));
+  double sum = 0.0;
+  for (auto& e : g->gs_events) {
+    float ms = 0.f;
+    EQ_CUDA(cudaEventElapsedTime(&ms, e.first, e.second));
+    sum += ms;
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
+  *total_ms = sum;
+  *launches = g->gs_events.size();
+  g->gs_events.clear();
+  return EQ_OK;
+}
+
 int eq_grad_set_wavefront_storage(eq_grad* g, int max_store) {
   if (!g) return fail(EQ_ERR_ARG, "null handle");
-  if (max_store < -1 || max_store > 2) return fail(EQ_ERR_ARG, "max_store must be in [-1, 2]");
+  if (max_store < -1 || max_store > 3) return fail(EQ_ERR_ARG, "max_store must be in [-1, 3]");
   g->gs_force = max_store;
+  return EQ_OK;
+}
+
+int eq_grad_get_wavefront_storage(const eq_grad* g, int* store, int* cluster_blocks) {
+  if (!g || !store || !cluster_blocks) return fail(EQ_ERR_ARG, "null argument");
+  *store = g->gs_store;
+  *cluster_blocks = g->gs_store == 3 ? g->gs_cluster : 1;
   return EQ_OK;
 }
 

@@ -35,6 +35,8 @@
 // y_s lives in the buffer of s's parity), one __syncthreads per step. The
 // band of live diagonals stays in shared memory where it fits.
 #pragma once
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "kernels.cuh"
 #include "wave.cuh"
@@ -232,6 +234,219 @@ __global__ void __launch_bounds__(1024, 1) k_gs_adj(GsAdjArgs A) {
     }
     if (STORE && --tb < 0) tb += R;
     __syncthreads();
+  }
+}
+
+// The same wavefront spread over a thread-block cluster of C blocks (one SM
+// each): block r owns the positions j in [1 + r J, (r + 1) J] of every
+// anti-diagonal (J = ceil(N / C)). Its shared memory holds, for its strip,
+// y and its sum in a ring of R = 3K + 4 diagonals, the incoming adjoint B of
+// every diagonal, and the boundary codes with one position of halo either
+// side, all staged once at the start, so that a step touches no global
+// memory except the final stores. The ring rows carry a halo too (positions
+// jb-2, jb-1 and je+1): whoever computes a strip's first or last two
+// positions also stores them into the neighbour block's halo through
+// distributed shared memory, so every read is local and no remote load sits
+// on a step's critical path. One cluster barrier per step orders every write,
+// local or remote, before the next step's reads, in all blocks.
+struct GsClLayout {  // byte offsets in one block's shared memory
+  size_t ring, b, code, flags, total;
+};
+__host__ __device__ inline GsClLayout gs_cl_layout(int S, int K, int C) {
+  const size_t J = (size_t)((S - 2 + C - 1) / C), R = (size_t)(3 * K + 4), D = (size_t)(2 * S - 1);
+  GsClLayout L;
+  L.ring = 0;                                          // 3 R (J + 3) floats (Y0, Y1, sum)
+  L.b = 3 * R * (J + 3) * 4;                           // D J floats
+  L.code = L.b + D * J * 4;                            // D (J + 2) bytes
+  L.flags = L.code + ((D * (J + 2) + 15) / 16) * 16;  // rowfl, colfl: 2 S bytes
+  L.total = L.flags + 2 * (size_t)S;
+  return L;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(1024, 1) k_gs_adj_cl(GsAdjArgs A) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char gs_cl_smem[];
+  const int S = A.S, P = A.P, K = A.K, N = S - 2, D0 = 2 * N, R = A.R;
+  const int C = (int)cluster.num_blocks(), r = (int)cluster.block_rank();
+  const int J = (N + C - 1) / C, JC = J + 2, W = J + 3;
+  const int jb = 1 + r * J, je = min(N, jb + J - 1);
+  const GsClLayout lay = gs_cl_layout(S, K, C);
+  float* const Y0 = reinterpret_cast<float*>(gs_cl_smem + lay.ring);
+  float* const Y1 = Y0 + (size_t)R * W;
+  float* const Ysm = Y0 + 2 * (size_t)R * W;
+  // the neighbours' rings (for the halo stores)
+  float* const Y0lo = r > 0 ? cluster.map_shared_rank(Y0, r - 1) : nullptr;
+  float* const Y0hi = r < C - 1 ? cluster.map_shared_rank(Y0, r + 1) : nullptr;
+  float* const Bs = reinterpret_cast<float*>(gs_cl_smem + lay.b);
+  uint8_t* const Cs = gs_cl_smem + lay.code;
+  uint8_t* const rowfl = gs_cl_smem + lay.flags;
+  uint8_t* const colfl = rowfl + S;
+  // stage B (own positions) and the codes (positions jb-1 .. je+1) of every diagonal
+  const int nd = 2 * S - 1;
+  for (int e = threadIdx.x; e < nd * JC; e += blockDim.x) {
+    const int d = e / JC, k = e - d * JC, j = jb - 1 + k;
+    const bool in = j >= 0 && j < S && d - j >= 0 && d - j < S;
+    Cs[e] = in ? A.code[(size_t)d * P + j] : (uint8_t)0;
+    if (k >= 1 && k <= J) Bs[(size_t)d * J + (k - 1)] = (in && j <= je) ? A.B[(size_t)d * P + j] : 0.0f;
+  }
+  for (int e = threadIdx.x; e < S; e += blockDim.x) {
+    rowfl[e] = A.rowfl[e];
+    colfl[e] = A.colfl[e];
+  }
+  auto code_at = [&](int d, int jj) { return Cs[d * JC + (jj - jb + 1)]; };
+  const int nsteps = (D0 - 2) + 3 * (K - 1) + 1;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const int ntask = K * ((J + 31) >> 5);
+  const int s0 = warp % K, c0 = warp / K, ds = nwarps % K, dc = nwarps / K;
+  const float al = A.alpha;
+  // y at (ring slot, position j in [jb-2, je+1]) of buffer `buf`
+  auto yat = [&](const float* buf, int slot, int jj) -> float {
+    return buf[slot * W + (jj - jb + 2)];
+  };
+  int tb = D0 % R;  // ring slot of diagonal D0 - t
+  cluster.sync();   // staging done; every block of the cluster runs before any remote read
+  if (ntask <= nwarps) {
+    // One task per warp (the usual shape): the warp's sweep and positions are
+    // fixed, its diagonal, column and ring row step down by one per step.
+    const int s = warp % K, j = jb + ((warp / K) << 5) + lane;
+    const bool jok = warp < ntask && j <= je;
+    float* const Yc = ((s & 1) ? Y1 : Y0) + (j - jb + 2);
+    const float* const Yp = ((s & 1) ? Y0 : Y1) + (j - jb + 2);
+    float* const Ys = Ysm + (j - jb + 2);
+    const size_t boff = (s & 1) ? (size_t)R * W : 0;
+    float* const plo = (jok && j == jb && Y0lo) ? Y0lo + boff + J + 2 : nullptr;
+    float* const phi = (jok && j >= je - 1 && Y0hi) ? Y0hi + boff + (j - je + 1) : nullptr;
+    const bool jp1 = j + 1 <= N, jm1 = j - 1 >= 1, jm2 = j - 2 >= 1;
+    const int RW = R * W;
+    int r0 = tb + 3 * s;
+    if (r0 >= R) r0 -= R;
+    int o0 = r0 * W;  // ring row of diagonal d = D0 - t + 3s
+    for (int t = 0; t < nsteps; ++t) {
+      const int d = D0 - t + 3 * s, i = d - j;
+      if (jok && t >= 3 * s && i >= 1 && i <= N) {
+        const int op1 = o0 + W == RW ? 0 : o0 + W;
+        const int om1 = o0 == 0 ? RW - W : o0 - W;
+        const int om2 = om1 == 0 ? RW - W : om1 - W;
+        float v = al * ((i < N ? Yc[op1] : 0.0f) + (jp1 ? Yc[op1 + 1] : 0.0f));
+        if (s == 0) {
+          v += Bs[(size_t)d * J + (j - jb)];
+        } else {
+          const uint8_t cd = code_at(d, j);
+          const bool written = (MODE == kRow)   ? (cd & kCodeRowMask) != 0
+                               : (MODE == kCol) ? (cd & kCodeColMask) != 0
+                                                : false;
+          if (!written) v += al * ((i > 1 ? Yp[om1] : 0.0f) + (jm1 ? Yp[om1 - 1] : 0.0f));
+          if (MODE == kPassive) {
+            if (i == 1 || i == N || j == 1 || j == N) {
+              const int n = (j == 1 && colfl[i]) + (j == N && colfl[i]) + (i == 1 && rowfl[j]) +
+                            (i == N && rowfl[j]);
+              v += al * (float)n * Yp[o0];
+            }
+          } else if (cd & kCodeWall) {
+            if (MODE == kRow) {
+              if (i > 1 && (code_at(d - 1, j) & kCodeRowRight))
+                v -= al * ((i > 2 ? Yp[om2] : 0.0f) + (jm1 ? Yp[om2 - 1] : 0.0f));
+              if (i < N && (code_at(d + 1, j) & kCodeRowLeft))
+                v -= al * (Yp[o0] + (jm1 ? Yp[o0 - 1] : 0.0f));
+            } else {
+              if (jp1 && (code_at(d + 1, j + 1) & kCodeColUp))
+                v -= al * ((i > 1 ? Yp[o0 + 1] : 0.0f) + Yp[o0]);
+              if (jm1 && (code_at(d - 1, j - 1) & kCodeColDown))
+                v -= al * ((i > 1 ? Yp[om2 - 1] : 0.0f) + (jm2 ? Yp[om2 - 2] : 0.0f));
+            }
+          }
+        }
+        Yc[o0] = v;
+        if (plo) plo[o0] = v;
+        if (phi) phi[o0] = v;
+        const float sum = (s == 0) ? v : Ys[o0] + v;
+        Ys[o0] = sum;
+        if (s == K - 1) {
+          const size_t q = dg_at(i, j, P);
+          A.Ysum[q] = sum;
+          A.yK[q] = v;
+        }
+      }
+      o0 = o0 == 0 ? RW - W : o0 - W;
+      cluster.sync();
+    }
+    return;
+  }
+  for (int t = 0; t < nsteps; ++t) {
+    const int x = t - D0 + 2;
+    const int slo = x > 0 ? (x + 2) / 3 : 0;
+    const int shi = min(t / 3, K - 1);
+    int s = s0, c = c0;
+    for (int id = warp; id < ntask; id += nwarps) {
+      const int sc = s, cc = c;
+      s += ds;
+      c += dc;
+      if (s >= K) {
+        s -= K;
+        ++c;
+      }
+      if (sc < slo || sc > shi) continue;
+      const int d = D0 - t + 3 * sc;
+      const int j = jb + (cc << 5) + lane;
+      if (j > je || j < d - N || j > d - 1) continue;
+      const int i = d - j;
+      float* Yc = (sc & 1) ? Y1 : Y0;
+      float* Yp = (sc & 1) ? Y0 : Y1;
+      int r0 = tb + 3 * sc;
+      if (r0 >= R) r0 -= R;
+      const int rp1 = r0 + 1 == R ? 0 : r0 + 1;
+      const int rm1 = r0 == 0 ? R - 1 : r0 - 1;
+      const int rm2 = r0 >= 2 ? r0 - 2 : r0 + R - 2;
+      float v = al * ((i + 1 <= N ? yat(Yc, rp1, j) : 0.0f) + (j + 1 <= N ? yat(Yc, rp1, j + 1) : 0.0f));
+      if (sc == 0) {
+        v += Bs[(size_t)d * J + (j - jb)];
+      } else {
+        const uint8_t cd = code_at(d, j);
+        const bool written = (MODE == kRow)   ? (cd & kCodeRowMask) != 0
+                             : (MODE == kCol) ? (cd & kCodeColMask) != 0
+                                              : false;
+        if (!written)
+          v += al * ((i - 1 >= 1 ? yat(Yp, rm1, j) : 0.0f) + (j - 1 >= 1 ? yat(Yp, rm1, j - 1) : 0.0f));
+        if (MODE == kPassive) {
+          if (i == 1 || i == N || j == 1 || j == N) {
+            const int n = (j == 1 && colfl[i]) + (j == N && colfl[i]) + (i == 1 && rowfl[j]) +
+                          (i == N && rowfl[j]);
+            v += al * (float)n * yat(Yp, r0, j);
+          }
+        } else if (cd & kCodeWall) {
+          // (i-1, j) lies on diagonal d-1, (i+1, j) and (i, j+1) on d+1, (i, j-1) on d-1
+          if (MODE == kRow) {
+            if (i - 1 >= 1 && (code_at(d - 1, j) & kCodeRowRight))
+              v -= al * ((i - 2 >= 1 ? yat(Yp, rm2, j) : 0.0f) + (j - 1 >= 1 ? yat(Yp, rm2, j - 1) : 0.0f));
+            if (i + 1 <= N && (code_at(d + 1, j) & kCodeRowLeft))
+              v -= al * (yat(Yp, r0, j) + (j - 1 >= 1 ? yat(Yp, r0, j - 1) : 0.0f));
+          } else {
+            if (j + 1 <= N && (code_at(d + 1, j + 1) & kCodeColUp))
+              v -= al * ((i - 1 >= 1 ? yat(Yp, r0, j + 1) : 0.0f) + yat(Yp, r0, j));
+            if (j - 1 >= 1 && (code_at(d - 1, j - 1) & kCodeColDown))
+              v -= al * ((i - 1 >= 1 ? yat(Yp, rm2, j - 1) : 0.0f) + (j - 2 >= 1 ? yat(Yp, rm2, j - 2) : 0.0f));
+          }
+        }
+      }
+      const int lo = r0 * W + (j - jb + 2);
+      Yc[lo] = v;
+      // halo copies: my first position is the lower neighbour's je+1 (index
+      // J+2 there), my last two its upper neighbour's jb-1, jb-2 (1, 0)
+      const size_t boff = (sc & 1) ? (size_t)R * W : 0;
+      if (j == jb && Y0lo) Y0lo[boff + r0 * W + J + 2] = v;
+      if (j >= je - 1 && Y0hi) Y0hi[boff + r0 * W + (j - je + 1)] = v;
+      const float sum = (sc == 0) ? v : Ysm[lo] + v;
+      Ysm[lo] = sum;
+      if (sc == K - 1) {
+        const size_t q = dg_at(i, j, P);
+        A.Ysum[q] = sum;
+        A.yK[q] = v;
+      }
+    }
+    if (--tb < 0) tb += R;
+    cluster.sync();
   }
 }
 

@@ -386,7 +386,8 @@ int eq_hfluid_launch_count(const eq_hfluid* h, uint64_t* count);
  * (add_density at each cell, fluid.rs:120-124), then step() (fluid.rs:437-524).
  * The state at every `checkpoint_every`-th frame is kept on the device;
  * backward() recomputes each segment from its checkpoint with the fields
- * every advect reads saved, and undoes it frame by frame with the adjoint
+ * every advect reads saved (the last segment keeps them from the forward
+ * itself), and undoes it frame by frame with the adjoint
  * kernels (set_boundaries^T, reverse Gauss-Seidel sweeps, the transposed
  * bilinear scatter of advect, project^T), FP32 arithmetic. Gradients are
  * those of the reference's f32 step, including its discrete choices (advect's
@@ -417,9 +418,18 @@ int eq_grad_backward_device(eq_grad* g, const float* d_adj_final, float* d_grad_
                             float* d_grad_src);
 int eq_grad_frames(const eq_grad* g, int64_t* recorded);
 /* Caps where the transposed Gauss-Seidel wavefront keeps its band of live
- * diagonals: 2 = y and its running sum in shared memory (the default where
- * they fit), 1 = y only, 0 = global memory; -1 restores the default. */
+ * diagonals: 3 = spread over a cluster of 8 blocks (distributed shared
+ * memory; the default where each block keeps >= 16 positions), 2 = one block,
+ * y and its running sum in shared memory, 1 = y only, 0 = global memory;
+ * -1 restores the default. */
 int eq_grad_set_wavefront_storage(eq_grad* g, int max_store);
+/* The form the last transposed solve used (store as above) and its blocks. */
+int eq_grad_get_wavefront_storage(const eq_grad* g, int* store, int* cluster_blocks);
+/* With profiling on, every transposed Gauss-Seidel wavefront launch is
+ * bracketed by CUDA events; kernel_stats returns (and clears) their total
+ * device time and count. */
+int eq_grad_set_profiling(eq_grad* g, int enable);
+int eq_grad_kernel_stats(eq_grad* g, double* total_ms, uint64_t* launches);
 int eq_grad_launch_count(const eq_grad* g, uint64_t* count);
 /* The adjoint of one phase on host size x size arrays (in/out), at the bound
  * handle's mask and configs: set_boundaries, lin_solve (x_b -> adjoint before

@@ -82,6 +82,8 @@ def lib():
             "eqo_project_adj_f64": (None, [P, P, P, P, u32, i64, P]),
             "eqo_adjoint_problem_f32": (f32, [P, u32, f32, i64, f32, f32, i64, P, P, P, P, P,
                                               P, P]),
+            "eqo_fd_direction_f64": (f64, [P, u32, f64, i64, f64, f64, i64, P, P, P, P, P, i64,
+                                           ci, P]),
             "eqo_fill_obstacle": (None, [P, u32, i64, i64, i64, i64]),
             "eqo_rectangle_valid": (ci, [i64, i64, i64, i64, i64]),
         }
@@ -320,6 +322,27 @@ def adjoint_problem_f32(cells, size, dt, iters, diff, visc, init, src, target):
                                          ptrs, _ptr(src), _ptr(target), _ptr(gvx), _ptr(gvy),
                                          _ptr(gsrc), ctypes.byref(sig))
     return loss, sig.value, gvx, gvy, gsrc
+
+
+def fd_direction_f64(cells, size, dt, iters, diff, visc, init, src, target, direction, hs,
+                     frozen=False):
+    """Losses of the f64 forward at +h and -h along `direction` for each h in
+    hs: array (len(hs), 2). frozen: the perturbed runs replay the unperturbed
+    run's advect choices (cells, clamps, row breaks), so the central
+    difference is the derivative of the piece the adjoint differentiates."""
+    n = size * size
+    init = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) for a in init]
+    src = np.ascontiguousarray(src, dtype=np.float64).reshape(-1)
+    target = np.ascontiguousarray(target, dtype=np.float64).reshape(-1)
+    direction = np.ascontiguousarray(direction, dtype=np.float64).reshape(-1)
+    assert direction.size == 2 * n + src.size
+    hs = np.ascontiguousarray(hs, dtype=np.float64)
+    out = np.zeros(2 * hs.size)
+    ptrs = (ctypes.c_void_p * 6)(*[_ptr(a) for a in init])
+    lib().eqo_fd_direction_f64(_ptr(cells), size, dt, iters, diff, visc, src.size // n, ptrs,
+                               _ptr(src), _ptr(target), _ptr(direction), _ptr(hs), hs.size,
+                               int(bool(frozen)), _ptr(out))
+    return out.reshape(-1, 2)
 
 
 def set_boundaries_adj_f64(mode, xb, size, cells):

@@ -326,3 +326,117 @@ inline T adjoint_problem(const uint8_t* cells, uint32_t size, T dt, int64_t K, T
 }
 
 }  // namespace eqo
+
+namespace eqo {
+
+// ---- frozen-path forward: finite differences on the adjoint's smooth piece --
+// The forward is piecewise smooth: each advect's cell choice floor(x),
+// its clamps and its row break are discrete. The adjoint differentiates the
+// piece the recorded run is on; a central difference matches it only if the
+// +h and -h runs stay on that piece. A frozen-path run replays the recorded
+// choices (cell, clamp side, break column) with the perturbed values, which
+// is that piece's polynomial extension: its central difference is what the
+// adjoint must equal, to O(h^2), whatever h.
+template <class T>
+struct AdvectPath {
+  std::vector<int64_t> brk;    // per row j: the break column (S - 1: none)
+  std::vector<T> fi0, fj0;     // per cell: floor of the clamped backtrace
+  std::vector<uint8_t> clamp;  // per cell: 1 x < 0.5, 2 x > S-1, 4 y < 0.5, 8 y > S-1
+};
+
+template <class T>
+inline void advect_path(Mode m, T* d, const T* d0, const T* u, const T* v, uint32_t size,
+                        T delta_t, const uint8_t* cells, AdvectPath<T>& P, bool record) {
+  const int64_t S = size;
+  const T dt0 = delta_t * (T)(size - 2);
+  const T sf = (T)size, hi = sf - (T)1.0;
+  if (record) {
+    P.brk.assign(S, S - 1);
+    P.fi0.assign((size_t)S * S, (T)0);
+    P.fj0.assign((size_t)S * S, (T)0);
+    P.clamp.assign((size_t)S * S, 0);
+  }
+  for (int64_t j = 1; j < S - 1; ++j) {
+    for (int64_t i = 1; i < S - 1; ++i) {
+      const size_t q = idx(i, j, S);
+      const T xr = (T)i - dt0 * u[q], yr = (T)j - dt0 * v[q];
+      T x, y, fi0, fj0;
+      if (record) {
+        P.clamp[q] = (uint8_t)((xr < (T)0.5) | ((xr > hi) << 1) | ((yr < (T)0.5) << 2) |
+                               ((yr > hi) << 3));
+        x = rust_clamp<T>(xr, (T)0.5, hi);
+        y = rust_clamp<T>(yr, (T)0.5, hi);
+        fi0 = std::floor(x);
+        fj0 = std::floor(y);
+        P.fi0[q] = fi0;
+        P.fj0[q] = fj0;
+        if (fi0 + (T)1.0 >= sf || fj0 + (T)1.0 >= sf) {
+          P.brk[j] = i;
+          d[q] = d[idx(i - 1, j, S)];
+          break;
+        }
+      } else {
+        if (i == P.brk[j]) {
+          d[q] = d[idx(i - 1, j, S)];
+          break;
+        }
+        const uint8_t c = P.clamp[q];
+        x = (c & 1) ? (T)0.5 : (c & 2) ? hi : xr;
+        y = (c & 4) ? (T)0.5 : (c & 8) ? hi : yr;
+        fi0 = P.fi0[q];
+        fj0 = P.fj0[q];
+      }
+      const T s1 = x - fi0, s0 = (T)1.0 - s1, t1 = y - fj0, t0 = (T)1.0 - t1;
+      const int64_t i0 = rust_as_u32<T>(fi0), i1 = rust_as_u32<T>(fi0 + (T)1.0);
+      const int64_t j0 = rust_as_u32<T>(fj0), j1 = rust_as_u32<T>(fj0 + (T)1.0);
+      d[q] = s0 * (t0 * d0[idx(i0, j0, S)] + t1 * d0[idx(i0, j1, S)]) +
+             s1 * (t0 * d0[idx(i1, j0, S)] + t1 * d0[idx(i1, j1, S)]);
+    }
+  }
+  set_boundaries<T>(m, d, size, cells);
+}
+
+// adjoint_problem's forward with every advect recording (record = true) or
+// replaying its discrete choices; returns the loss.
+template <class T>
+inline T forward_path(const uint8_t* cells, uint32_t size, T dt, int64_t K, T diff, T visc,
+                      int64_t nframes, const T* const init[6], const T* src, const T* target,
+                      std::vector<AdvectPath<T>>& paths, bool record) {
+  const int64_t S = size;
+  const size_t n = (size_t)S * S;
+  std::vector<T> f[6];
+  for (int q = 0; q < 6; ++q) f[q].assign(init[q], init[q] + n);
+  if (record) paths.assign((size_t)nframes * 3, AdvectPath<T>());
+  T* sc = f[Scratch].data();
+  T* de = f[Density].data();
+  T* vx = f[VelX].data();
+  T* vy = f[VelY].data();
+  T* vx0 = f[VelX0].data();
+  T* vy0 = f[VelY0].data();
+  for (int64_t fr = 0; fr < nframes; ++fr) {
+    const T* s = src + (size_t)fr * n;
+    for (size_t q = 0; q < n; ++q) {
+      de[q] += s[q];
+      sc[q] += s[q];
+    }
+    AdvectPath<T>* P = &paths[(size_t)fr * 3];
+    diffuse<T>(AdjustRow, vx0, vx, visc, size, dt, K, cells);
+    diffuse<T>(AdjustColumn, vy0, vy, visc, size, dt, K, cells);
+    project<T>(vx0, vy0, vx, vy, size, K, cells);
+    advect_path<T>(AdjustRow, vx, vx0, vx0, vy0, size, dt, cells, P[0], record);
+    advect_path<T>(AdjustColumn, vy, vy0, vx0, vy0, size, dt, cells, P[1], record);
+    project<T>(vx, vy, vx0, vy0, size, K, cells);
+    diffuse<T>(Passive, sc, de, diff, size, dt, K, cells);
+    advect_path<T>(Passive, de, sc, vx, vy, size, dt, cells, P[2], record);
+    std::memcpy(sc, de, sizeof(T) * n);
+  }
+  T loss = 0;
+  for (int64_t j = 1; j < S - 1; ++j)
+    for (int64_t i = 1; i < S - 1; ++i) {
+      const T e = de[idx(i, j, S)] - target[idx(i, j, S)];
+      loss += (T)0.5 * e * e;
+    }
+  return loss;
+}
+
+}  // namespace eqo

@@ -177,6 +177,42 @@ float eqo_adjoint_problem_f32(const uint8_t* cells, uint32_t size, float dt, int
                                 g_vx, g_vy, g_src, sig);
 }
 
+// Central differences along one direction (over the initial vx, vy and every
+// source field: 2n + nframes*n values) for each of nh step sizes: out[2k] the
+// loss at +h[k], out[2k+1] at -h[k]. frozen != 0: the perturbed runs replay
+// the unperturbed run's discrete choices (returns its loss); else plain runs
+// (returns 0).
+double eqo_fd_direction_f64(const uint8_t* cells, uint32_t size, double dt, int64_t iters,
+                            double diff, double visc, int64_t nframes,
+                            const double* const init[6], const double* src, const double* target,
+                            const double* dir, const double* h, int64_t nh, int frozen,
+                            double* out) {
+  const size_t n = (size_t)size * size, ns = (size_t)nframes * n;
+  std::vector<AdvectPath<double>> paths;
+  double base = 0.0;
+  if (frozen)
+    base = forward_path<double>(cells, size, dt, iters, diff, visc, nframes, init, src, target,
+                                paths, true);
+  std::vector<double> f[6], s(ns);
+  for (int64_t k = 0; k < 2 * nh; ++k) {
+    const double e = (k & 1) ? -h[k / 2] : h[k / 2];
+    for (int q = 0; q < 6; ++q) f[q].assign(init[q], init[q] + n);
+    for (size_t c = 0; c < n; ++c) {
+      f[VelX][c] += e * dir[c];
+      f[VelY][c] += e * dir[n + c];
+    }
+    for (size_t c = 0; c < ns; ++c) s[c] = src[c] + e * dir[2 * n + c];
+    const double* p[6] = {f[0].data(), f[1].data(), f[2].data(), f[3].data(), f[4].data(),
+                          f[5].data()};
+    out[k] = frozen ? forward_path<double>(cells, size, dt, iters, diff, visc, nframes, p,
+                                           s.data(), target, paths, false)
+                    : adjoint_problem<double>(cells, size, dt, iters, diff, visc, nframes, p,
+                                              s.data(), target, nullptr, nullptr, nullptr,
+                                              nullptr);
+  }
+  return base;
+}
+
 // ---- mask / obstacles -----------------------------------------------------
 void eqo_fill_obstacle(uint8_t* cells, uint32_t size, int64_t x0, int64_t y0, int64_t x1,
                        int64_t y1) {

@@ -58,13 +58,14 @@ def test_set_boundaries_adj(eqlib, scene, mode):
     f.close()
 
 
-@pytest.mark.parametrize("store", [2, 1, 0])
+@pytest.mark.parametrize("store", [3, 2, 1, 0])
 @pytest.mark.parametrize("size,K", [(20, 1), (20, 2), (41, 3), (41, 20), (66, 20), (130, 7),
-                                    (258, 20)])
+                                    (258, 20), (514, 20), (300, 33)])
 @pytest.mark.parametrize("mode", [ROW, COL, PAS])
 def test_lin_solve_adj(eqlib, size, K, mode, store):
-    """store: where the wavefront keeps its band (2 = shared memory for y and
-    its sum, 1 = y only, 0 = global memory)."""
+    """store: where the wavefront keeps its band (3 = a cluster of 8 blocks
+    where the size allows it, 2 = one block, shared memory for y and its sum,
+    1 = y only, 0 = global memory)."""
     rects = SCENES["edges"] if size >= 41 else [(3, 4, 7, 9)]
     f, of = make(size, K=K, rects=rects)
     g = Recorder(f, 1)
@@ -228,6 +229,31 @@ def test_backward_fd_random_directions(eqlib):
         fd = (lp - lm) / (2 * h)
         errs.append(abs(fd - pred) / max(abs(fd), 1e-12))
     assert len(errs) >= 4 and np.median(errs) < 1e-3, errs
+
+
+def test_backward_frozen_path_fd(eqlib):
+    """The GPU gradient against central differences (h = 1e-3, f64) whose
+    perturbed runs replay the unperturbed run's advect choices: the
+    derivative of the smooth piece the recording is on. Errors are scaled by
+    the gradient's RMS directional derivative |g| / sqrt(dim)."""
+    size, frames = 41, 5
+    f, of, init, src, target = problem(size, frames, [(9, 9, 14, 13), (25, 2, 29, 12)], seed=4)
+    g = Recorder(f, frames, 2)
+    g.forward(src)
+    g.l2_loss(target)
+    gi, gs = g.backward()
+    gv = np.concatenate([gi[2], gi[3], gs.reshape(-1)]).astype(np.float64)
+    rms = np.linalg.norm(gv) / np.sqrt(gv.size)
+    rng = np.random.default_rng(21)
+    for _ in range(6):
+        d = rng.standard_normal(gv.size)
+        d /= np.linalg.norm(d)
+        (lp, lm), = oracle.fd_direction_f64(of.cells, size, 0.1, 20, 1e-4, 1e-4, init, src,
+                                            target, d, [1e-3], frozen=True)
+        err = abs((lp - lm) / 2e-3 - gv @ d) / rms
+        assert err < 1e-3, err
+    g.close()
+    f.close()
 
 
 def test_grad_rejects_bad_use(eqlib):
