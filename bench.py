@@ -45,6 +45,10 @@ N = SIZE - 2
 BYTES_PER_CELL_LINSOLVE = 13  # read x0, read x, write x (f32) + mask byte, per S^2 cell
 BYTES_PER_CELL_FRAME = 164    # fused-phase compulsory traffic per S^2 cell per frame
 BYTES_PER_CELL_FRAME_HALF = 86  # the same with FP16 / BF16 fields: (164 - 8) / 2 + 8
+BYTES_PER_CELL_FRAME_F16_SCALARS = 150  # density and scratch FP16, velocities FP32
+BYTES_BY_STORAGE = {"f32": BYTES_PER_CELL_FRAME, "f16": BYTES_PER_CELL_FRAME_HALF,
+                    "bf16": BYTES_PER_CELL_FRAME_HALF,
+                    "f16_scalars": BYTES_PER_CELL_FRAME_F16_SCALARS}
 
 
 def baseline_metric():
@@ -153,11 +157,9 @@ def run_batched_form(local_rank: int, frames: int, plain_sample: int = 12, stora
                       "autotune_ms_per_frame": tune_ms},
            "gpu_launches": int(launches),
            "roofline": {"bound": "hbm",
-                        "achieved": (BYTES_PER_CELL_FRAME if storage == "f32" else
-                                     BYTES_PER_CELL_FRAME_HALF) * cells / (ms / 1e3) / 1e9,
+                        "achieved": BYTES_BY_STORAGE[storage] * cells / (ms / 1e3) / 1e9,
                         "unit": "GB/s",
-                        "bytes_per_cell_frame": (BYTES_PER_CELL_FRAME if storage == "f32"
-                                                 else BYTES_PER_CELL_FRAME_HALF)}}
+                        "bytes_per_cell_frame": BYTES_BY_STORAGE[storage]}}
     if storage == "f32":
         # end to end: one frame through the C ABI, then every scene's three pub
         # fields read back to host memory
@@ -514,6 +516,25 @@ def run_diff_form(local_rank: int, reps: int = 2, fd_dirs: int = 32, size: int =
     _lib.check(L.eq_grad_set_profiling(g.handle, 0))
     gi = d_gi.view(6, n).cpu().numpy()
     gsrc = d_gs.view(frames, n).cpu().numpy()
+    # variant: one segment (the forward keeps the whole tape, no recompute)
+    gf = Recorder(f, frames, frames)
+    full_ms = []
+    for rep in range(reps + 1):
+        reset()
+        torch.cuda.synchronize()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        e[0].record(stream)
+        _lib.check(L.eq_grad_forward_device(gf.handle, frames, d_src.data_ptr()))
+        gf.nframes = frames
+        gf.l2_loss(target)
+        _lib.check(L.eq_grad_backward_device(gf.handle, None, d_gi.data_ptr(), d_gs.data_ptr()))
+        e[1].record(stream)
+        torch.cuda.synchronize()
+        if rep > 0:
+            full_ms.append(e[0].elapsed_time(e[1]))
+    full_diff = float(np.linalg.norm(d_gs.view(frames, n).cpu().numpy() - gsrc) /
+                      np.linalg.norm(gsrc))
+    gf.close()
     # end to end through the C ABI with host buffers
     e2e_ms = []
     for rep in range(reps):
@@ -544,7 +565,14 @@ def run_diff_form(local_rank: int, reps: int = 2, fd_dirs: int = 32, size: int =
                    "unit": "cell-steps/s", "ms_per_gradient": statistics.mean(e2e_ms),
                    "h2d_bytes_per_gradient": frames * n * 4 + n * 4,
                    "d2h_bytes_per_gradient": (6 + frames) * n * 4 + 8},
-           "loss": loss, "rerun_rel_diff": rerun}
+           "loss": loss, "rerun_rel_diff": rerun,
+           "variant_full_tape": {
+               "what": "checkpoint_every = frames: the forward keeps every frame's tape "
+                       f"({frames * 5 * size * ((size + 31) // 32 * 32) * 4 / 1e6:.0f} MB), "
+                       "backward recomputes nothing",
+               "value": cells_steps / (statistics.mean(full_ms) / 1e3),
+               "ms_per_gradient": statistics.mean(full_ms),
+               "g_src_rel_diff_to_checkpointed": full_diff}}
     avg_gs = gs_ms.value / max(gs_n.value, 1)
     store, blocks = g.wavefront_storage()
     # the adjoint wavefront: per cell and sweep it reads 2 + 2 (+ sum) values
@@ -940,6 +968,8 @@ def run_ours(args):
         form("batched", lambda: run_batched_form(local_rank, args.batch_frames))
         form("batched_f16", lambda: run_batched_form(local_rank, args.batch_frames, 0, "f16",
                                                      autotune=False, err_sample=24))
+        form("batched_f16_scalars", lambda: run_batched_form(
+            local_rank, args.batch_frames, 0, "f16_scalars", autotune=False, err_sample=24))
         form("precision", lambda: run_precision_form(local_rank, args.precision_frames))
         form("differentiation", lambda: run_diff_form(local_rank, fd_dirs=args.fd_dirs))
         for k in ("f16", "bf16"):

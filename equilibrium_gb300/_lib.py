@@ -16,7 +16,7 @@ HEADER = os.path.join(ROOT, "include", "eqfluid.h")
 EQ_OK, EQ_ERR_ARG, EQ_ERR_CUDA, EQ_ERR_TIMEOUT, EQ_ERR_OOM, EQ_ERR_STATE = range(6)
 FIELD_SCRATCH, FIELD_DENSITY, FIELD_VX, FIELD_VY, FIELD_VX0, FIELD_VY0 = range(6)
 MODE_ADJUST_ROW, MODE_ADJUST_COLUMN, MODE_PASSIVE = range(3)
-STORE_F16, STORE_BF16 = 1, 2
+STORE_F16, STORE_BF16, STORE_F16_SCALARS = 1, 2, 3
 
 
 class EqError(RuntimeError):

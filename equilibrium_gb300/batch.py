@@ -39,7 +39,8 @@ class Batch:
             arr[q].diffusion = float(sc.diffusion)
             arr[q].viscousity = float(sc.viscousity)
         h = ctypes.c_void_p()
-        st = {"f32": 0, "f16": _lib.STORE_F16, "bf16": _lib.STORE_BF16}[storage]
+        st = {"f32": 0, "f16": _lib.STORE_F16, "bf16": _lib.STORE_BF16,
+              "f16_scalars": _lib.STORE_F16_SCALARS}[storage]
         check(L.eq_batch_new_storage(n, arr, st, device, ctypes.byref(h)))
         self.storage = storage
         self.handle = h

@@ -16,8 +16,9 @@
 
 struct eq_batch {
   int device = 0;
-  int storage = 0;   // 0 FP32 (bit-exact), EQ_STORE_F16, EQ_STORE_BF16
-  size_t esize = 4;  // bytes per stored cell value
+  int storage = 0;   // 0 FP32 (bit-exact), EQ_STORE_F16, EQ_STORE_BF16, EQ_STORE_F16_SCALARS
+  size_t esize = 4;  // bytes per stored cell value (velocity fields)
+  size_t esize2 = 4; // bytes per stored cell value of density and scratch
   cudaStream_t stream = nullptr;
   int64_t n = 0;
   std::vector<eqk::BScene> desc;
@@ -31,6 +32,7 @@ struct eq_batch {
   int smax = 0;
 
   void* arena = nullptr;
+  void* arena2 = nullptr;  // density and scratch when stored apart (== arena otherwise)
   size_t arena_elems = 0;
   uint8_t* marena = nullptr;
   size_t marena_bytes = 0;
@@ -70,6 +72,7 @@ void batch_free(eq_batch* b) {
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
   batch_drop_graph(b);
+  if (b->arena2 && b->arena2 != b->arena) cudaFree(b->arena2);
   cudaFree(b->arena);
   cudaFree(b->marena);
   cudaFree(b->d_desc);
@@ -84,14 +87,16 @@ void batch_free(eq_batch* b) {
 
 // Fluid::new state (fluid.rs:93-110 then init(), fluid.rs:602-606) of every
 // scene: zeros, vx = vy = 0 + 1, density = scratch = 0 + 0 (+ 0.9 on the
-// block [size/2-10, size/2+10]^2). The arena was zeroed before.
-template <class ST>
-__global__ void k_batch_init(ST* arena, const eqk::BScene* scenes, int64_t n) {
+// block [size/2-10, size/2+10]^2). The arenas were zeroed before; density and
+// scratch live in arena2 (== arena unless stored apart).
+template <class ST, class STS>
+__global__ void k_batch_init(ST* arena, STS* arena2, const eqk::BScene* scenes, int64_t n) {
   for (int64_t s = blockIdx.x; s < n; s += gridDim.x) {
     const eqk::BScene sc = scenes[s];
     const int S = sc.S, P = sc.P;
     const int lo = S / 2 - 10, hi = S / 2 + 10;
     ST* f = arena + sc.foff;
+    STS* g = arena2 + sc.foff;
     const size_t cells = (size_t)S * S;
     // idx! clamps the block's coordinates into the grid (fluid.rs:31-35), so for
     // size 20 the last column / row receives the 0.9 twice (the corner 4x).
@@ -106,8 +111,8 @@ __global__ void k_batch_init(ST* arena, const eqk::BScene* scenes, int64_t n) {
       for (int r = mult(i) * mult(j); r > 0; --r) dens = eqk::fadd(dens, 0.9f);
       const float vel = eqk::fadd(0.0f, 1.0f);
       const size_t a = eqk::dg_at(i, j, P);
-      eqk::hs(f, a, dens);
-      eqk::hs(f, sc.fstride + a, dens);
+      eqk::hs(g, a, dens);
+      eqk::hs(g, sc.fstride + a, dens);
       eqk::hs(f, 2 * sc.fstride + a, vel);
       eqk::hs(f, 3 * sc.fstride + a, vel);
     }
@@ -215,6 +220,8 @@ int batch_launch_shape(eq_batch* b, BLaunch* L) {
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem));
   EQ_CUDA(cudaFuncSetAttribute(eqk::k_batch_run<__nv_bfloat16>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem));
+  EQ_CUDA(cudaFuncSetAttribute(eqk::k_batch_run<float, __half>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem));
   return EQ_OK;
 }
 
@@ -262,6 +269,7 @@ eqk::BatchArgs batch_args(eq_batch* b, const BLaunch& L, unsigned* queue) {
   (void)L;
   eqk::BatchArgs A;
   A.arena = b->arena;
+  A.arena2 = b->arena2;
   A.marena = b->marena;
   A.scenes = b->d_desc;
   A.order = b->d_order;
@@ -299,7 +307,9 @@ int batch_ensure_queue(eq_batch* b, int64_t n) {
 
 void batch_launch_run(eq_batch* b, const BLaunch& L, const eqk::BatchArgs& A,
                       const eqk::BOpList& ops) {
-  if (b->storage == EQ_STORE_F16)
+  if (b->storage == EQ_STORE_F16_SCALARS)
+    eqk::k_batch_run<float, __half><<<L.blocks, L.threads, L.smem, b->stream>>>(A, ops);
+  else if (b->storage == EQ_STORE_F16)
     eqk::k_batch_run<__half><<<L.blocks, L.threads, L.smem, b->stream>>>(A, ops);
   else if (b->storage == EQ_STORE_BF16)
     eqk::k_batch_run<__nv_bfloat16><<<L.blocks, L.threads, L.smem, b->stream>>>(A, ops);
@@ -369,8 +379,10 @@ int eq_batch_new(int64_t nscenes, const eq_scene_desc* scenes, int device, eq_ba
 int eq_batch_new_storage(int64_t nscenes, const eq_scene_desc* scenes, int storage, int device,
                          eq_batch** out) {
   if (!out || !scenes) return fail(EQ_ERR_ARG, "null argument");
-  if (storage != 0 && storage != EQ_STORE_F16 && storage != EQ_STORE_BF16)
-    return fail(EQ_ERR_ARG, "storage must be 0 (FP32), EQ_STORE_F16 or EQ_STORE_BF16");
+  if (storage != 0 && storage != EQ_STORE_F16 && storage != EQ_STORE_BF16 &&
+      storage != EQ_STORE_F16_SCALARS)
+    return fail(EQ_ERR_ARG,
+                "storage must be 0 (FP32), EQ_STORE_F16, EQ_STORE_BF16 or EQ_STORE_F16_SCALARS");
   *out = nullptr;
   if (nscenes <= 0) return fail(EQ_ERR_ARG, "nscenes must be > 0");
   if (nscenes > (int64_t)1 << 30) return fail(EQ_ERR_ARG, "too many scenes");
@@ -386,7 +398,8 @@ int eq_batch_new_storage(int64_t nscenes, const eq_scene_desc* scenes, int stora
   b->device = device;
   b->n = nscenes;
   b->storage = storage;
-  b->esize = storage == 0 ? 4 : 2;
+  b->esize = (storage == 0 || storage == EQ_STORE_F16_SCALARS) ? 4 : 2;
+  b->esize2 = storage == 0 ? 4 : 2;
   auto bail = [&](int code, const char* what) {
     batch_free(b);
     return fail(code, what);
@@ -434,6 +447,15 @@ int eq_batch_new_storage(int64_t nscenes, const eq_scene_desc* scenes, int stora
     return bail(EQ_ERR_OOM, "cudaMalloc (batch fields)");
   if (cudaMemsetAsync(b->arena, 0, foff * b->esize, b->stream) != cudaSuccess)
     return bail(EQ_ERR_CUDA, "cudaMemsetAsync (batch fields)");
+  b->arena2 = b->arena;
+  if (storage == EQ_STORE_F16_SCALARS) {  // density and scratch apart, same offsets
+    if (cudaMalloc(&b->arena2, foff * b->esize2) != cudaSuccess) {
+      b->arena2 = nullptr;
+      return bail(EQ_ERR_OOM, "cudaMalloc (batch scalar fields)");
+    }
+    if (cudaMemsetAsync(b->arena2, 0, foff * b->esize2, b->stream) != cudaSuccess)
+      return bail(EQ_ERR_CUDA, "cudaMemsetAsync (batch scalar fields)");
+  }
   if (cudaMalloc(&b->marena, moff) != cudaSuccess ||
       cudaMalloc(&b->d_desc, nscenes * sizeof(eqk::BScene)) != cudaSuccess ||
       cudaMalloc(&b->d_order, nscenes * sizeof(int)) != cudaSuccess)
@@ -461,11 +483,13 @@ int eq_batch_new_storage(int64_t nscenes, const eq_scene_desc* scenes, int stora
   {
     const int blocks = (int)std::min<int64_t>(nscenes, 4096);
     if (storage == EQ_STORE_F16)
-      k_batch_init<__half><<<blocks, 256, 0, b->stream>>>(static_cast<__half*>(b->arena), b->d_desc, nscenes);
+      k_batch_init<<<blocks, 256, 0, b->stream>>>(static_cast<__half*>(b->arena), static_cast<__half*>(b->arena2), b->d_desc, nscenes);
     else if (storage == EQ_STORE_BF16)
-      k_batch_init<__nv_bfloat16><<<blocks, 256, 0, b->stream>>>(static_cast<__nv_bfloat16*>(b->arena), b->d_desc, nscenes);
+      k_batch_init<<<blocks, 256, 0, b->stream>>>(static_cast<__nv_bfloat16*>(b->arena), static_cast<__nv_bfloat16*>(b->arena2), b->d_desc, nscenes);
+    else if (storage == EQ_STORE_F16_SCALARS)
+      k_batch_init<<<blocks, 256, 0, b->stream>>>(static_cast<float*>(b->arena), static_cast<__half*>(b->arena2), b->d_desc, nscenes);
     else
-      k_batch_init<float><<<blocks, 256, 0, b->stream>>>(static_cast<float*>(b->arena), b->d_desc, nscenes);
+      k_batch_init<<<blocks, 256, 0, b->stream>>>(static_cast<float*>(b->arena), static_cast<float*>(b->arena2), b->d_desc, nscenes);
     if (cudaGetLastError() != cudaSuccess) return bail(EQ_ERR_CUDA, "k_batch_init");
     b->launches++;
   }
@@ -549,19 +573,24 @@ static int batch_field_copy(eq_batch* b, int64_t scene, int field, void* host, u
   const int S = d.S, P = d.P;
   if (n != (uint64_t)S * S) return fail(EQ_ERR_ARG, "element count must be size*size");
   if (!host) return fail(EQ_ERR_ARG, "null host buffer");
-  uint8_t* dev = static_cast<uint8_t*>(b->arena) + (d.foff + (size_t)field * d.fstride) * b->esize;
-  std::vector<uint8_t> diag(d.fstride * b->esize, 0);
+  // density (1) and scratch (0) live in arena2 in their own format
+  const bool scalar = field < 2;
+  const size_t es = scalar ? b->esize2 : b->esize;
+  const int fmt = es == 4 ? 0 : (b->storage == EQ_STORE_BF16 ? EQ_STORE_BF16 : EQ_STORE_F16);
+  uint8_t* dev = static_cast<uint8_t*>(scalar ? b->arena2 : b->arena) +
+                 (d.foff + (size_t)field * d.fstride) * es;
+  std::vector<uint8_t> diag(d.fstride * es, 0);
   float* dense = static_cast<float*>(host);
   auto get = [&](size_t q) -> float {
-    if (b->storage == EQ_STORE_F16) return __half2float(reinterpret_cast<const __half*>(diag.data())[q]);
-    if (b->storage == EQ_STORE_BF16)
+    if (fmt == EQ_STORE_F16) return __half2float(reinterpret_cast<const __half*>(diag.data())[q]);
+    if (fmt == EQ_STORE_BF16)
       return __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(diag.data())[q]);
     return reinterpret_cast<const float*>(diag.data())[q];
   };
   auto put = [&](size_t q, float v) {
-    if (b->storage == EQ_STORE_F16)
+    if (fmt == EQ_STORE_F16)
       reinterpret_cast<__half*>(diag.data())[q] = __float2half_rn(v);
-    else if (b->storage == EQ_STORE_BF16)
+    else if (fmt == EQ_STORE_BF16)
       reinterpret_cast<__nv_bfloat16*>(diag.data())[q] = __float2bfloat16_rn(v);
     else
       reinterpret_cast<float*>(diag.data())[q] = v;
@@ -773,10 +802,19 @@ int eq_batch_autotune(eq_batch* b, int trial_frames, double* ms_out, int cap, in
     }
   }
   void* snap = nullptr;
+  void* snap2 = nullptr;  // density and scratch when stored apart
+  const bool apart = b->arena2 != b->arena;
   if (cudaMalloc(&snap, b->arena_elems * b->esize) != cudaSuccess)
     return fail(EQ_ERR_OOM, "cudaMalloc (autotune snapshot)");
+  if (apart && cudaMalloc(&snap2, b->arena_elems * b->esize2) != cudaSuccess) {
+    cudaFree(snap);
+    return fail(EQ_ERR_OOM, "cudaMalloc (autotune snapshot)");
+  }
   EQ_CUDA(cudaMemcpyAsync(snap, b->arena, b->arena_elems * b->esize, cudaMemcpyDeviceToDevice,
                           b->stream));
+  if (apart)
+    EQ_CUDA(cudaMemcpyAsync(snap2, b->arena2, b->arena_elems * b->esize2,
+                            cudaMemcpyDeviceToDevice, b->stream));
   const int onw = b->nwmax, obps = b->bps;
   int best = -1;
   double best_ms = 0.0;
@@ -799,6 +837,9 @@ int eq_batch_autotune(eq_batch* b, int trial_frames, double* ms_out, int cap, in
       ms = (double)t / trial_frames;
       EQ_CUDA(cudaMemcpyAsync(b->arena, snap, b->arena_elems * b->esize,
                               cudaMemcpyDeviceToDevice, b->stream));
+      if (apart)
+        EQ_CUDA(cudaMemcpyAsync(b->arena2, snap2, b->arena_elems * b->esize2,
+                                cudaMemcpyDeviceToDevice, b->stream));
       if (best < 0 || ms < best_ms) {
         best = (int)q;
         best_ms = ms;
@@ -810,6 +851,7 @@ int eq_batch_autotune(eq_batch* b, int trial_frames, double* ms_out, int cap, in
   cudaEventDestroy(e1);
   cudaStreamSynchronize(b->stream);
   cudaFree(snap);
+  cudaFree(snap2);
   if (rc) return rc;
   if (ncand) *ncand = (int)cand.size();
   if (best < 0) {

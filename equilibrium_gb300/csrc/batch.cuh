@@ -8,6 +8,8 @@
 // barriers between phases. No inter-block communication exists at all, so
 // the result of every scene is bit-identical to the plain form's.
 #pragma once
+#include <type_traits>
+
 #include "common.cuh"
 #include "kernels.cuh"
 #include "store.cuh"
@@ -28,7 +30,9 @@ struct BScene {
 };
 
 struct BatchArgs {
-  void* arena;  // fields in the storage format (FP32, FP16 or BF16)
+  void* arena;   // fields in the storage format (FP32, FP16 or BF16)
+  void* arena2;  // density and scratch (fields 0, 1) when their storage differs
+                 // from the velocity fields' (same offsets); else == arena
   const uint8_t* marena;
   const BScene* scenes;
   const int* order;  // queue position -> scene index
@@ -62,9 +66,9 @@ __device__ __forceinline__ void dg_for_cells(int ilo, int ihi, int jlo, int jhi,
   }
 }
 
-template <class ST>
-__device__ __forceinline__ void blk_sources(const BatchArgs& A, const BScene& sc, ST* de,
-                                            ST* scr, ST* vx, ST* vy) {
+template <class STS, class ST>
+__device__ __forceinline__ void blk_sources(const BatchArgs& A, const BScene& sc, STS* de,
+                                            STS* scr, ST* vx, ST* vy) {
   if (threadIdx.x != 0 || sc.nsrc <= 0) return;
   const int S = sc.S, P = sc.P;
   for (int s = sc.src_off; s < sc.src_off + sc.nsrc; ++s) {  // array order, like k_sources
@@ -125,6 +129,19 @@ __device__ void blk_bnd(ST* __restrict__ x, const uint8_t* __restrict__ code,
 }
 
 // project's divergence + zero pressure (fluid.rs:339-352).
+// set_boundaries with the mode known at run time.
+template <class ST>
+__device__ __forceinline__ void blk_bnd_mode(int mode, ST* x, const uint8_t* code,
+                                             const uint8_t* rowfl, const uint8_t* colfl, int S,
+                                             int P) {
+  if (mode == kRow)
+    blk_bnd<kRow>(x, code, rowfl, colfl, S, P);
+  else if (mode == kCol)
+    blk_bnd<kCol>(x, code, rowfl, colfl, S, P);
+  else
+    blk_bnd<kPassive>(x, code, rowfl, colfl, S, P);
+}
+
 template <class ST>
 __device__ void blk_divergence(const ST* __restrict__ vx, const ST* __restrict__ vy,
                                ST* __restrict__ p, ST* __restrict__ div, int S, int P) {
@@ -226,8 +243,8 @@ __device__ void blk_advect_breaks(const ST* __restrict__ u, const ST* __restrict
 // advect's second pass (fluid.rs:378-432): the cells before the row's break
 // by bilinear interpolation, the break cell with its left neighbour's new
 // value (the old ghost when it is column 1); the cells after it untouched.
-template <class ST>
-__device__ void blk_advect_write(ST* __restrict__ d, const ST* __restrict__ d0,
+template <class SD, class ST>
+__device__ void blk_advect_write(SD* __restrict__ d, const SD* __restrict__ d0,
                                  const ST* __restrict__ u, const ST* __restrict__ v,
                                  int S, int P, float dt0, const int* brk) {
   const int N = S - 2;
@@ -323,12 +340,22 @@ template <class ST>
 __device__ __forceinline__ ST* bfield(const BatchArgs& A, const BScene& sc, int f) {
   return static_cast<ST*>(A.arena) + sc.foff + (size_t)f * sc.fstride;
 }
+// density (1) and scratch (0) in their own storage format (arena2 only when
+// it differs from the velocity fields')
+template <class STS, class ST>
+__device__ __forceinline__ STS* bscalar(const BatchArgs& A, const BScene& sc, int f) {
+  if constexpr (std::is_same<ST, STS>::value) return bfield<ST>(A, sc, f);
+  return static_cast<STS*>(A.arena2) + sc.foff + (size_t)f * sc.fstride;
+}
 
-// One operation on the scene in shared memory.
-template <class ST>
+// One operation on the scene in shared memory. ST: the velocity fields'
+// storage; STS: density and scratch's (fields 0 and 1; the op list never
+// mixes the two kinds in one solve, copy or advected pair).
+template <class ST, class STS>
 __device__ __forceinline__ void blk_op(const BatchArgs& A, const BScene* ssc, const BOp& op,
                                        const WBufs& Bf, int* brk) {
   const BScene& sc = *ssc;
+  constexpr bool kApart = !std::is_same<ST, STS>::value;
   const int S = sc.S, P = sc.P;
   const uint8_t* code = A.marena + sc.moff;
   const uint8_t* rowfl = code + sc.fstride;
@@ -342,13 +369,11 @@ __device__ __forceinline__ void blk_op(const BatchArgs& A, const BScene* ssc, co
   G.P = P;
   switch (op.kind) {
     case kOpSources:
-      blk_sources(A, sc, bfield<ST>(A, sc, 1), bfield<ST>(A, sc, 0), bfield<ST>(A, sc, 2), bfield<ST>(A, sc, 3));
+      blk_sources(A, sc, bscalar<STS, ST>(A, sc, 1), bscalar<STS, ST>(A, sc, 0), bfield<ST>(A, sc, 2), bfield<ST>(A, sc, 3));
       __syncthreads();
       break;
     case kOpDiffuse:
     case kOpLinSolve: {
-      G.x = bfield<ST>(A, sc, op.f[0]);
-      G.x0 = bfield<ST>(A, sc, op.f[1]);
       float a, cr;
       if (op.kind == kOpDiffuse) {
         // diffuse (fluid.rs:276-298): a = ((dt*diff)*sf)*sf, c = 1 + 4a
@@ -360,6 +385,25 @@ __device__ __forceinline__ void blk_op(const BatchArgs& A, const BScene* ssc, co
         a = op.a;
         cr = fdiv(1.0f, op.c);
       }
+      if (kApart && op.f[0] < 2) {  // density diffusion: the scalar fields
+        WGrid<STS> H;
+        H.code = code;
+        H.rowfl = rowfl;
+        H.colfl = colfl;
+        H.S = S;
+        H.P = P;
+        H.x = bscalar<STS, ST>(A, sc, op.f[0]);
+        H.x0 = bscalar<STS, ST>(A, sc, op.f[1]);
+        if (op.mode == kRow)
+          wave_lin_solve<kRow, STS>(H, Bf, sc.K, A.nwmax, a, cr);
+        else if (op.mode == kCol)
+          wave_lin_solve<kCol, STS>(H, Bf, sc.K, A.nwmax, a, cr);
+        else
+          wave_lin_solve<kPassive, STS>(H, Bf, sc.K, A.nwmax, a, cr);
+        break;
+      }
+      G.x = bfield<ST>(A, sc, op.f[0]);
+      G.x0 = bfield<ST>(A, sc, op.f[1]);
       if (op.mode == kRow)
         wave_lin_solve<kRow, ST>(G, Bf, sc.K, A.nwmax, a, cr);
       else if (op.mode == kCol)
@@ -388,29 +432,30 @@ __device__ __forceinline__ void blk_op(const BatchArgs& A, const BScene* ssc, co
       blk_advect_breaks(bfield<ST>(A, sc, op.f[0]), bfield<ST>(A, sc, op.f[1]), S, P, dt0, brk);
       break;
     case kOpAdvectWrite: {
+      if (kApart && op.f[0] < 2) {  // density advected from scratch
+        STS* d = bscalar<STS, ST>(A, sc, op.f[0]);
+        blk_advect_write(d, bscalar<STS, ST>(A, sc, op.f[1]), bfield<ST>(A, sc, op.f[2]),
+                         bfield<ST>(A, sc, op.f[3]), S, P, dt0, brk);
+        blk_bnd_mode(op.mode, d, code, rowfl, colfl, S, P);
+        break;
+      }
       ST* d = bfield<ST>(A, sc, op.f[0]);
       blk_advect_write(d, bfield<ST>(A, sc, op.f[1]), bfield<ST>(A, sc, op.f[2]),
                        bfield<ST>(A, sc, op.f[3]), S, P, dt0, brk);
-      if (op.mode == kRow)
-        blk_bnd<kRow>(d, code, rowfl, colfl, S, P);
-      else if (op.mode == kCol)
-        blk_bnd<kCol>(d, code, rowfl, colfl, S, P);
-      else
-        blk_bnd<kPassive>(d, code, rowfl, colfl, S, P);
+      blk_bnd_mode(op.mode, d, code, rowfl, colfl, S, P);
       break;
     }
-    case kOpBnd: {
-      ST* x = bfield<ST>(A, sc, op.f[0]);
-      if (op.mode == kRow)
-        blk_bnd<kRow>(x, code, rowfl, colfl, S, P);
-      else if (op.mode == kCol)
-        blk_bnd<kCol>(x, code, rowfl, colfl, S, P);
+    case kOpBnd:
+      if (kApart && op.f[0] < 2)
+        blk_bnd_mode(op.mode, bscalar<STS, ST>(A, sc, op.f[0]), code, rowfl, colfl, S, P);
       else
-        blk_bnd<kPassive>(x, code, rowfl, colfl, S, P);
+        blk_bnd_mode(op.mode, bfield<ST>(A, sc, op.f[0]), code, rowfl, colfl, S, P);
       break;
-    }
     case kOpCopy:
-      blk_copy(bfield<ST>(A, sc, op.f[0]), bfield<ST>(A, sc, op.f[1]), S, P);
+      if (kApart && op.f[0] < 2)
+        blk_copy(bscalar<STS, ST>(A, sc, op.f[0]), bscalar<STS, ST>(A, sc, op.f[1]), S, P);
+      else
+        blk_copy(bfield<ST>(A, sc, op.f[0]), bfield<ST>(A, sc, op.f[1]), S, P);
       break;
     default:
       break;
@@ -428,8 +473,9 @@ __device__ __forceinline__ WBufs batch_bufs(const BatchArgs& A) {
 }
 
 // The operation list on every scene: persistent blocks draining the scene
-// queue (one launch = one frame when L is the frame's list).
-template <class ST>
+// queue (one launch = one frame when L is the frame's list). ST: the velocity
+// fields' storage, STS: density and scratch's.
+template <class ST, class STS = ST>
 __global__ void __launch_bounds__(672, 1) k_batch_run(BatchArgs A, BOpList L) {
   extern __shared__ __align__(16) float bsm[];
   __shared__ int s_next;
@@ -445,7 +491,7 @@ __global__ void __launch_bounds__(672, 1) k_batch_run(BatchArgs A, BOpList L) {
     __syncthreads();
     const int q = s_next;
     if (q >= A.nscenes) break;
-    for (int k = 0; k < L.n; ++k) blk_op<ST>(A, &s_sc, L.op[k], Bf, brk);
+    for (int k = 0; k < L.n; ++k) blk_op<ST, STS>(A, &s_sc, L.op[k], Bf, brk);
     __syncthreads();
   }
 }

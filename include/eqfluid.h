@@ -266,10 +266,11 @@ typedef struct eq_batch eq_batch; /* opaque; owns device state */
  * init() once, frame = DefaultWall). `device` < 0 = current device. */
 int eq_batch_new(int64_t nscenes, const eq_scene_desc* scenes, int device, eq_batch** out);
 /* The same with the fields STORED in FP16 or BF16 (storage EQ_STORE_F16 /
- * EQ_STORE_BF16, defined with the precision form below; 0 = FP32): every
- * phase computes exactly as the FP32 batch on the widened values and rounds
- * once on store, so the per-scene results differ from the reference's only by
- * those roundings (and their propagation). */
+ * EQ_STORE_BF16, defined with the precision form below; 0 = FP32), or with
+ * only density and scratch in FP16 (EQ_STORE_F16_SCALARS): every phase
+ * computes exactly as the FP32 batch on the widened values and rounds once on
+ * store, so the per-scene results differ from the reference's only by those
+ * roundings (and their propagation). */
 int eq_batch_new_storage(int64_t nscenes, const eq_scene_desc* scenes, int storage, int device,
                          eq_batch** out);
 int eq_batch_free(eq_batch* b); /* accepts NULL */
@@ -347,6 +348,10 @@ int eq_batch_launch_count(const eq_batch* b, uint64_t* count);
  * refinement and the post-projection divergence of the last frame. */
 #define EQ_STORE_F16 1
 #define EQ_STORE_BF16 2
+/* Batches only: density and scratch stored in FP16, the four velocity fields
+ * in FP32 (advect's backtraces multiply a velocity's rounding by dt*N cells,
+ * so FP16 velocities dominate the density error; see eq_batch_new_storage). */
+#define EQ_STORE_F16_SCALARS 3
 
 typedef struct eq_hstats {
   int32_t ir_iterations[2];  /* refinement rounds of the frame's two projects */

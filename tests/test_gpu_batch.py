@@ -198,10 +198,14 @@ def test_batch_rejects_bad_arguments(eqlib):
 # amplify any rounding quickly (the reference's own FP32 step drifts from its
 # FP64 step by a factor ~40 in 3 frames there, and rounding to FP16 once per
 # frame alone gives 6e-3 / 2e-3), the third is diffusion-dominated.
-HALF_TOL = {"f16": (0.1, 0.05, 2e-3), "bf16": (0.5, 0.3, 2e-2)}
+# With only density and scratch in FP16 (velocities FP32) the error stays at
+# the FP16 rounding of the density itself (about 2e-4 here), within the 1e-3
+# the benchmark spec sets for the FP16 batch.
+HALF_TOL = {"f16": (0.1, 0.05, 2e-3), "bf16": (0.5, 0.3, 2e-2),
+            "f16_scalars": (1e-3, 1e-3, 1e-3)}
 
 
-@pytest.mark.parametrize("storage", ["f16", "bf16"])
+@pytest.mark.parametrize("storage", ["f16", "bf16", "f16_scalars"])
 def test_batch_half_storage_vs_f64(eqlib, storage):
     """FP16 / BF16 storage, FP32 arithmetic, the reference's method: each
     scene's density stays close to the f64 reference step (relative L2 over
