@@ -323,7 +323,17 @@ __global__ void __launch_bounds__(1024, 1) k_gs_adj_cl(GsAdjArgs A) {
     int r0 = tb + 3 * s;
     if (r0 >= R) r0 -= R;
     int o0 = r0 * W;  // ring row of diagonal d = D0 - t + 3s
+    // The last sweep's results go to global memory one step late, after the
+    // next barrier, so that no barrier's release waits for an L2 write.
+    size_t pend_q = 0;
+    float pend_v = 0.0f, pend_sum = 0.0f;
+    bool pend = false;
     for (int t = 0; t < nsteps; ++t) {
+      if (pend) {
+        A.Ysum[pend_q] = pend_sum;
+        A.yK[pend_q] = pend_v;
+        pend = false;
+      }
       const int d = D0 - t + 3 * s, i = d - j;
       if (jok && t >= 3 * s && i >= 1 && i <= N) {
         const int op1 = o0 + W == RW ? 0 : o0 + W;
@@ -364,13 +374,18 @@ __global__ void __launch_bounds__(1024, 1) k_gs_adj_cl(GsAdjArgs A) {
         const float sum = (s == 0) ? v : Ys[o0] + v;
         Ys[o0] = sum;
         if (s == K - 1) {
-          const size_t q = dg_at(i, j, P);
-          A.Ysum[q] = sum;
-          A.yK[q] = v;
+          pend_q = dg_at(i, j, P);
+          pend_v = v;
+          pend_sum = sum;
+          pend = true;
         }
       }
       o0 = o0 == 0 ? RW - W : o0 - W;
       cluster.sync();
+    }
+    if (pend) {
+      A.Ysum[pend_q] = pend_sum;
+      A.yK[pend_q] = pend_v;
     }
     return;
   }
