@@ -5,6 +5,8 @@
 // fields each advect reads saved (the tape), then undone frame by frame with
 // the adjoint kernels. Compiled in the same translation unit as eqfluid.cu (it
 // drives the plain handle's launches).
+#include <atomic>
+
 #include "adjoint.cuh"
 
 struct eq_grad {
@@ -152,10 +154,12 @@ int launch_gs_adj(eq_grad* g, const eqk::GsAdjArgs& A) {
 // hold the cluster, else one block with shared memory where the band fits
 // (the kernels' attributes are raised once).
 int pick_gs_store(eq_grad* g, int S, int K) {
-  static bool raised = false;
+  // kernel attributes are per device: one bit per device once they are raised
+  static std::atomic<uint64_t> raised{0};
   int dev = g->h->device, optin = 0;
   EQ_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  if (!raised) {
+  const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
+  if (!bit || !(raised.load() & bit)) {
     auto raise = [&](const void* fn) {
       return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     };
@@ -175,7 +179,7 @@ int pick_gs_store(eq_grad* g, int S, int K) {
         nonportable((const void*)eqk::k_gs_adj_cl<eqk::kCol>) != cudaSuccess ||
         nonportable((const void*)eqk::k_gs_adj_cl<eqk::kPassive>) != cudaSuccess)
       return fail(EQ_ERR_CUDA, "cudaFuncSetAttribute (adjoint wavefront)");
-    raised = true;
+    raised.fetch_or(bit);
   }
   bool ok[4];
   ok[0] = true;

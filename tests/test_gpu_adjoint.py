@@ -40,7 +40,10 @@ def make(size, K=20, dt=0.1, diff=1e-4, visc=1e-4, rects=()):
 
 
 def rel(a, b):
-    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
+    """Relative L2 distance (absolute when the reference is exactly zero)."""
+    den = float(np.linalg.norm(np.asarray(b, np.float64)))
+    num = float(np.linalg.norm(np.asarray(a, np.float64) - np.asarray(b, np.float64)))
+    return num / den if den > 0.0 else num
 
 
 @pytest.mark.parametrize("scene", list(SCENES))
@@ -170,6 +173,42 @@ def test_backward_vs_tape(eqlib, size, frames, every):
         fin.step()
     for k in range(6):
         assert np.array_equal(f.read_field(k), fin.fields[k]), k
+    g.close()
+    f.close()
+
+
+@pytest.mark.parametrize("size,K,frames,every,vel,store", [
+    (37, 1, 3, 1, 0.3, -1),    # one sweep per solve, a checkpoint every frame, odd size
+    (40, 0, 2, 1, 0.3, -1),    # no sweeps: lin_solve is the identity, its adjoint too
+    (50, 20, 4, 3, 3.0, -1),   # fast flow: many clamped backtraces and early row breaks
+    (66, 20, 3, 2, 0.3, 2),    # the single-block transposed solver
+    (66, 20, 3, 2, 0.3, 0),    # the global-memory transposed solver
+])
+def test_backward_more_cases(eqlib, size, K, frames, every, vel, store):
+    """backward() against the f32 tape adjoint (the same forward and discrete
+    path) across sweep counts, checkpoint spacings and flow speeds."""
+    rects = [(size // 4, size // 3, size // 4 + 5, size // 3 + 4), (size - 9, 0, size - 5, 7)]
+    rng = np.random.default_rng(size + K)
+    f, of = make(size, K=K, dt=0.1, diff=1e-4, visc=1e-4, rects=rects)
+    n = size * size
+    init = [fl.copy() for fl in of.fields]
+    init[2] = (init[2] * 0.0 + rng.normal(0, vel, n)).astype(np.float32)
+    init[3] = (init[3] * 0.0 + rng.normal(0, vel, n)).astype(np.float32)
+    for k in range(6):
+        f.write_field(k, init[k])
+    src = rng.uniform(0, 0.5, (frames, n)).astype(np.float32)
+    target = oracle.gaussian_target(size, 6, (2.0, 5.0), seed=3).astype(np.float32)
+    g = Recorder(f, frames, every)
+    if store >= 0:
+        g.set_wavefront_storage(store)
+    g.forward(src)
+    loss = g.l2_loss(target)
+    gi, gs = g.backward()
+    l32, _, vx32, vy32, src32 = oracle.adjoint_problem_f32(of.cells, size, 0.1, K, 1e-4, 1e-4,
+                                                           init, src, target)
+    assert abs(loss - l32) <= 1e-5 * abs(l32), (loss, l32)
+    for name, got, ref in (("vx", gi[2], vx32), ("vy", gi[3], vy32), ("src", gs, src32)):
+        assert rel(got, ref) < 1e-4, (name, rel(got, ref))
     g.close()
     f.close()
 
