@@ -272,45 +272,60 @@ def precision_scene(size, seed=4, nframes=1):
             gauss[..., 1].astype(np.float32))
 
 
+def _precision_reference(task):
+    """One f64 host reference of the precision workload (spawned worker, the
+    oracle only): 'f64_reference' = the reference step, 'f64_converged_pressure'
+    = the same step with both pressure solves converged; returns the density
+    and velocities after each frame in err_frames."""
+    import oracle
+    kind, size, err_frames = task
+    nmax = max(err_frames)
+    rects, sx, sy, sd, su, sv = precision_scene(size, nframes=nmax)
+    r = oracle.OracleFluid(size, PREC_DT, ITERS, PREC_DIFF, PREC_VISC, dtype=np.float64)
+    for rc in rects:
+        r.fill_obstacle(*rc)
+    snaps = {}
+    for fr in range(nmax):
+        oracle.add_sources(r, sx, sy, sd[fr], su[fr], sv[fr])
+        if kind == "f64_reference":
+            r.step()
+        else:
+            oracle.converged_step_f64(r)
+        if fr + 1 in err_frames:
+            snaps[fr + 1] = (r.fields[1].copy(), r.fields[2].copy(), r.fields[3].copy())
+    return kind, snaps
+
+
 def run_precision_form(local_rank: int, frames: int, size: int = PREC_SIZE,
                        err_frames=(1,), storages=("f16", "bf16")):
     """The precision form on one scene: throughput of `frames` timed frames per
     storage format, its refinement statistics, and at `err_frames` the relative
     L2 density error, max-abs velocity error and post-projection divergence
-    against two f64 references run on the host: the reference step itself and
-    the same step with both pressure solves converged exactly."""
+    against two f64 references run on the host (in two spawned processes,
+    while the GPU runs): the reference step itself and the same step with both
+    pressure solves converged exactly."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
     import torch
-    import oracle
     from equilibrium_gb300.precision import HalfFluid, max_abs, rel_l2
     nmax = max(err_frames) if err_frames else 0
     total = max(frames + 1, nmax)
     rects, sx, sy, sd, su, sv = precision_scene(size, nframes=total)
-    refs = {}
+    pool, futs, refs = None, [], {}
     if err_frames:
-        for kind in ("f64_reference", "f64_converged_pressure"):
-            r = oracle.OracleFluid(size, PREC_DT, ITERS, PREC_DIFF, PREC_VISC, dtype=np.float64)
-            for rc in rects:
-                r.fill_obstacle(*rc)
-            refs[kind] = (r, {})
-        for fr in range(nmax):
-            for kind, (r, snaps) in refs.items():
-                oracle.add_sources(r, sx, sy, sd[fr], su[fr], sv[fr])
-                if kind == "f64_reference":
-                    r.step()
-                else:
-                    oracle.converged_step_f64(r)
-                if fr + 1 in err_frames:
-                    snaps[fr + 1] = (r.fields[1].copy(), r.fields[2].copy(), r.fields[3].copy())
+        pool = cf.ProcessPoolExecutor(2, mp_context=mp.get_context("spawn"))
+        futs = [pool.submit(_precision_reference, (kind, size, tuple(err_frames)))
+                for kind in ("f64_reference", "f64_converged_pressure")]
     out = {"workload": f"one scene, N = {size - 2} interior, dt {PREC_DT}, diffusion = viscosity "
                        f"= {PREC_DIFF}, 20 sweeps per diffusion solve, pressure refined to a "
                        f"relative residual of {PREC_RTOL}, 4 seeded rectangles, {NSRC} seeded "
                        "sources per frame"}
+    gpu_snaps = {}
     for storage in storages:
         g = HalfFluid(size, PREC_DT, ITERS, PREC_DIFF, PREC_VISC, storage, PREC_RTOL, 30,
                       device=local_rank)
         for rc in rects:
             g.fill_obstacle(*rc)
-        errs = {}
         ms, launches = [], []
         for fr in range(max(total, frames + 1)):
             g.add_sources(sx, sy, sd[fr % total], su[fr % total], sv[fr % total])
@@ -321,22 +336,34 @@ def run_precision_form(local_rank: int, frames: int, size: int = PREC_SIZE,
             ms.append((time.perf_counter() - t0) * 1e3)
             launches.append(g.launch_count() - c0)
             if fr + 1 in err_frames:
-                de, vx, vy = g.read_field(1), g.read_field(2), g.read_field(3)
-                st = g.stats()
-                errs[f"frame_{fr + 1}"] = {
-                    kind: {"density_rel_l2": rel_l2(de, snaps[fr + 1][0]),
-                           "velocity_max_abs": max(max_abs(vx, snaps[fr + 1][1]),
-                                                   max_abs(vy, snaps[fr + 1][2]))}
-                    for kind, (_, snaps) in refs.items()}
-                errs[f"frame_{fr + 1}"]["post_projection_divergence_l2"] = st["div_norm"]
+                gpu_snaps[(storage, fr + 1)] = (g.read_field(1), g.read_field(2),
+                                                g.read_field(3), g.stats()["div_norm"])
         timed = ms[1:frames + 1]
         t = statistics.mean(timed)
         out[storage] = {"value": (size - 2) ** 2 / (t / 1e3), "unit": "cell-steps/s",
                         "ms_per_frame": t, "frames_timed": len(timed),
                         "clock": "host, per frame (the refinement loop reads its norms)",
-                        "stats_last_frame": g.stats(), "errors": errs,
+                        "stats_last_frame": g.stats(),
                         "gpu_launches_per_frame": statistics.mean(launches[1:frames + 1])}
         g.close()
+    if err_frames:
+        t0 = time.perf_counter()
+        for f in futs:
+            kind, snaps = f.result()
+            refs[kind] = snaps
+        pool.shutdown()
+        for storage in storages:
+            errs = {}
+            for fr in err_frames:
+                de, vx, vy, div = gpu_snaps[(storage, fr)]
+                errs[f"frame_{fr}"] = {
+                    kind: {"density_rel_l2": rel_l2(de, snaps[fr][0]),
+                           "velocity_max_abs": max(max_abs(vx, snaps[fr][1]),
+                                                   max_abs(vy, snaps[fr][2]))}
+                    for kind, snaps in refs.items()}
+                errs[f"frame_{fr}"]["post_projection_divergence_l2"] = div
+            out[storage]["errors"] = errs
+        out["f64_references_wait_s"] = time.perf_counter() - t0
     return out
 
 
@@ -1010,9 +1037,11 @@ def main():
                          "the batched workload (after one warm-up frame), 'precision1024' = two "
                          "frames of the precision form at N = 1024 (FP16), 'diff256' = one "
                          "gradient of the differentiation workload at N = 256 over 4 frames")
+    ap.add_argument("--study-size", type=int, default=514,
+                    help="size (N + 2) of --precision-study")
     ap.add_argument("--precision-study", action="store_true",
-                    help="only the precision form's error study: N=512, errors at frames 1, "
-                         "50 and 200 against both f64 references")
+                    help="only the precision form's error study: N = study-size - 2, errors "
+                         "at frames 1, 50 and 200 against both f64 references")
     ap.add_argument("--no-forms", dest="forms", action="store_false",
                     help="skip the batched / half-storage forms")
     args = ap.parse_args()
@@ -1026,7 +1055,7 @@ def main():
         eqbuild.build()
         torch.cuda.set_device(0)
         print(json.dumps({"precision_study": run_precision_form(
-            0, 3, size=514, err_frames=(1, 50, 200))}), flush=True)
+            0, 3, size=args.study_size, err_frames=(1, 50, 200))}), flush=True)
     elif args.diff_only:
         import torch
         from equilibrium_gb300 import build as eqbuild

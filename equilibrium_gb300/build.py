@@ -18,7 +18,7 @@ LIB = os.path.join(HERE, "libeqfluid.so")
 SOURCES = ["eqfluid.cu"]
 HEADERS = ["common.cuh", "kernels.cuh", "linsolve.cuh", "noalloc.cu", "wave.cuh", "batch.cuh",
            "batch.cu", "half.cuh", "mg.cuh", "half.cu", "store.cuh",
-           "frame.cuh", "frame.cu", "adjoint.cuh", "adjoint.cu"]
+           "frame.cuh", "frame.cu", "adjoint.cuh", "adjoint.cu", "lscl.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: device FP stays un-contracted even outside the explicitly

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -19,6 +20,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "linsolve.cuh"
+#include "lscl.cuh"
 
 namespace {
 
@@ -92,6 +94,12 @@ struct eq_fluid {
   float gdt = 0.f, gdiff = 0.f, gvisc = 0.f;
   uint64_t glaunches = 0;
   bool graph_mode = false;  // lin_solve clears its tagged buffers (graph replay)
+
+  // lin_solve form: 0 auto (the cluster wavefront where it applies), 1 the
+  // multi-block wavefront always, 2 the cluster wavefront where it applies
+  int solver = 0;
+  int64_t cl_K = -1;  // sweep count the cluster check below was made for
+  int cl_blocks = 0;  // blocks per cluster for cl_K, 0 = not applicable
 
   size_t grid_elems() const { return (size_t)P * S; }
 };
@@ -199,11 +207,123 @@ int launch_bnd(eq_fluid* h, int mode, float* x) {
   return check_launch(h);
 }
 
+// Blocks per cluster for the cluster wavefront (lscl.cuh) at this size and
+// sweep count, or 0 where it does not apply: one warp per sweep (K <= 32),
+// strips of 16 to 32 positions, the staged strip and band within the opt-in
+// shared memory, and a device that can hold the cluster.
+int cluster_blocks(eq_fluid* h, int64_t K) {
+  if (h->cl_K == K) return h->cl_blocks;
+  h->cl_K = K;
+  h->cl_blocks = 0;
+  const int S = (int)h->S, N = S - 2;
+  if (K < 1 || K > 32 || N < 32) return 0;
+  const int C = std::min(16, (N + 31) / 32), J = (N + C - 1) / C;
+  if (C < 2 || J > 32 || J < 16 || (C - 1) * J >= N) return 0;
+  int optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device) !=
+      cudaSuccess)
+    return 0;
+  const size_t bytes = eqk::ls_cl_layout(S, (int)K, C).total;
+  if (bytes > (size_t)optin) return 0;
+  static std::atomic<uint64_t> raised{0};
+  const uint64_t bit = h->device < 64 ? (1ull << h->device) : 0ull;
+  if (!bit || !(raised.load() & bit)) {
+    const void* fns[3] = {(const void*)eqk::k_ls_cl<eqk::kRow>, (const void*)eqk::k_ls_cl<eqk::kCol>,
+                          (const void*)eqk::k_ls_cl<eqk::kPassive>};
+    for (const void* fn : fns)
+      if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) !=
+              cudaSuccess ||
+          cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+              cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+      }
+    raised.fetch_or(bit);
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(C);
+  cfg.blockDim = dim3(32 * (unsigned)K);
+  cfg.dynamicSmemBytes = bytes;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int nclusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&nclusters, eqk::k_ls_cl<eqk::kPassive>, &cfg) ==
+          cudaSuccess &&
+      nclusters >= 1)
+    h->cl_blocks = C;
+  cudaGetLastError();
+  return h->cl_blocks;
+}
+
+// lin_solve by the cluster wavefront, then set_boundaries of the last sweep.
+int launch_lin_solve_cluster(eq_fluid* h, int mode, float* x, const float* x0, float a,
+                             float c_recip, int C) {
+  const int S = (int)h->S;
+  const int K = (int)h->frames;
+  eqk::LsClArgs A;
+  A.x = x;
+  A.x0 = x0;
+  A.code = h->code;
+  A.rowfl = h->rowfl;
+  A.colfl = h->colfl;
+  A.S = S;
+  A.P = h->P;
+  A.K = K;
+  A.R = 3 * K + 4;
+  A.a = a;
+  A.cr = c_recip;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(C);
+  cfg.blockDim = dim3(32 * (unsigned)K);
+  cfg.dynamicSmemBytes = eqk::ls_cl_layout(S, K, C).total;
+  cfg.stream = h->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  if (h->profiling) {
+    EQ_CUDA(cudaEventCreate(&ev0));
+    EQ_CUDA(cudaEventCreate(&ev1));
+    EQ_CUDA(cudaEventRecord(ev0, h->stream));
+  }
+  switch (mode) {
+    case eqk::kRow:
+      EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cl<eqk::kRow>, A));
+      break;
+    case eqk::kCol:
+      EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cl<eqk::kCol>, A));
+      break;
+    default:
+      EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cl<eqk::kPassive>, A));
+      break;
+  }
+  int rc = check_launch(h);
+  if (rc) return rc;
+  if (h->profiling) {
+    EQ_CUDA(cudaEventRecord(ev1, h->stream));
+    h->ls_events.emplace_back(ev0, ev1);
+  }
+  return launch_bnd(h, mode, x);
+}
+
 // lin_solve (fluid.rs:301-325) on device grids.
 int launch_lin_solve(eq_fluid* h, int mode, float* x, const float* x0, float a, float c) {
   const int64_t K = h->frames;
   if (K <= 0) return EQ_OK;
   const float c_recip = 1.0f / c;  // fluid.rs:311, IEEE f32 division
+  if (h->solver != 1) {
+    const int C = cluster_blocks(h, K);
+    if (C > 0) return launch_lin_solve_cluster(h, mode, x, x0, a, c_recip, C);
+  }
   const int S = (int)h->S;
   for (int64_t done = 0; done < K; done += kMaxSweepsPerLaunch) {
     const int Kc = (int)std::min<int64_t>(kMaxSweepsPerLaunch, K - done);
@@ -884,6 +1004,21 @@ int eq_fluid_kernel_stats(eq_fluid* h, int kernel, double* total_ms, uint64_t* l
   *total_ms = sum;
   *launches = h->ls_events.size();
   h->ls_events.clear();
+  return EQ_OK;
+}
+
+int eq_fluid_set_solver(eq_fluid* h, int solver) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  if (solver < 0 || solver > 2) return fail(EQ_ERR_ARG, "solver must be 0, 1 or 2");
+  h->solver = solver;
+  return EQ_OK;
+}
+
+int eq_fluid_get_solver(eq_fluid* h, int* cluster_blocks_out) {
+  if (!h || !cluster_blocks_out) return fail(EQ_ERR_ARG, "null argument");
+  int rc = select_device(h);
+  if (rc) return rc;
+  *cluster_blocks_out = h->solver == 1 ? 0 : cluster_blocks(h, h->frames);
   return EQ_OK;
 }
 

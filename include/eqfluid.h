@@ -484,6 +484,14 @@ int eq_fluid_launch_count(const eq_fluid* h, uint64_t* count);
  * cannot complete end with EQ_ERR_TIMEOUT sooner. */
 int eq_fluid_set_spin_limit(eq_fluid* h, int64_t iterations);
 
+/* Which kernel runs lin_solve: 0 (default) = the thread-block-cluster
+ * wavefront where it applies (sizes with 32 < N <= ~300 and <= 32 sweeps;
+ * both kernels are bit-exact), else the multi-block wavefront; 1 = the
+ * multi-block wavefront always; 2 = like 0. get_solver reports the blocks
+ * per cluster the next solve uses (0 = the multi-block wavefront). */
+int eq_fluid_set_solver(eq_fluid* h, int solver);
+int eq_fluid_get_solver(eq_fluid* h, int* cluster_blocks);
+
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their own
  * work or events against the handle's launches. */
 int eq_fluid_get_stream(eq_fluid* h, void** stream);

@@ -101,10 +101,14 @@ def test_large_workload_two_frames_bitexact(eqlib):
 
 
 def test_bounded_wait_reports_timeout_and_recovers(eqlib):
-    """A spin budget of one poll makes the wavefront's waits run out: the
-    kernel records EQ_ERR_TIMEOUT in its error word and every block returns;
-    the handle stays usable. No fault, trap or hang is involved."""
+    """A spin budget of one poll makes the multi-block wavefront's waits run
+    out: the kernel records EQ_ERR_TIMEOUT in its error word and every block
+    returns; the handle stays usable. No fault, trap or hang is involved. (The
+    cluster wavefront, the default at this size, has no inter-block waits:
+    it synchronises with cluster barriers, so the multi-block form is
+    selected here.)"""
     g = gpu_fluid(300, 20, 0.1, 1e-4, 1e-4)
+    assert eqlib.eq_fluid_set_solver(g.handle, 1) == 0
     assert eqlib.eq_fluid_set_spin_limit(g.handle, 1) == 0
     g.step()
     rc = eqlib.eq_fluid_synchronize(g.handle)
