@@ -100,6 +100,8 @@ struct eq_fluid {
   int solver = 0;
   int64_t cl_K = -1;  // sweep count the cluster check below was made for
   int cl_blocks = 0;  // blocks per cluster for cl_K, 0 = not applicable
+  int cl_m = 0;       // its barrier interval - 1 (lscl.cuh)
+  int cl_mmax = 1;    // cap on cl_m (1: the fastest or within 3 % at N = 64..288, measured)
 
   size_t grid_elems() const { return (size_t)P * S; }
 };
@@ -223,8 +225,12 @@ int cluster_blocks(eq_fluid* h, int64_t K) {
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device) !=
       cudaSuccess)
     return 0;
-  const size_t bytes = eqk::ls_cl_layout(S, (int)K, C).total;
+  // the longest barrier interval whose band still fits
+  int m = h->cl_mmax;
+  while (m > 0 && eqk::ls_cl_layout(S, (int)K, C, m).total > (size_t)optin) --m;
+  const size_t bytes = eqk::ls_cl_layout(S, (int)K, C, m).total;
   if (bytes > (size_t)optin) return 0;
+  h->cl_m = m;
   static std::atomic<uint64_t> raised{0};
   const uint64_t bit = h->device < 64 ? (1ull << h->device) : 0ull;
   if (!bit || !(raised.load() & bit)) {
@@ -274,13 +280,14 @@ int launch_lin_solve_cluster(eq_fluid* h, int mode, float* x, const float* x0, f
   A.S = S;
   A.P = h->P;
   A.K = K;
-  A.R = 3 * K + 4;
+  A.m = h->cl_m;
+  A.R = eqk::ls_cl_rows(K, A.m);
   A.a = a;
   A.cr = c_recip;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(C);
   cfg.blockDim = dim3(32 * (unsigned)K);
-  cfg.dynamicSmemBytes = eqk::ls_cl_layout(S, K, C).total;
+  cfg.dynamicSmemBytes = eqk::ls_cl_layout(S, K, C, A.m).total;
   cfg.stream = h->stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1011,6 +1018,14 @@ int eq_fluid_set_solver(eq_fluid* h, int solver) {
   if (!h) return fail(EQ_ERR_ARG, "null handle");
   if (solver < 0 || solver > 2) return fail(EQ_ERR_ARG, "solver must be 0, 1 or 2");
   h->solver = solver;
+  return EQ_OK;
+}
+
+int eq_fluid_set_cluster_interval(eq_fluid* h, int max_m) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  if (max_m < 0 || max_m > 3) return fail(EQ_ERR_ARG, "max_m must be in [0, 3]");
+  h->cl_mmax = max_m;
+  h->cl_K = -1;  // re-check
   return EQ_OK;
 }
 

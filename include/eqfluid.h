@@ -491,6 +491,10 @@ int eq_fluid_set_spin_limit(eq_fluid* h, int64_t iterations);
  * per cluster the next solve uses (0 = the multi-block wavefront). */
 int eq_fluid_set_solver(eq_fluid* h, int solver);
 int eq_fluid_get_solver(eq_fluid* h, int* cluster_blocks);
+/* Caps the cluster wavefront's barrier interval at max_m + 1 steps (0..3;
+ * default 1; the longest interval up to the cap that fits in shared memory
+ * is used). */
+int eq_fluid_set_cluster_interval(eq_fluid* h, int max_m);
 
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their own
  * work or events against the handle's launches. */

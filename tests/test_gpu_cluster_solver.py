@@ -57,6 +57,14 @@ def test_cluster_lin_solve_bitexact(eqlib, size, K, mode):
     ref = x.copy()
     oracle.lin_solve(mode, ref, x0, a, c, size, K, r.cells)
     assert_bitexact(f.read_field(2), ref, f"cluster lin_solve mode {mode} K {K}", size)
+    # every barrier interval (1, 2, 3, 4 steps) gives the same bits
+    for max_m in (0, 2, 3):
+        _lib.check(L.eq_fluid_set_cluster_interval(f.handle, max_m))
+        f.write_field(2, x)
+        _lib.check(L.eq_fluid_lin_solve(f.handle, mode, 2, 4, a, c))
+        f.synchronize()
+        assert_bitexact(f.read_field(2), ref, f"cluster interval {max_m + 1} mode {mode}", size)
+    _lib.check(L.eq_fluid_set_cluster_interval(f.handle, 1))
     # and the multi-block wavefront gives the same bits
     _lib.check(L.eq_fluid_set_solver(f.handle, 1))
     assert blocks(f) == 0
