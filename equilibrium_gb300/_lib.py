@@ -173,6 +173,7 @@ def load(path: str = LIB_PATH):
         "eq_grad_backward_device": (i32, [H, P, P, P]),
         "eq_grad_frames": (i32, [H, ctypes.POINTER(ctypes.c_int64)]),
         "eq_grad_set_wavefront_storage": (i32, [H, i32]),
+        "eq_grad_set_cluster_interval": (i32, [H, i32]),
         "eq_grad_get_wavefront_storage": (i32, [H, ctypes.POINTER(ctypes.c_int),
                                                 ctypes.POINTER(ctypes.c_int)]),
         "eq_grad_set_profiling": (i32, [H, i32]),

@@ -40,6 +40,8 @@ struct eq_grad {
   int gs_store = 0;   // where the adjoint wavefront keeps its band (see gs_adj_smem_bytes)
   int gs_force = -1;  // cap on gs_store (tests of the other forms)
   int gs_cluster = 8; // blocks per cluster (gs_store == 3)
+  int gs_m = 0;       // its barrier interval - 1
+  int gs_mmax = -1;   // cap on gs_m; -1: 2 for N >= 192, else 1 (the fastest, measured)
 };
 
 namespace {
@@ -110,7 +112,7 @@ int launch_gs_adj(eq_grad* g, const eqk::GsAdjArgs& A) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(g->gs_cluster);
     cfg.blockDim = dim3(gs_cl_threads(A.S, A.K, g->gs_cluster));
-    cfg.dynamicSmemBytes = eqk::gs_cl_layout(A.S, A.K, g->gs_cluster).total;
+    cfg.dynamicSmemBytes = eqk::gs_cl_layout(A.S, A.K, g->gs_cluster, A.m).total;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -187,7 +189,14 @@ int pick_gs_store(eq_grad* g, int S, int K) {
   ok[2] = eqk::gs_adj_smem_bytes(2, S, K) <= (size_t)optin;
   ok[3] = false;
   const int C = (S - 2) >= 384 ? 16 : 8;
-  const size_t cl_bytes = eqk::gs_cl_layout(S, K, C).total;
+  // the barrier interval: m + 1 steps where every warp has one task (the
+  // streamlined path) and the stretched band fits, else a barrier per step
+  const int J = (S - 2 + C - 1) / C;
+  const int mcap = g->gs_mmax >= 0 ? g->gs_mmax : (S - 2 >= 192 ? 2 : 1);
+  int m = (K * ((J + 31) / 32) <= 32) ? mcap : 0;
+  while (m > 0 && eqk::gs_cl_layout(S, K, C, m).total > (size_t)optin) --m;
+  g->gs_m = m;
+  const size_t cl_bytes = eqk::gs_cl_layout(S, K, C, m).total;
   if ((S - 2) / C >= 16 && cl_bytes <= (size_t)optin) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(C);
@@ -260,7 +269,8 @@ int adj_lin_solve(eq_grad* g, int mode, float* xb, float* x0b, float a, float c)
   A.S = S;
   A.P = P;
   A.K = (int)K;
-  A.R = (int)(3 * K + 4);
+  A.m = g->gs_store == 3 ? g->gs_m : 0;
+  A.R = g->gs_store == 3 ? eqk::gs_cl_rows((int)K, A.m) : (int)(3 * K + 4);
   A.alpha = alpha;
   switch (mode) {
     case eqk::kRow:
@@ -708,6 +718,13 @@ int eq_grad_set_wavefront_storage(eq_grad* g, int max_store) {
   if (!g) return fail(EQ_ERR_ARG, "null handle");
   if (max_store < -1 || max_store > 3) return fail(EQ_ERR_ARG, "max_store must be in [-1, 3]");
   g->gs_force = max_store;
+  return EQ_OK;
+}
+
+int eq_grad_set_cluster_interval(eq_grad* g, int max_m) {
+  if (!g) return fail(EQ_ERR_ARG, "null handle");
+  if (max_m < 0 || max_m > 3) return fail(EQ_ERR_ARG, "max_m must be in [0, 3]");
+  g->gs_mmax = max_m;
   return EQ_OK;
 }
 

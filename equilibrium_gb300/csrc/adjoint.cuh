@@ -122,6 +122,7 @@ struct GsAdjArgs {
   const uint8_t* colfl;
   int S, P, K;
   int R;            // diagonals kept in shared memory (STORE > 0)
+  int m;            // cluster form: a barrier every m + 1 steps (see k_gs_adj_cl)
   float alpha;
 };
 
@@ -252,8 +253,12 @@ __global__ void __launch_bounds__(1024, 1) k_gs_adj(GsAdjArgs A) {
 struct GsClLayout {  // byte offsets in one block's shared memory
   size_t ring, b, code, flags, total;
 };
-__host__ __device__ inline GsClLayout gs_cl_layout(int S, int K, int C) {
-  const size_t J = (size_t)((S - 2 + C - 1) / C), R = (size_t)(3 * K + 4), D = (size_t)(2 * S - 1);
+// Ring rows of the cluster form: the band a step touches, stretched by the
+// schedule of barrier interval m + 1 (lag 2m + 3 per sweep).
+__host__ __device__ inline int gs_cl_rows(int K, int m) { return (2 * m + 3) * K + 8; }
+__host__ __device__ inline GsClLayout gs_cl_layout(int S, int K, int C, int m) {
+  const size_t J = (size_t)((S - 2 + C - 1) / C), R = (size_t)gs_cl_rows(K, m),
+               D = (size_t)(2 * S - 1);
   GsClLayout L;
   L.ring = 0;                                          // 3 R (J + 3) floats (Y0, Y1, sum)
   L.b = 3 * R * (J + 3) * 4;                           // D J floats
@@ -272,7 +277,7 @@ __global__ void __launch_bounds__(1024, 1) k_gs_adj_cl(GsAdjArgs A) {
   const int C = (int)cluster.num_blocks(), r = (int)cluster.block_rank();
   const int J = (N + C - 1) / C, JC = J + 2, W = J + 3;
   const int jb = 1 + r * J, je = min(N, jb + J - 1);
-  const GsClLayout lay = gs_cl_layout(S, K, C);
+  const GsClLayout lay = gs_cl_layout(S, K, C, A.m);
   float* const Y0 = reinterpret_cast<float*>(gs_cl_smem + lay.ring);
   float* const Y1 = Y0 + (size_t)R * W;
   float* const Ysm = Y0 + 2 * (size_t)R * W;
@@ -309,7 +314,15 @@ __global__ void __launch_bounds__(1024, 1) k_gs_adj_cl(GsAdjArgs A) {
   cluster.sync();   // staging done; every block of the cluster runs before any remote read
   if (ntask <= nwarps) {
     // One task per warp (the usual shape): the warp's sweep and positions are
-    // fixed, its diagonal, column and ring row step down by one per step.
+    // fixed. With m > 0 the schedule stretches: sweep s of block r updates
+    // diagonal D0 - t + (2m + 3) s + m (C - 1 - r) at step t (upper blocks
+    // ahead, since this sweep reads position j + 1), so every value from
+    // another warp or block is at least m + 1 steps old and one cluster
+    // barrier every m + 1 steps orders them. This sweep's previous-step
+    // values travel in registers: (i+1, j) is this lane's last result,
+    // (i, j+1) lane l+1's (a shuffle; the strip's last position reads the
+    // upper block's pushed value).
+    const int m = A.m, Lg = 2 * m + 3;
     const int s = warp % K, j = jb + ((warp / K) << 5) + lane;
     const bool jok = warp < ntask && j <= je;
     float* const Yc = ((s & 1) ? Y1 : Y0) + (j - jb + 2);
@@ -318,30 +331,37 @@ __global__ void __launch_bounds__(1024, 1) k_gs_adj_cl(GsAdjArgs A) {
     const size_t boff = (s & 1) ? (size_t)R * W : 0;
     float* const plo = (jok && j == jb && Y0lo) ? Y0lo + boff + J + 2 : nullptr;
     float* const phi = (jok && j >= je - 1 && Y0hi) ? Y0hi + boff + (j - je + 1) : nullptr;
-    const bool jp1 = j + 1 <= N, jm1 = j - 1 >= 1, jm2 = j - 2 >= 1;
+    const bool jp1 = j + 1 <= N, jm1 = j - 1 >= 1, jm2 = j - 2 >= 1, jlast = j == je;
     const int RW = R * W;
-    int r0 = tb + 3 * s;
-    if (r0 >= R) r0 -= R;
-    int o0 = r0 * W;  // ring row of diagonal d = D0 - t + 3s
+    const int dtop = D0 + Lg * s + m * (C - 1 - r);  // this warp's diagonal at step 0
+    const int nst = (D0 - 2) + Lg * (K - 1) + m * (C - 1) + 1;
+    int o0 = (dtop % R) * W;
+    int i = dtop - j;
+    int bo = dtop * J + (j - jb);
+    const unsigned Nu = (unsigned)N;
+    float prev = 0.0f;
+    int cnt = m;
     // The last sweep's results go to global memory one step late, after the
     // next barrier, so that no barrier's release waits for an L2 write.
     size_t pend_q = 0;
     float pend_v = 0.0f, pend_sum = 0.0f;
     bool pend = false;
-    for (int t = 0; t < nsteps; ++t) {
+    for (int t = 0; t < nst; ++t, --i, bo -= J) {
       if (pend) {
         A.Ysum[pend_q] = pend_sum;
         A.yK[pend_q] = pend_v;
         pend = false;
       }
-      const int d = D0 - t + 3 * s, i = d - j;
-      if (jok && t >= 3 * s && i >= 1 && i <= N) {
+      const float dn = __shfl_down_sync(0xffffffffu, prev, 1);
+      if (jok && (unsigned)(i - 1) < Nu) {
+        const int d = i + j;
         const int op1 = o0 + W == RW ? 0 : o0 + W;
         const int om1 = o0 == 0 ? RW - W : o0 - W;
-        const int om2 = om1 == 0 ? RW - W : om1 - W;
-        float v = al * ((i < N ? Yc[op1] : 0.0f) + (jp1 ? Yc[op1 + 1] : 0.0f));
+        const float yr = i < N ? prev : 0.0f;                          // (i+1, j)
+        const float yd = jp1 ? (jlast ? Yc[op1 + 1] : dn) : 0.0f;       // (i, j+1)
+        float v = al * (yr + yd);
         if (s == 0) {
-          v += Bs[(size_t)d * J + (j - jb)];
+          v += Bs[bo];
         } else {
           const uint8_t cd = code_at(d, j);
           const bool written = (MODE == kRow)   ? (cd & kCodeRowMask) != 0
@@ -355,6 +375,7 @@ __global__ void __launch_bounds__(1024, 1) k_gs_adj_cl(GsAdjArgs A) {
               v += al * (float)n * Yp[o0];
             }
           } else if (cd & kCodeWall) {
+            const int om2 = om1 == 0 ? RW - W : om1 - W;
             if (MODE == kRow) {
               if (i > 1 && (code_at(d - 1, j) & kCodeRowRight))
                 v -= al * ((i > 2 ? Yp[om2] : 0.0f) + (jm1 ? Yp[om2 - 1] : 0.0f));
@@ -379,9 +400,13 @@ __global__ void __launch_bounds__(1024, 1) k_gs_adj_cl(GsAdjArgs A) {
           pend_sum = sum;
           pend = true;
         }
+        prev = v;
       }
       o0 = o0 == 0 ? RW - W : o0 - W;
-      cluster.sync();
+      if (--cnt < 0 || t == nst - 1) {
+        cluster.sync();  // also the last step: no remote store may follow a block's exit
+        cnt = m;
+      }
     }
     if (pend) {
       A.Ysum[pend_q] = pend_sum;

@@ -101,7 +101,7 @@ struct eq_fluid {
   int64_t cl_K = -1;  // sweep count the cluster check below was made for
   int cl_blocks = 0;  // blocks per cluster for cl_K, 0 = not applicable
   int cl_m = 0;       // its barrier interval - 1 (lscl.cuh)
-  int cl_mmax = 1;    // cap on cl_m (1: the fastest or within 3 % at N = 64..288, measured)
+  int cl_mmax = -1;   // cap on cl_m; -1: 2 for N >= 192, else 1 (the fastest, measured)
 
   size_t grid_elems() const { return (size_t)P * S; }
 };
@@ -226,7 +226,7 @@ int cluster_blocks(eq_fluid* h, int64_t K) {
       cudaSuccess)
     return 0;
   // the longest barrier interval whose band still fits
-  int m = h->cl_mmax;
+  int m = h->cl_mmax >= 0 ? h->cl_mmax : (N >= 192 ? 2 : 1);
   while (m > 0 && eqk::ls_cl_layout(S, (int)K, C, m).total > (size_t)optin) --m;
   const size_t bytes = eqk::ls_cl_layout(S, (int)K, C, m).total;
   if (bytes > (size_t)optin) return 0;

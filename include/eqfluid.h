@@ -428,6 +428,9 @@ int eq_grad_frames(const eq_grad* g, int64_t* recorded);
  * y and its running sum in shared memory, 1 = y only, 0 = global memory;
  * -1 restores the default. */
 int eq_grad_set_wavefront_storage(eq_grad* g, int max_store);
+/* Caps the cluster form's barrier interval at max_m + 1 steps (0..3, same
+ * default as the forward's), as eq_fluid_set_cluster_interval does there. */
+int eq_grad_set_cluster_interval(eq_grad* g, int max_m);
 /* The form the last transposed solve used (store as above) and its blocks. */
 int eq_grad_get_wavefront_storage(const eq_grad* g, int* store, int* cluster_blocks);
 /* With profiling on, every transposed Gauss-Seidel wavefront launch is
@@ -492,8 +495,8 @@ int eq_fluid_set_spin_limit(eq_fluid* h, int64_t iterations);
 int eq_fluid_set_solver(eq_fluid* h, int solver);
 int eq_fluid_get_solver(eq_fluid* h, int* cluster_blocks);
 /* Caps the cluster wavefront's barrier interval at max_m + 1 steps (0..3;
- * default 1; the longest interval up to the cap that fits in shared memory
- * is used). */
+ * by default 3 steps for N >= 192 and 2 below, the fastest measured; the
+ * longest interval up to the cap that fits in shared memory is used). */
 int eq_fluid_set_cluster_interval(eq_fluid* h, int max_m);
 
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their own

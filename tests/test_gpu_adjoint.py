@@ -83,6 +83,11 @@ def test_lin_solve_adj(eqlib, size, K, mode, store):
                                        float(a), float(c), size, K, of.cells)
     assert rel(gx, rx) < 1e-5, ("xb", rel(gx, rx))
     assert rel(gx0, rx0) < 1e-5, ("x0b", rel(gx0, rx0))
+    if store == 3:  # the cluster form with a barrier every 1 and every 4 steps
+        for max_m in (0, 3):
+            _lib.check(_lib.load().eq_grad_set_cluster_interval(g.handle, max_m))
+            hx, hx0 = g.lin_solve_adj(mode, xb, x0b, a, c)
+            assert rel(hx, rx) < 1e-5 and rel(hx0, rx0) < 1e-5, (max_m, rel(hx, rx))
     g.close()
     f.close()
 
