@@ -199,7 +199,31 @@ def run_batched_form(local_rank: int, frames: int, plain_sample: int = 12, stora
         out["plain_looped"] = {"value": pcells / (pms / 1e3), "unit": "cell-steps/s",
                                "sample": f"{plain_sample} scenes of the workload stepped one by "
                                          "one through eq_fluid (host clock, 2 frames each)"}
+    out["cpu_baseline"] = batch_cpu_baseline(cfgs, rects)
     return out
+
+
+def batch_cpu_baseline(cfgs, rects, nsample: int = 24, seed: int = 7):
+    """The reference's step on one host core (the oracle, f32) over a seeded
+    sample of the batch workload's scenes, one frame each: cell-steps/s of
+    the sample (the workload's sizes are log-uniform, so a uniform sample of
+    scenes is a fair sample of its cost per cell)."""
+    import oracle
+    rng = np.random.default_rng(seed)
+    pick = rng.choice(len(cfgs), size=nsample, replace=False)
+    cells, secs = 0, 0.0
+    for q in pick:
+        size, dt, k, dif, vis = cfgs[q]
+        r = oracle.OracleFluid(size, dt, k, dif, vis)
+        for rc in rects[q]:
+            r.fill_obstacle(*rc)
+        t = time.perf_counter()
+        r.step()
+        secs += time.perf_counter() - t
+        cells += (size - 2) ** 2
+    return {"value": cells / secs, "unit": "cell-steps/s", "cores": 1, "kind": "port",
+            "sample": f"{nsample} seeded scenes of the workload, one frame each, the oracle's "
+                      f"f32 step ({secs:.1f} s)"}
 
 
 def batch_half_errors(storage: str, nsample: int, local_rank: int, frames=(1, 3)):
@@ -340,12 +364,32 @@ def run_precision_form(local_rank: int, frames: int, size: int = PREC_SIZE,
                                                 g.read_field(3), g.stats()["div_norm"])
         timed = ms[1:frames + 1]
         t = statistics.mean(timed)
+        hbm, _ = peaks()
+        ach = BYTES_PER_CELL_FRAME_HALF * size * size / (t / 1e3) / 1e9
         out[storage] = {"value": (size - 2) ** 2 / (t / 1e3), "unit": "cell-steps/s",
+                        "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                                     "frac": ach / hbm,
+                                     "bytes_per_cell_frame": BYTES_PER_CELL_FRAME_HALF,
+                                     "note": "the fused-phase bytes of a frame with half fields; "
+                                             "the refinement rounds' own traffic is not counted"},
                         "ms_per_frame": t, "frames_timed": len(timed),
                         "clock": "host, per frame (the refinement loop reads its norms)",
                         "stats_last_frame": g.stats(),
                         "gpu_launches_per_frame": statistics.mean(launches[1:frames + 1])}
         g.close()
+    # the reference's step on one host core at this size (the oracle, f32), one frame
+    import oracle
+    r = oracle.OracleFluid(size, PREC_DT, ITERS, PREC_DIFF, PREC_VISC)
+    for rc in rects:
+        r.fill_obstacle(*rc)
+    oracle.add_sources(r, sx, sy, sd[0], su[0], sv[0])
+    t0 = time.perf_counter()
+    r.step()
+    tc = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": (size - 2) ** 2 / tc, "unit": "cell-steps/s", "cores": 1,
+                           "kind": "port",
+                           "sample": f"one frame of this workload, the oracle's f32 step "
+                                     f"({tc:.1f} s)"}
     if err_frames:
         t0 = time.perf_counter()
         for f in futs:

@@ -399,7 +399,7 @@ int eq_hfluid_launch_count(const eq_hfluid* h, uint64_t* count);
  * row breaks and clamps) as the recorded run took them. The handle's configs
  * and mask must not change between forward and backward (EQ_ERR_STATE);
  * backward leaves the handle in the forward's final state. */
-typedef struct eq_grad eq_grad; /* opaque; binds one eq_fluid */
+typedef struct eq_grad eq_grad; /* opaque; binds one eq_fluid, free it first */
 
 int eq_grad_new(eq_fluid* h, int64_t max_frames, int64_t checkpoint_every, eq_grad** out);
 int eq_grad_free(eq_grad* g); /* accepts NULL */
