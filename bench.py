@@ -525,6 +525,70 @@ def fd_check(grads, size, frames, ndirs=32, h=1e-3, workers=None):
     return out
 
 
+def concurrent_gradients(local_rank: int, size: int, frames: int, nscenes: int):
+    """nscenes independent gradients of the differentiation workload (seeds
+    11, 12, ...), each on its own handle and stream, driven from one host
+    thread each: one gradient's solves occupy a cluster of 8 SMs, so several
+    run side by side. Aggregate cell-steps/s over the wall time of all."""
+    import threading
+    import torch
+    from equilibrium_gb300 import _lib
+    from equilibrium_gb300.adjoint import Recorder
+    from equilibrium_gb300.simulation import Fluid, FluidConfigs, SimulationConfigs
+    L = _lib.load()
+    dev = torch.device("cuda", local_rank)
+    jobs = []
+    for q in range(nscenes):
+        rects, cells, init, src, target = diff_problem(size, frames, DIFF_SEED + q)
+        f = Fluid(FluidConfigs(DIFF_NU, DIFF_NU, False), SimulationConfigs(DIFF_DT, ITERS, size),
+                  device=local_rank)
+        for r in rects:
+            _lib.check(L.eq_fluid_fill_obstacle(f.handle, *r))
+        g = Recorder(f, frames, DIFF_EVERY)
+        n = size * size
+        jobs.append((f, g, init, torch.from_numpy(src).to(dev), target,
+                     torch.empty(6 * n, dtype=torch.float32, device=dev),
+                     torch.empty(frames * n, dtype=torch.float32, device=dev)))
+    errs = []
+
+    def one(job):
+        f, g, init, d_src, target, d_gi, d_gs = job
+        try:
+            _lib.check(L.eq_grad_forward_device(g.handle, frames, d_src.data_ptr()))
+            g.nframes = frames
+            g.l2_loss(target)
+            _lib.check(L.eq_grad_backward_device(g.handle, None, d_gi.data_ptr(), d_gs.data_ptr()))
+        except Exception as e:  # reported below
+            errs.append(repr(e))
+
+    def reset():
+        for f, g, init, *_ in jobs:
+            for k in range(6):
+                f.write_field(k, init[k])
+        torch.cuda.synchronize()
+
+    reset()
+    for job in jobs:  # warm-up, one at a time
+        one(job)
+    reset()
+    t0 = time.perf_counter()
+    th = [threading.Thread(target=one, args=(job,)) for job in jobs]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    wall = time.perf_counter() - t0
+    for f, g, *_ in jobs:
+        g.close()
+        f.close()
+    if errs:
+        return {"error": errs[0]}
+    return {"what": f"{nscenes} independent gradients (seeds {DIFF_SEED}..{DIFF_SEED + nscenes - 1}) "
+                    "on their own handles and streams, one host thread each",
+            "value": nscenes * (size - 2) ** 2 * frames / wall, "unit": "cell-steps/s",
+            "wall_s": wall, "clock": "host, all gradients (each ends with a synchronisation)"}
+
+
 def run_diff_form(local_rank: int, reps: int = 2, fd_dirs: int = 32, size: int = DIFF_SIZE,
                   frames: int = DIFF_FRAMES):
     """The differentiation form: one gradient evaluation = `frames` recorded
@@ -587,6 +651,7 @@ def run_diff_form(local_rank: int, reps: int = 2, fd_dirs: int = 32, size: int =
     _lib.check(L.eq_grad_set_profiling(g.handle, 0))
     gi = d_gi.view(6, n).cpu().numpy()
     gsrc = d_gs.view(frames, n).cpu().numpy()
+    concurrent = concurrent_gradients(local_rank, size, frames, 16)
     # variant: one segment (the forward keeps the whole tape, no recompute)
     gf = Recorder(f, frames, frames)
     full_ms = []
@@ -637,6 +702,7 @@ def run_diff_form(local_rank: int, reps: int = 2, fd_dirs: int = 32, size: int =
                    "h2d_bytes_per_gradient": frames * n * 4 + n * 4,
                    "d2h_bytes_per_gradient": (6 + frames) * n * 4 + 8},
            "loss": loss, "rerun_rel_diff": rerun,
+           "variant_concurrent": concurrent,
            "variant_full_tape": {
                "what": "checkpoint_every = frames: the forward keeps every frame's tape "
                        f"({frames * 5 * size * ((size + 31) // 32 * 32) * 4 / 1e6:.0f} MB), "
