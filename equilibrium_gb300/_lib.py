@@ -115,6 +115,7 @@ def load(path: str = LIB_PATH):
         "eq_fluid_launch_count": (i32, [H, ctypes.POINTER(ctypes.c_uint64)]),
         "eq_fluid_set_spin_limit": (i32, [H, i64]),
         "eq_fluid_set_solver": (i32, [H, i32]),
+        "eq_fluid_set_concurrency": (i32, [H, i32]),
         "eq_fluid_get_solver": (i32, [H, ctypes.POINTER(ctypes.c_int)]),
         "eq_fluid_set_cluster_interval": (i32, [H, i32]),
         "eq_fluid_get_stream": (i32, [H, PP]),

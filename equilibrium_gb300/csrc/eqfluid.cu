@@ -68,6 +68,23 @@ struct eq_fluid {
   unsigned* counters = nullptr;        // [0] ticket, [1] done
   uint32_t tag = 1;                    // next W(-1) tag (monotonic)
   int* err = nullptr;
+
+  // Concurrent phases of one step: two side streams (the vy diffusion and the
+  // density diffusion run beside the vx diffusion and the velocity pipeline),
+  // fork / join events, and the side solves' own wavefront state (slots 1, 2;
+  // slot 0 is wt / edge / counters / tag above). `cur` / `cur_slot` are the
+  // stream and slot the launch helpers use (the main stream and slot 0
+  // outside launch_step's side branches).
+  bool concurrent = true;
+  cudaStream_t cur = nullptr;
+  int cur_slot = 0;
+  cudaStream_t side[2] = {};
+  cudaEvent_t fork_ev = nullptr;
+  cudaEvent_t join_ev[2] = {};
+  unsigned long long* xwt[2] = {};
+  unsigned long long* xedge[2] = {};
+  unsigned* xcounters[2] = {};
+  uint32_t xtag[2] = {1, 1};
   long long spin_limit = kDefaultSpinLimit;
 
   // source staging
@@ -197,13 +214,13 @@ int launch_bnd(eq_fluid* h, int mode, float* x) {
   const dim3 grd = grid2d((int)h->S, (int)h->S, blk);
   switch (mode) {
     case eqk::kRow:
-      eqk::k_set_boundaries<eqk::kRow><<<grd, blk, 0, h->stream>>>(x, h->code, h->rowfl, h->colfl, (int)h->S, h->P);
+      eqk::k_set_boundaries<eqk::kRow><<<grd, blk, 0, h->cur>>>(x, h->code, h->rowfl, h->colfl, (int)h->S, h->P);
       break;
     case eqk::kCol:
-      eqk::k_set_boundaries<eqk::kCol><<<grd, blk, 0, h->stream>>>(x, h->code, h->rowfl, h->colfl, (int)h->S, h->P);
+      eqk::k_set_boundaries<eqk::kCol><<<grd, blk, 0, h->cur>>>(x, h->code, h->rowfl, h->colfl, (int)h->S, h->P);
       break;
     default:
-      eqk::k_set_boundaries<eqk::kPassive><<<grd, blk, 0, h->stream>>>(x, h->code, h->rowfl, h->colfl, (int)h->S, h->P);
+      eqk::k_set_boundaries<eqk::kPassive><<<grd, blk, 0, h->cur>>>(x, h->code, h->rowfl, h->colfl, (int)h->S, h->P);
       break;
   }
   return check_launch(h);
@@ -288,7 +305,7 @@ int launch_lin_solve_cluster(eq_fluid* h, int mode, float* x, const float* x0, f
   cfg.gridDim = dim3(C);
   cfg.blockDim = dim3(32 * (unsigned)K);
   cfg.dynamicSmemBytes = eqk::ls_cl_layout(S, K, C, A.m).total;
-  cfg.stream = h->stream;
+  cfg.stream = h->cur;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = C;
@@ -300,7 +317,7 @@ int launch_lin_solve_cluster(eq_fluid* h, int mode, float* x, const float* x0, f
   if (h->profiling) {
     EQ_CUDA(cudaEventCreate(&ev0));
     EQ_CUDA(cudaEventCreate(&ev1));
-    EQ_CUDA(cudaEventRecord(ev0, h->stream));
+    EQ_CUDA(cudaEventRecord(ev0, h->cur));
   }
   switch (mode) {
     case eqk::kRow:
@@ -316,7 +333,7 @@ int launch_lin_solve_cluster(eq_fluid* h, int mode, float* x, const float* x0, f
   int rc = check_launch(h);
   if (rc) return rc;
   if (h->profiling) {
-    EQ_CUDA(cudaEventRecord(ev1, h->stream));
+    EQ_CUDA(cudaEventRecord(ev1, h->cur));
     h->ls_events.emplace_back(ev0, ev1);
   }
   return launch_bnd(h, mode, x);
@@ -332,42 +349,48 @@ int launch_lin_solve(eq_fluid* h, int mode, float* x, const float* x0, float a, 
     if (C > 0) return launch_lin_solve_cluster(h, mode, x, x0, a, c_recip, C);
   }
   const int S = (int)h->S;
+  // this solve's wavefront state (slot 0 on the main stream, 1 / 2 on the side streams)
+  const int sl = h->cur_slot;
+  unsigned long long* const wt = sl ? h->xwt[sl - 1] : h->wt;
+  unsigned long long* const edge = sl ? h->xedge[sl - 1] : h->edge;
+  unsigned* const counters = sl ? h->xcounters[sl - 1] : h->counters;
+  uint32_t& tag = sl ? h->xtag[sl - 1] : h->tag;
   for (int64_t done = 0; done < K; done += kMaxSweepsPerLaunch) {
     const int Kc = (int)std::min<int64_t>(kMaxSweepsPerLaunch, K - done);
     if (h->graph_mode) {
       // A captured frame replays with the same tags: clear what a previous
       // replay left so that no stale word carries a current tag.
-      EQ_CUDA(cudaMemsetAsync(h->wt, 0, 2 * h->grid_elems() * 8, h->stream));
-      EQ_CUDA(cudaMemsetAsync(h->edge, 0, (size_t)h->B * kMaxSweepsPerLaunch * h->P * 8,
-                              h->stream));
+      EQ_CUDA(cudaMemsetAsync(wt, 0, 2 * h->grid_elems() * 8, h->cur));
+      EQ_CUDA(cudaMemsetAsync(edge, 0, (size_t)h->B * kMaxSweepsPerLaunch * h->P * 8,
+                              h->cur));
     }
-    if (h->tag > 0xF0000000u) {  // tags would wrap: restart from clean buffers
-      EQ_CUDA(cudaMemsetAsync(h->wt, 0, 2 * h->grid_elems() * 8, h->stream));
-      EQ_CUDA(cudaMemsetAsync(h->edge, 0, (size_t)h->B * kMaxSweepsPerLaunch * h->P * 8,
-                              h->stream));
-      h->tag = 1;
+    if (tag > 0xF0000000u) {  // tags would wrap: restart from clean buffers
+      EQ_CUDA(cudaMemsetAsync(wt, 0, 2 * h->grid_elems() * 8, h->cur));
+      EQ_CUDA(cudaMemsetAsync(edge, 0, (size_t)h->B * kMaxSweepsPerLaunch * h->P * 8,
+                              h->cur));
+      tag = 1;
     }
-    EQ_CUDA(cudaMemsetAsync(h->counters, 0, 2 * sizeof(unsigned), h->stream));
+    EQ_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned), h->cur));
     {
       const size_t n = h->grid_elems();
       const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
-      eqk::k_ls_tag_init<<<blocks, 256, 0, h->stream>>>(h->wt, x, n, h->tag);
+      eqk::k_ls_tag_init<<<blocks, 256, 0, h->cur>>>(wt, x, n, tag);
       int rc0 = check_launch(h);
       if (rc0) return rc0;
     }
     eqk::LinSolveArgs A;
     A.x = x;
-    A.wt[0] = h->wt;
-    A.wt[1] = h->wt + h->grid_elems();
-    A.tag0 = h->tag;
-    h->tag += (uint32_t)Kc + 1u;
+    A.wt[0] = wt;
+    A.wt[1] = wt + h->grid_elems();
+    A.tag0 = tag;
+    tag += (uint32_t)Kc + 1u;
     A.x0 = x0;
     A.code = h->code;
     A.rowfl = h->rowfl;
     A.colfl = h->colfl;
-    A.edge = h->edge;
-    A.ticket = h->counters;
-    A.done = h->counters + 1;
+    A.edge = edge;
+    A.ticket = counters;
+    A.done = counters + 1;
     A.err = h->err;
     A.spin_limit = h->spin_limit;
     A.S = S;
@@ -381,23 +404,23 @@ int launch_lin_solve(eq_fluid* h, int mode, float* x, const float* x0, float a, 
     if (h->profiling) {
       EQ_CUDA(cudaEventCreate(&ev0));
       EQ_CUDA(cudaEventCreate(&ev1));
-      EQ_CUDA(cudaEventRecord(ev0, h->stream));
+      EQ_CUDA(cudaEventRecord(ev0, h->cur));
     }
     switch (mode) {
       case eqk::kRow:
-        eqk::k_lin_solve<eqk::kRow><<<ntasks, 32, 0, h->stream>>>(A);
+        eqk::k_lin_solve<eqk::kRow><<<ntasks, 32, 0, h->cur>>>(A);
         break;
       case eqk::kCol:
-        eqk::k_lin_solve<eqk::kCol><<<ntasks, 32, 0, h->stream>>>(A);
+        eqk::k_lin_solve<eqk::kCol><<<ntasks, 32, 0, h->cur>>>(A);
         break;
       default:
-        eqk::k_lin_solve<eqk::kPassive><<<ntasks, 32, 0, h->stream>>>(A);
+        eqk::k_lin_solve<eqk::kPassive><<<ntasks, 32, 0, h->cur>>>(A);
         break;
     }
     int rc = check_launch(h);
     if (rc) return rc;
     if (h->profiling) {
-      EQ_CUDA(cudaEventRecord(ev1, h->stream));
+      EQ_CUDA(cudaEventRecord(ev1, h->cur));
       h->ls_events.emplace_back(ev0, ev1);
     }
   }
@@ -417,13 +440,13 @@ int launch_project(eq_fluid* h, float* vx, float* vy, float* p, float* div) {
   const int S = (int)h->S, N = S - 2;
   const dim3 blk(32, 8);
   const dim3 grd = grid2d(N, N, blk);
-  eqk::k_divergence<<<grd, blk, 0, h->stream>>>(vx, vy, p, div, S, h->P);
+  eqk::k_divergence<<<grd, blk, 0, h->cur>>>(vx, vy, p, div, S, h->P);
   int rc = check_launch(h);
   if (rc) return rc;
   if ((rc = launch_bnd(h, eqk::kPassive, div))) return rc;
   if ((rc = launch_bnd(h, eqk::kPassive, p))) return rc;
   if ((rc = launch_lin_solve(h, eqk::kPassive, p, div, 1.0f, 4.0f))) return rc;
-  eqk::k_gradient<<<grd, blk, 0, h->stream>>>(vx, vy, p, S, h->P);
+  eqk::k_gradient<<<grd, blk, 0, h->cur>>>(vx, vy, p, S, h->P);
   if ((rc = check_launch(h))) return rc;
   if ((rc = launch_bnd(h, eqk::kRow, vx))) return rc;
   return launch_bnd(h, eqk::kCol, vy);
@@ -435,7 +458,7 @@ int launch_advect(eq_fluid* h, int mode, float* d, const float* d0, const float*
   const int S = (int)h->S, N = S - 2;
   const float dt0 = h->dt * (float)(h->S - 2);
   const int threads = std::min(256, ((N + 31) / 32) * 32);
-  eqk::k_advect_rows<<<N, threads, 0, h->stream>>>(d, d0, u, v, S, h->P, dt0);
+  eqk::k_advect_rows<<<N, threads, 0, h->cur>>>(d, d0, u, v, S, h->P, dt0);
   int rc = check_launch(h);
   if (rc) return rc;
   return launch_bnd(h, mode, d);
@@ -445,7 +468,7 @@ int launch_copy(eq_fluid* h, float* dst, const float* src) {
   const size_t n4 = h->grid_elems() / 4;
   const int threads = 256;
   const int blocks = (int)std::min<size_t>((n4 + threads - 1) / threads, 152 * 16);
-  eqk::k_copy<<<blocks, threads, 0, h->stream>>>(dst, src, n4);
+  eqk::k_copy<<<blocks, threads, 0, h->cur>>>(dst, src, n4);
   return check_launch(h);
 }
 
@@ -459,13 +482,46 @@ int launch_step(eq_fluid* h) {
   float* vy = h->field[EQ_FIELD_VY];
   float* vx0 = h->field[EQ_FIELD_VX0];
   float* vy0 = h->field[EQ_FIELD_VY0];
+  if (!h->concurrent) {
+    if ((rc = launch_diffuse(h, eqk::kRow, vx0, vx, h->visc))) return rc;
+    if ((rc = launch_diffuse(h, eqk::kCol, vy0, vy, h->visc))) return rc;
+    if ((rc = launch_project(h, vx0, vy0, vx, vy))) return rc;
+    if ((rc = launch_advect(h, eqk::kRow, vx, vx0, vx0, vy0))) return rc;
+    if ((rc = launch_advect(h, eqk::kCol, vy, vy0, vx0, vy0))) return rc;
+    if ((rc = launch_project(h, vx, vy, vx0, vy0))) return rc;
+    if ((rc = launch_diffuse(h, eqk::kPassive, sc, de, h->diff))) return rc;
+    if ((rc = launch_advect(h, eqk::kPassive, de, sc, vx, vy))) return rc;
+    return launch_copy(h, sc, de);
+  }
+  // The same phases with the independent ones side by side (every solve is
+  // latency-bound and leaves most of the GPU idle): diffuse(vy0 <- vy) and
+  // diffuse(scratch <- density) touch nothing the vx diffusion or the
+  // velocity pipeline reads or writes until their joins, so the results are
+  // those of the sequence above, bit for bit.
+  EQ_CUDA(cudaEventRecord(h->fork_ev, h->stream));
+  EQ_CUDA(cudaStreamWaitEvent(h->side[0], h->fork_ev, 0));
+  EQ_CUDA(cudaStreamWaitEvent(h->side[1], h->fork_ev, 0));
+  auto on = [&](cudaStream_t st, int slot) {
+    h->cur = st;
+    h->cur_slot = slot;
+  };
+  on(h->side[0], 1);
+  rc = launch_diffuse(h, eqk::kCol, vy0, vy, h->visc);
+  if (!rc) rc = cudaEventRecord(h->join_ev[0], h->side[0]) == cudaSuccess ? EQ_OK : EQ_ERR_CUDA;
+  if (!rc) {
+    on(h->side[1], 2);
+    rc = launch_diffuse(h, eqk::kPassive, sc, de, h->diff);
+    if (!rc) rc = cudaEventRecord(h->join_ev[1], h->side[1]) == cudaSuccess ? EQ_OK : EQ_ERR_CUDA;
+  }
+  on(h->stream, 0);
+  if (rc) return rc == EQ_ERR_CUDA ? fail(EQ_ERR_CUDA, "side stream event") : rc;
   if ((rc = launch_diffuse(h, eqk::kRow, vx0, vx, h->visc))) return rc;
-  if ((rc = launch_diffuse(h, eqk::kCol, vy0, vy, h->visc))) return rc;
+  EQ_CUDA(cudaStreamWaitEvent(h->stream, h->join_ev[0], 0));
   if ((rc = launch_project(h, vx0, vy0, vx, vy))) return rc;
   if ((rc = launch_advect(h, eqk::kRow, vx, vx0, vx0, vy0))) return rc;
   if ((rc = launch_advect(h, eqk::kCol, vy, vy0, vx0, vy0))) return rc;
   if ((rc = launch_project(h, vx, vy, vx0, vy0))) return rc;
-  if ((rc = launch_diffuse(h, eqk::kPassive, sc, de, h->diff))) return rc;
+  EQ_CUDA(cudaStreamWaitEvent(h->stream, h->join_ev[1], 0));
   if ((rc = launch_advect(h, eqk::kPassive, de, sc, vx, vy))) return rc;
   return launch_copy(h, sc, de);
 }
@@ -490,6 +546,8 @@ void free_handle(eq_fluid* h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  for (int k = 0; k < 2; ++k)
+    if (h->side[k]) cudaStreamSynchronize(h->side[k]);
   for (auto& e : h->ls_events) {
     cudaEventDestroy(e.first);
     cudaEventDestroy(e.second);
@@ -506,6 +564,14 @@ void free_handle(eq_fluid* h) {
   cudaFree(h->edge);
   cudaFree(h->wt);
   cudaFree(h->counters);
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(h->xedge[k]);
+    cudaFree(h->xwt[k]);
+    cudaFree(h->xcounters[k]);
+    if (h->side[k]) cudaStreamDestroy(h->side[k]);
+    if (h->join_ev[k]) cudaEventDestroy(h->join_ev[k]);
+  }
+  if (h->fork_ev) cudaEventDestroy(h->fork_ev);
   cudaFree(h->err);
   cudaFree(h->d_src);
   if (h->h_src) cudaFreeHost(h->h_src);
@@ -551,6 +617,22 @@ int alloc_handle(uint32_t size, int device, eq_fluid** out) {
       cudaMemsetAsync(h->counters, 0, 2 * sizeof(unsigned), h->stream) != cudaSuccess ||
       cudaMemsetAsync(h->err, 0, sizeof(int), h->stream) != cudaSuccess)
     return bail(EQ_ERR_CUDA, "cudaMemsetAsync");
+  h->cur = h->stream;
+  if (cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming) != cudaSuccess)
+    return bail(EQ_ERR_CUDA, "cudaEventCreate");
+  for (int k = 0; k < 2; ++k) {
+    if (cudaStreamCreateWithFlags(&h->side[k], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->join_ev[k], cudaEventDisableTiming) != cudaSuccess)
+      return bail(EQ_ERR_CUDA, "cudaStreamCreate (side streams)");
+    if (cudaMalloc(&h->xedge[k], ntasks * h->P * 8) != cudaSuccess ||
+        cudaMalloc(&h->xwt[k], 2 * g * 8) != cudaSuccess ||
+        cudaMalloc(&h->xcounters[k], 2 * sizeof(unsigned)) != cudaSuccess)
+      return bail(EQ_ERR_OOM, "cudaMalloc (side wavefront state)");
+    if (cudaMemsetAsync(h->xwt[k], 0, 2 * g * 8, h->stream) != cudaSuccess ||
+        cudaMemsetAsync(h->xedge[k], 0, ntasks * h->P * 8, h->stream) != cudaSuccess ||
+        cudaMemsetAsync(h->xcounters[k], 0, 2 * sizeof(unsigned), h->stream) != cudaSuccess)
+      return bail(EQ_ERR_CUDA, "cudaMemsetAsync");
+  }
   h->host_cells.assign((size_t)size * size, 0);
   *out = h;
   return EQ_OK;
@@ -612,6 +694,8 @@ int read_err_word(eq_fluid* h) {
   if (e != 0) {
     // Leave the wavefront state clean for the next launch.
     EQ_CUDA(cudaMemsetAsync(h->counters, 0, 2 * sizeof(unsigned), h->stream));
+    for (int k = 0; k < 2; ++k)
+      EQ_CUDA(cudaMemsetAsync(h->xcounters[k], 0, 2 * sizeof(unsigned), h->stream));
     EQ_CUDA(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
     EQ_CUDA(cudaStreamSynchronize(h->stream));
     if (e == EQ_ERR_TIMEOUT)
@@ -764,6 +848,8 @@ int eq_fluid_synchronize(eq_fluid* h) {
   int rc = select_device(h);
   if (rc) return rc;
   EQ_CUDA(cudaStreamSynchronize(h->stream));
+  for (int k = 0; k < 2; ++k)  // joined into the main stream by every step; an
+    EQ_CUDA(cudaStreamSynchronize(h->side[k]));  // aborted step may have left work
   return read_err_word(h);
 }
 
@@ -1011,6 +1097,12 @@ int eq_fluid_kernel_stats(eq_fluid* h, int kernel, double* total_ms, uint64_t* l
   *total_ms = sum;
   *launches = h->ls_events.size();
   h->ls_events.clear();
+  return EQ_OK;
+}
+
+int eq_fluid_set_concurrency(eq_fluid* h, int enable) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  h->concurrent = enable != 0;
   return EQ_OK;
 }
 
