@@ -10,12 +10,19 @@ import os
 import shutil
 import subprocess
 import sys
+import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libeqfluid.so")
-SOURCES = ["eqfluid.cu"]
+# Translation units, compiled in parallel and linked into one library: the
+# main one (the C ABI, every kernel of the plain, precision, frame and
+# differentiation forms) and the batched frame kernel's instances, one unit
+# per storage format.
+UNITS = [("eqfluid.cu", ())] + [("batch_kernels.cu", (f"-DEQ_BATCH_STORE={st}",))
+                                for st in range(4)]
+SOURCES = sorted({u for u, _ in UNITS})
 HEADERS = ["common.cuh", "kernels.cuh", "linsolve.cuh", "noalloc.cu", "wave.cuh", "batch.cuh",
            "batch.cu", "half.cuh", "mg.cuh", "half.cu", "store.cuh",
            "frame.cuh", "frame.cu", "adjoint.cuh", "adjoint.cu", "lscl.cuh"]
@@ -24,9 +31,13 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: device FP stays un-contracted even outside the explicitly
 # rounded intrinsics; -ffp-contract=off does the same for host-side scalars
 # (diffusion coefficients, 1/c), which gcc on aarch64 would otherwise fuse.
+# -static-global-template-stub=false: the batched frame kernel's instances
+# are defined in batch_kernels.cu and launched from eqfluid.cu, so their host
+# stubs need external linkage (each instance exists in exactly one unit).
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fno-fast-math",
-              "-shared", "-cudart", "shared"]
+              "-static-global-template-stub=false"]
+LINK_FLAGS = ["-shared", "-cudart", "shared"]
 
 
 def nvcc() -> str:
@@ -53,13 +64,29 @@ def up_to_date() -> bool:
 def build(force: bool = False, verbose: bool = False, extra=()) -> str:
     if not force and up_to_date():
         return LIB
-    tmp = LIB + f".tmp{os.getpid()}"
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-o", tmp,
-           *[os.path.join(CSRC, s) for s in SOURCES]]
-    if verbose:
-        print(" ".join(cmd), file=sys.stderr)
-    subprocess.check_call(cmd)
-    os.replace(tmp, LIB)
+    tmpdir = tempfile.mkdtemp(prefix="eqfluid_build_")
+    try:
+        procs = []
+        objs = []
+        for q, (unit, defs) in enumerate(UNITS):
+            obj = os.path.join(tmpdir, f"u{q}.o")
+            cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *defs, *extra, "-c", "-o", obj,
+                   os.path.join(CSRC, unit)]
+            if verbose:
+                print(" ".join(cmd), file=sys.stderr)
+            procs.append((cmd, subprocess.Popen(cmd)))
+            objs.append(obj)
+        failed = [cmd for cmd, p in procs if p.wait() != 0]
+        if failed:
+            raise subprocess.CalledProcessError(1, failed[0])
+        tmp = LIB + f".tmp{os.getpid()}"
+        cmd = [nvcc(), *ARCH, *LINK_FLAGS, "-o", tmp, *objs]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        subprocess.check_call(cmd)
+        os.replace(tmp, LIB)
+    finally:
+        shutil.rmtree(tmpdir, ignore_errors=True)
     return LIB
 
 

@@ -496,4 +496,14 @@ __global__ void __launch_bounds__(672, 1) k_batch_run(BatchArgs A, BOpList L) {
   }
 }
 
+// The frame kernel's instances are compiled in batch_kernels.cu (one
+// translation unit per storage format, built in parallel); every other
+// includer only declares them.
+#ifndef EQ_BATCH_KERNELS_TU
+extern template __global__ void k_batch_run<float, float>(BatchArgs, BOpList);
+extern template __global__ void k_batch_run<__half, __half>(BatchArgs, BOpList);
+extern template __global__ void k_batch_run<__nv_bfloat16, __nv_bfloat16>(BatchArgs, BOpList);
+extern template __global__ void k_batch_run<float, __half>(BatchArgs, BOpList);
+#endif
+
 }  // namespace eqk

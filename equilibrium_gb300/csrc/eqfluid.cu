@@ -74,8 +74,9 @@ struct eq_fluid {
   // fork / join events, and the side solves' own wavefront state (slots 1, 2;
   // slot 0 is wt / edge / counters / tag above). `cur` / `cur_slot` are the
   // stream and slot the launch helpers use (the main stream and slot 0
-  // outside launch_step's side branches).
-  bool concurrent = true;
+  // outside launch_step's side branches). `concurrent`: which diffusions run
+  // on a side stream (EQ_CONC_* bits).
+  int concurrent = EQ_CONC_VY | EQ_CONC_DENSITY;
   cudaStream_t cur = nullptr;
   int cur_slot = 0;
   cudaStream_t side[2] = {};
@@ -498,30 +499,42 @@ int launch_step(eq_fluid* h) {
   // diffuse(scratch <- density) touch nothing the vx diffusion or the
   // velocity pipeline reads or writes until their joins, so the results are
   // those of the sequence above, bit for bit.
+  const bool sideVy = (h->concurrent & EQ_CONC_VY) != 0;
+  const bool sideDe = (h->concurrent & EQ_CONC_DENSITY) != 0;
   EQ_CUDA(cudaEventRecord(h->fork_ev, h->stream));
-  EQ_CUDA(cudaStreamWaitEvent(h->side[0], h->fork_ev, 0));
-  EQ_CUDA(cudaStreamWaitEvent(h->side[1], h->fork_ev, 0));
   auto on = [&](cudaStream_t st, int slot) {
     h->cur = st;
     h->cur_slot = slot;
   };
-  on(h->side[0], 1);
-  rc = launch_diffuse(h, eqk::kCol, vy0, vy, h->visc);
-  if (!rc) rc = cudaEventRecord(h->join_ev[0], h->side[0]) == cudaSuccess ? EQ_OK : EQ_ERR_CUDA;
-  if (!rc) {
+  if (sideVy) {
+    EQ_CUDA(cudaStreamWaitEvent(h->side[0], h->fork_ev, 0));
+    on(h->side[0], 1);
+    rc = launch_diffuse(h, eqk::kCol, vy0, vy, h->visc);
+    if (!rc && cudaEventRecord(h->join_ev[0], h->side[0]) != cudaSuccess) rc = EQ_ERR_CUDA;
+    on(h->stream, 0);
+    if (rc) return rc == EQ_ERR_CUDA ? fail(EQ_ERR_CUDA, "side stream event") : rc;
+  }
+  if (sideDe) {
+    EQ_CUDA(cudaStreamWaitEvent(h->side[1], h->fork_ev, 0));
     on(h->side[1], 2);
     rc = launch_diffuse(h, eqk::kPassive, sc, de, h->diff);
-    if (!rc) rc = cudaEventRecord(h->join_ev[1], h->side[1]) == cudaSuccess ? EQ_OK : EQ_ERR_CUDA;
+    if (!rc && cudaEventRecord(h->join_ev[1], h->side[1]) != cudaSuccess) rc = EQ_ERR_CUDA;
+    on(h->stream, 0);
+    if (rc) return rc == EQ_ERR_CUDA ? fail(EQ_ERR_CUDA, "side stream event") : rc;
   }
-  on(h->stream, 0);
-  if (rc) return rc == EQ_ERR_CUDA ? fail(EQ_ERR_CUDA, "side stream event") : rc;
   if ((rc = launch_diffuse(h, eqk::kRow, vx0, vx, h->visc))) return rc;
-  EQ_CUDA(cudaStreamWaitEvent(h->stream, h->join_ev[0], 0));
+  if (sideVy)
+    EQ_CUDA(cudaStreamWaitEvent(h->stream, h->join_ev[0], 0));
+  else if ((rc = launch_diffuse(h, eqk::kCol, vy0, vy, h->visc)))
+    return rc;
   if ((rc = launch_project(h, vx0, vy0, vx, vy))) return rc;
   if ((rc = launch_advect(h, eqk::kRow, vx, vx0, vx0, vy0))) return rc;
   if ((rc = launch_advect(h, eqk::kCol, vy, vy0, vx0, vy0))) return rc;
   if ((rc = launch_project(h, vx, vy, vx0, vy0))) return rc;
-  EQ_CUDA(cudaStreamWaitEvent(h->stream, h->join_ev[1], 0));
+  if (sideDe)
+    EQ_CUDA(cudaStreamWaitEvent(h->stream, h->join_ev[1], 0));
+  else if ((rc = launch_diffuse(h, eqk::kPassive, sc, de, h->diff)))
+    return rc;
   if ((rc = launch_advect(h, eqk::kPassive, de, sc, vx, vy))) return rc;
   return launch_copy(h, sc, de);
 }
@@ -1100,9 +1113,11 @@ int eq_fluid_kernel_stats(eq_fluid* h, int kernel, double* total_ms, uint64_t* l
   return EQ_OK;
 }
 
-int eq_fluid_set_concurrency(eq_fluid* h, int enable) {
+int eq_fluid_set_concurrency(eq_fluid* h, int mask) {
   if (!h) return fail(EQ_ERR_ARG, "null handle");
-  h->concurrent = enable != 0;
+  if (mask < 0 || mask > (EQ_CONC_VY | EQ_CONC_DENSITY))
+    return fail(EQ_ERR_ARG, "concurrency mask must be in [0, 3]");
+  h->concurrent = mask;
   return EQ_OK;
 }
 

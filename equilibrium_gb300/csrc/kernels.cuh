@@ -82,7 +82,7 @@ __global__ void k_set_boundaries(float* __restrict__ x, const uint8_t* __restric
 // ---------------------------------------------------------------------------
 // project (fluid.rs:330-375): divergence + zero pressure on the interior ...
 // ---------------------------------------------------------------------------
-__global__ void k_divergence(const float* __restrict__ vx, const float* __restrict__ vy,
+static __global__ void k_divergence(const float* __restrict__ vx, const float* __restrict__ vy,
                              float* __restrict__ p, float* __restrict__ div, int S, int P) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -95,7 +95,7 @@ __global__ void k_divergence(const float* __restrict__ vx, const float* __restri
 }
 
 // ... and the gradient subtraction (fluid.rs:364-371), interior incl. walls.
-__global__ void k_gradient(float* __restrict__ vx, float* __restrict__ vy,
+static __global__ void k_gradient(float* __restrict__ vx, float* __restrict__ vy,
                            const float* __restrict__ p, int S, int P) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -153,7 +153,7 @@ __device__ __forceinline__ float bilerp(const Backtrace& b, const float* __restr
               fmul(b.s1, fadd(fmul(b.t0, C), fmul(b.t1, D))));
 }
 
-__global__ void k_advect_rows(float* __restrict__ d, const float* __restrict__ d0,
+static __global__ void k_advect_rows(float* __restrict__ d, const float* __restrict__ d0,
                               const float* __restrict__ u, const float* __restrict__ v,
                               int S, int P, float dt0) {
   const int j = blockIdx.x + 1;
@@ -194,7 +194,7 @@ __global__ void k_advect_rows(float* __restrict__ d, const float* __restrict__ d
 // Sources (add_density / add_velocity, fluid.rs:120-131), applied serially in
 // array order so repeated cells accumulate in the reference's order.
 // ---------------------------------------------------------------------------
-__global__ void k_sources(float* __restrict__ density, float* __restrict__ scratch,
+static __global__ void k_sources(float* __restrict__ density, float* __restrict__ scratch,
                           float* __restrict__ vx, float* __restrict__ vy, int S, int P,
                           int64_t n, const uint32_t* __restrict__ xs,
                           const uint32_t* __restrict__ ys, const float* __restrict__ dd,
@@ -214,7 +214,7 @@ __global__ void k_sources(float* __restrict__ density, float* __restrict__ scrat
 }
 
 // scratch_space = density.clone() (fluid.rs:523) over the whole pitched grid.
-__global__ void k_copy(float* __restrict__ dst, const float* __restrict__ src, size_t n4) {
+static __global__ void k_copy(float* __restrict__ dst, const float* __restrict__ src, size_t n4) {
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   const float4* s = reinterpret_cast<const float4*>(src);

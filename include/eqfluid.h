@@ -487,11 +487,13 @@ int eq_fluid_launch_count(const eq_fluid* h, uint64_t* count);
  * cannot complete end with EQ_ERR_TIMEOUT sooner. */
 int eq_fluid_set_spin_limit(eq_fluid* h, int64_t iterations);
 
-/* step() runs its independent phases side by side by default (the vy and the
- * density diffusions on two side streams of the handle, joined before their
- * results are read; bit-exact, the same kernels in the same data order).
- * 0 = one stream, in the reference's order. */
-int eq_fluid_set_concurrency(eq_fluid* h, int enable);
+/* step() can run its independent phases side by side: EQ_CONC_VY puts the
+ * vy diffusion, EQ_CONC_DENSITY the density diffusion on a side stream of the
+ * handle, joined before its result is read (bit-exact: the same kernels on
+ * the same data). 0 = one stream, in the reference's order. Default: both. */
+#define EQ_CONC_VY 1
+#define EQ_CONC_DENSITY 2
+int eq_fluid_set_concurrency(eq_fluid* h, int mask);
 
 /* Which kernel runs lin_solve: 0 (default) = the thread-block-cluster
  * wavefront where it applies (sizes with 32 < N <= ~300 and <= 32 sweeps;

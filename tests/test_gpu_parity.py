@@ -132,6 +132,25 @@ def test_full_step_random_state(eqlib, layout, size, iters, frames):
     p.close()
 
 
+@pytest.mark.parametrize("mask", [0, 1, 2, 3])
+@pytest.mark.parametrize("solver", [0, 1])
+@pytest.mark.parametrize("size", [66, 258])
+def test_full_step_concurrency_masks(eqlib, mask, solver, size):
+    """step() with the vy and / or the density diffusion on side streams
+    (EQ_CONC_* bits) under both lin_solve kernels: the reference's frames."""
+    rng = np.random.default_rng(size + mask)
+    p = Pair(size, 20, dt=0.1, diff=1e-3, visc=2e-3, rects=LAYOUTS["random4"](rng, size),
+             seed=size + 7 * mask, vel_scale=2.0)
+    assert L().eq_fluid_set_concurrency(p.gpu.handle, mask) == 0
+    assert L().eq_fluid_set_solver(p.gpu.handle, solver) == 0
+    for fr in range(3):
+        p.gpu.step()
+        p.ref.step()
+        p.compare(f"step {fr} mask={mask} solver={solver} size={size}")
+    assert L().eq_fluid_set_concurrency(p.gpu.handle, 4) != 0
+    p.close()
+
+
 def test_frames_zero_is_identity(eqlib):
     """frames = 0: lin_solve runs no sweep and no set_boundaries."""
     p = Pair(30, 0, seed=1)
