@@ -1080,6 +1080,14 @@ def run_ours(args):
                 "algorithmic_bytes_per_launch": BYTES_PER_CELL_LINSOLVE * SIZE * SIZE,
                 "launches_timed": int(ls_n.value), "avg_launch_ms": avg_ls * 1e3,
                 "share_of_step": (ls_ms.value / (dev_s / world * 1e3)) if dev_s else None,
+                "overlap": ("step() runs the vy and the density diffusions on two side "
+                            "streams, so up to three solves overlap: each launch's event "
+                            "time includes the others' contention and share_of_step sums "
+                            "overlapping intervals"),
+                # every solve's algorithmic bytes of one step over the step time
+                "aggregate_achieved": (BYTES_PER_CELL_LINSOLVE * SIZE * SIZE
+                                       * (ls_n.value / max(args.steps, 1))
+                                       / (ms_per_step / 1e3) / 1e9),
                 "frame_roofline_frac": (BYTES_PER_CELL_FRAME * SIZE * SIZE /
                                         (ms_per_step / 1e3) / 1e9 / hbm),
                 "traffic_source": traffic_src}
