@@ -506,6 +506,8 @@ int launch_step(eq_fluid* h) {
     h->cur = st;
     h->cur_slot = slot;
   };
+  // the critical path's solve first, then the side solves
+  if ((rc = launch_diffuse(h, eqk::kRow, vx0, vx, h->visc))) return rc;
   if (sideVy) {
     EQ_CUDA(cudaStreamWaitEvent(h->side[0], h->fork_ev, 0));
     on(h->side[0], 1);
@@ -522,7 +524,6 @@ int launch_step(eq_fluid* h) {
     on(h->stream, 0);
     if (rc) return rc == EQ_ERR_CUDA ? fail(EQ_ERR_CUDA, "side stream event") : rc;
   }
-  if ((rc = launch_diffuse(h, eqk::kRow, vx0, vx, h->visc))) return rc;
   if (sideVy)
     EQ_CUDA(cudaStreamWaitEvent(h->stream, h->join_ev[0], 0));
   else if ((rc = launch_diffuse(h, eqk::kCol, vy0, vy, h->visc)))
@@ -606,7 +607,16 @@ int alloc_handle(uint32_t size, int device, eq_fluid** out) {
     free_handle(h);
     return fail(code, what);
   };
-  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+  // Stream priorities: the main stream and the vy side stream carry the
+  // step's critical path (both feed the first project); the density side
+  // stream is only joined before the last advect, so its blocks are
+  // dispatched after theirs.
+  int prio_low = 0, prio_high = 0;
+  if (cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high) != cudaSuccess) {
+    cudaGetLastError();
+    prio_low = prio_high = 0;
+  }
+  if (cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, prio_high) != cudaSuccess)
     return bail(EQ_ERR_CUDA, "cudaStreamCreate");
   if (cudaEventCreateWithFlags(&h->src_ev, cudaEventDisableTiming) != cudaSuccess)
     return bail(EQ_ERR_CUDA, "cudaEventCreate");
@@ -634,7 +644,8 @@ int alloc_handle(uint32_t size, int device, eq_fluid** out) {
   if (cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming) != cudaSuccess)
     return bail(EQ_ERR_CUDA, "cudaEventCreate");
   for (int k = 0; k < 2; ++k) {
-    if (cudaStreamCreateWithFlags(&h->side[k], cudaStreamNonBlocking) != cudaSuccess ||
+    if (cudaStreamCreateWithPriority(&h->side[k], cudaStreamNonBlocking,
+                                     k == 0 ? prio_high : prio_low) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->join_ev[k], cudaEventDisableTiming) != cudaSuccess)
       return bail(EQ_ERR_CUDA, "cudaStreamCreate (side streams)");
     if (cudaMalloc(&h->xedge[k], ntasks * h->P * 8) != cudaSuccess ||
