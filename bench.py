@@ -1075,7 +1075,9 @@ def run_ours(args):
     traffic, traffic_src = profile_traffic()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
-                "kernel": "k_lin_solve (persistent temporal-wavefront Gauss-Seidel)",
+                "kernel": ("lin_solve: k_lin_solve (multi-block temporal wavefront, the "
+                           "three solves on the critical path) and k_ls_cs (cluster "
+                           "wavefront, strips streamed; the two side-stream diffusions)"),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": BYTES_PER_CELL_LINSOLVE * SIZE * SIZE,
                 "launches_timed": int(ls_n.value), "avg_launch_ms": avg_ls * 1e3,

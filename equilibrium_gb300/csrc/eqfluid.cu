@@ -21,6 +21,7 @@
 #include "kernels.cuh"
 #include "linsolve.cuh"
 #include "lscl.cuh"
+#include "lscs.cuh"
 
 namespace {
 
@@ -119,6 +120,12 @@ struct eq_fluid {
   int64_t cl_K = -1;  // sweep count the cluster check below was made for
   int cl_blocks = 0;  // blocks per cluster for cl_K, 0 = not applicable
   int cl_m = 0;       // its barrier interval - 1 (lscl.cuh)
+  int cl_kind = 0;    // 1: strips staged whole (k_ls_cl), 2: streamed (k_ls_cs)
+  int cl_H = 1;       // positions per lane of the streamed form
+  // the streamed form's strip-ordered codes, one copy per mode (lscs.cuh),
+  // rebuilt with the mask; allocated where the streamed form can apply
+  uint8_t* cs_strip = nullptr;
+  int cs_C = 0, cs_J = 0;
   int cl_mmax = -1;   // cap on cl_m; -1: 2 for N >= 192, else 1 (the fastest, measured)
 
   size_t grid_elems() const { return (size_t)P * S; }
@@ -193,6 +200,18 @@ int upload_mask(eq_fluid* h) {
                           h->stream));
   EQ_CUDA(cudaMemcpyAsync(h->rowfl, rowfl.data(), S, cudaMemcpyHostToDevice, h->stream));
   EQ_CUDA(cudaMemcpyAsync(h->colfl, colfl.data(), S, cudaMemcpyHostToDevice, h->stream));
+  if (h->cs_strip) {  // the streamed cluster solver's strip-ordered codes, per mode
+    const size_t sb = eqk::ls_cs_strip_bytes(S, h->cs_C, h->cs_J);
+    const int blocks = (int)std::min<size_t>((sb + 255) / 256, 152 * 8);
+    eqk::k_ls_cs_codes<eqk::kRow><<<blocks, 256, 0, h->stream>>>(h->cs_strip, h->code, S, P,
+                                                                  h->cs_C, h->cs_J);
+    eqk::k_ls_cs_codes<eqk::kCol><<<blocks, 256, 0, h->stream>>>(h->cs_strip + sb, h->code, S,
+                                                                  P, h->cs_C, h->cs_J);
+    eqk::k_ls_cs_codes<eqk::kPassive><<<blocks, 256, 0, h->stream>>>(
+        h->cs_strip + 2 * sb, h->code, S, P, h->cs_C, h->cs_J);
+    h->launches += 3;
+    EQ_CUDA(cudaGetLastError());
+  }
   // The staging vectors are pageable: the async copies above are staged
   // synchronously, but wait anyway before they go out of scope.
   EQ_CUDA(cudaStreamSynchronize(h->stream));
@@ -231,42 +250,83 @@ int launch_bnd(eq_fluid* h, int mode, float* x) {
 // sweep count, or 0 where it does not apply: one warp per sweep (K <= 32),
 // strips of 16 to 32 positions, the staged strip and band within the opt-in
 // shared memory, and a device that can hold the cluster.
+// Raises the dynamic shared memory limit and allows 16-block clusters for a
+// set of cluster kernels, once per device (bit `set` of a per-device mask).
+bool raise_cluster_attrs(int device, int set, const void* const* fns, int nfn, int optin) {
+  static std::atomic<uint64_t> raised[4];
+  const uint64_t bit = device < 64 ? (1ull << device) : 0ull;
+  if (bit && (raised[set].load() & bit)) return true;
+  for (int q = 0; q < nfn; ++q)
+    if (cudaFuncSetAttribute(fns[q], cudaFuncAttributeMaxDynamicSharedMemorySize, optin) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(fns[q], cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+            cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+  raised[set].fetch_or(bit);
+  return true;
+}
+
+// Blocks per cluster of the cluster wavefront for K sweeps (0: it does not
+// apply). Strips of J <= 32 positions whose x0, initial x and codes fit in
+// shared memory whole use k_ls_cl (lscl.cuh); otherwise strips of J <= 64
+// stream them (k_ls_cs, lscs.cuh). Either needs a cluster of C <= 16 blocks
+// that can be resident.
 int cluster_blocks(eq_fluid* h, int64_t K) {
   if (h->cl_K == K) return h->cl_blocks;
   h->cl_K = K;
   h->cl_blocks = 0;
+  h->cl_kind = 0;
   const int S = (int)h->S, N = S - 2;
   if (K < 1 || K > 32 || N < 32) return 0;
   const int C = std::min(16, (N + 31) / 32), J = (N + C - 1) / C;
-  if (C < 2 || J > 32 || J < 16 || (C - 1) * J >= N) return 0;
+  if (C < 2 || J > 64 || J < 16 || (C - 1) * J >= N) return 0;
   int optin = 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device) !=
       cudaSuccess)
     return 0;
-  // the longest barrier interval whose band still fits
-  int m = h->cl_mmax >= 0 ? h->cl_mmax : (N >= 192 ? 2 : 1);
-  while (m > 0 && eqk::ls_cl_layout(S, (int)K, C, m).total > (size_t)optin) --m;
-  const size_t bytes = eqk::ls_cl_layout(S, (int)K, C, m).total;
-  if (bytes > (size_t)optin) return 0;
-  h->cl_m = m;
-  static std::atomic<uint64_t> raised{0};
-  const uint64_t bit = h->device < 64 ? (1ull << h->device) : 0ull;
-  if (!bit || !(raised.load() & bit)) {
-    const void* fns[3] = {(const void*)eqk::k_ls_cl<eqk::kRow>, (const void*)eqk::k_ls_cl<eqk::kCol>,
-                          (const void*)eqk::k_ls_cl<eqk::kPassive>};
-    for (const void* fn : fns)
-      if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) !=
-              cudaSuccess ||
-          cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
-              cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-      }
-    raised.fetch_or(bit);
+  const int mcap = h->cl_mmax >= 0 ? h->cl_mmax : (N >= 192 ? 2 : 1);
+  int kind = 0, m = 0, H = 1;
+  size_t bytes = 0;
+  if (J <= 32) {  // the longest barrier interval whose strips still fit whole
+    m = mcap;
+    while (m > 0 && eqk::ls_cl_layout(S, (int)K, C, m).total > (size_t)optin) --m;
+    bytes = eqk::ls_cl_layout(S, (int)K, C, m).total;
+    if (bytes <= (size_t)optin) kind = 1;
   }
+  if (!kind && h->cs_strip && h->cs_C == C && h->cs_J == J && K <= 31) {
+    // the streamed rings' bound holds for m <= 3; 3 is the fastest measured
+    m = h->cl_mmax >= 0 ? std::min(h->cl_mmax, 3) : 3;
+    while (m > 0 && eqk::ls_cs_layout(S, (int)K, C, m).total > (size_t)optin) --m;
+    bytes = eqk::ls_cs_layout(S, (int)K, C, m).total;
+    if (bytes <= (size_t)optin) {
+      kind = 2;
+      H = J > 32 ? 2 : 1;
+    }
+  }
+  if (!kind) return 0;
+  const void* fns[3];
+  int set = 0;
+  if (kind == 1) {
+    fns[0] = (const void*)eqk::k_ls_cl<eqk::kRow>;
+    fns[1] = (const void*)eqk::k_ls_cl<eqk::kCol>;
+    fns[2] = (const void*)eqk::k_ls_cl<eqk::kPassive>;
+  } else if (H == 1) {
+    set = 1;
+    fns[0] = (const void*)eqk::k_ls_cs<eqk::kRow, 1>;
+    fns[1] = (const void*)eqk::k_ls_cs<eqk::kCol, 1>;
+    fns[2] = (const void*)eqk::k_ls_cs<eqk::kPassive, 1>;
+  } else {
+    set = 2;
+    fns[0] = (const void*)eqk::k_ls_cs<eqk::kRow, 2>;
+    fns[1] = (const void*)eqk::k_ls_cs<eqk::kCol, 2>;
+    fns[2] = (const void*)eqk::k_ls_cs<eqk::kPassive, 2>;
+  }
+  if (!raise_cluster_attrs(h->device, set, fns, 3, optin)) return 0;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(C);
-  cfg.blockDim = dim3(32 * (unsigned)K);
+  cfg.blockDim = dim3(32 * (unsigned)(kind == 1 ? K : K + 1));
   cfg.dynamicSmemBytes = bytes;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -276,10 +336,12 @@ int cluster_blocks(eq_fluid* h, int64_t K) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int nclusters = 0;
-  if (cudaOccupancyMaxActiveClusters(&nclusters, eqk::k_ls_cl<eqk::kPassive>, &cfg) ==
-          cudaSuccess &&
-      nclusters >= 1)
+  if (cudaOccupancyMaxActiveClusters(&nclusters, fns[2], &cfg) == cudaSuccess && nclusters >= 1) {
     h->cl_blocks = C;
+    h->cl_kind = kind;
+    h->cl_H = H;
+    h->cl_m = m;
+  }
   cudaGetLastError();
   return h->cl_blocks;
 }
@@ -289,6 +351,7 @@ int launch_lin_solve_cluster(eq_fluid* h, int mode, float* x, const float* x0, f
                              float c_recip, int C) {
   const int S = (int)h->S;
   const int K = (int)h->frames;
+  const bool streamed = h->cl_kind == 2;
   eqk::LsClArgs A;
   A.x = x;
   A.x0 = x0;
@@ -302,10 +365,13 @@ int launch_lin_solve_cluster(eq_fluid* h, int mode, float* x, const float* x0, f
   A.R = eqk::ls_cl_rows(K, A.m);
   A.a = a;
   A.cr = c_recip;
+  A.strip = streamed ? h->cs_strip + (size_t)mode * eqk::ls_cs_strip_bytes(S, h->cs_C, h->cs_J)
+                     : nullptr;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(C);
-  cfg.blockDim = dim3(32 * (unsigned)K);
-  cfg.dynamicSmemBytes = eqk::ls_cl_layout(S, K, C, A.m).total;
+  cfg.blockDim = dim3(32 * (unsigned)(streamed ? K + 1 : K));
+  cfg.dynamicSmemBytes = streamed ? eqk::ls_cs_layout(S, K, C, A.m).total
+                                  : eqk::ls_cl_layout(S, K, C, A.m).total;
   cfg.stream = h->cur;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -320,16 +386,42 @@ int launch_lin_solve_cluster(eq_fluid* h, int mode, float* x, const float* x0, f
     EQ_CUDA(cudaEventCreate(&ev1));
     EQ_CUDA(cudaEventRecord(ev0, h->cur));
   }
-  switch (mode) {
-    case eqk::kRow:
-      EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cl<eqk::kRow>, A));
-      break;
-    case eqk::kCol:
-      EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cl<eqk::kCol>, A));
-      break;
-    default:
-      EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cl<eqk::kPassive>, A));
-      break;
+  if (!streamed) {
+    switch (mode) {
+      case eqk::kRow:
+        EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cl<eqk::kRow>, A));
+        break;
+      case eqk::kCol:
+        EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cl<eqk::kCol>, A));
+        break;
+      default:
+        EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cl<eqk::kPassive>, A));
+        break;
+    }
+  } else if (h->cl_H == 1) {
+    switch (mode) {
+      case eqk::kRow:
+        EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cs<eqk::kRow, 1>, A));
+        break;
+      case eqk::kCol:
+        EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cs<eqk::kCol, 1>, A));
+        break;
+      default:
+        EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cs<eqk::kPassive, 1>, A));
+        break;
+    }
+  } else {
+    switch (mode) {
+      case eqk::kRow:
+        EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cs<eqk::kRow, 2>, A));
+        break;
+      case eqk::kCol:
+        EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cs<eqk::kCol, 2>, A));
+        break;
+      default:
+        EQ_CUDA(cudaLaunchKernelEx(&cfg, eqk::k_ls_cs<eqk::kPassive, 2>, A));
+        break;
+    }
   }
   int rc = check_launch(h);
   if (rc) return rc;
@@ -346,8 +438,14 @@ int launch_lin_solve(eq_fluid* h, int mode, float* x, const float* x0, float a, 
   if (K <= 0) return EQ_OK;
   const float c_recip = 1.0f / c;  // fluid.rs:311, IEEE f32 division
   if (h->solver != 1) {
+    // The staged cluster form is the fastest kernel where it applies. The
+    // streamed one is slower alone than the multi-block wavefront but holds
+    // only C SMs, so by default it takes the side-stream solves of step()
+    // (beside the multi-block solve of the critical path); solver 2 uses it
+    // for every solve.
     const int C = cluster_blocks(h, K);
-    if (C > 0) return launch_lin_solve_cluster(h, mode, x, x0, a, c_recip, C);
+    if (C > 0 && (h->cl_kind == 1 || h->cur_slot != 0 || h->solver == 2))
+      return launch_lin_solve_cluster(h, mode, x, x0, a, c_recip, C);
   }
   const int S = (int)h->S;
   // this solve's wavefront state (slot 0 on the main stream, 1 / 2 on the side streams)
@@ -573,6 +671,7 @@ void free_handle(eq_fluid* h) {
   cudaFree(h->block);
   cudaFree(h->cells);
   cudaFree(h->code);
+  cudaFree(h->cs_strip);
   cudaFree(h->rowfl);
   cudaFree(h->colfl);
   cudaFree(h->edge);
@@ -627,6 +726,18 @@ int alloc_handle(uint32_t size, int device, eq_fluid** out) {
   if (cudaMalloc(&h->cells, g) != cudaSuccess || cudaMalloc(&h->code, g) != cudaSuccess ||
       cudaMalloc(&h->rowfl, size) != cudaSuccess || cudaMalloc(&h->colfl, size) != cudaSuccess)
     return bail(EQ_ERR_OOM, "cudaMalloc (mask)");
+  {
+    // strips of the cluster wavefront: 16-64 positions per block, at most 16
+    // blocks; grids from N = 128 may need the streamed form (lscs.cuh)
+    const int N = (int)size - 2;
+    const int C = std::min(16, (N + 31) / 32), J = C > 0 ? (N + C - 1) / C : 0;
+    if (N >= 128 && C >= 2 && J >= 16 && J <= 64 && (C - 1) * J < N) {
+      h->cs_C = C;
+      h->cs_J = J;
+      if (cudaMalloc(&h->cs_strip, 3 * eqk::ls_cs_strip_bytes((int)size, C, J)) != cudaSuccess)
+        return bail(EQ_ERR_OOM, "cudaMalloc (cluster strip codes)");
+    }
+  }
   h->B = strips_for((int)size, kMaxSweepsPerLaunch);
   const size_t ntasks = (size_t)h->B * kMaxSweepsPerLaunch;
   if (cudaMalloc(&h->edge, ntasks * h->P * 8) != cudaSuccess ||
@@ -1152,6 +1263,14 @@ int eq_fluid_get_solver(eq_fluid* h, int* cluster_blocks_out) {
   int rc = select_device(h);
   if (rc) return rc;
   *cluster_blocks_out = h->solver == 1 ? 0 : cluster_blocks(h, h->frames);
+  return EQ_OK;
+}
+
+int eq_fluid_get_cluster_form(eq_fluid* h, int* form) {
+  if (!h || !form) return fail(EQ_ERR_ARG, "null argument");
+  int rc = select_device(h);
+  if (rc) return rc;
+  *form = (h->solver != 1 && cluster_blocks(h, h->frames) > 0) ? h->cl_kind : 0;
   return EQ_OK;
 }
 

@@ -53,6 +53,7 @@ struct LsClArgs {
   int S, P, K, R;
   int m;  // a cluster barrier every m + 1 steps; lag 2m + 3, skew m per block
   float a, cr;
+  const uint8_t* strip;  // the streamed form's strip-ordered codes (lscs.cuh)
 };
 
 struct LsClLayout {  // byte offsets in one block's shared memory

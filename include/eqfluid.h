@@ -495,13 +495,21 @@ int eq_fluid_set_spin_limit(eq_fluid* h, int64_t iterations);
 #define EQ_CONC_DENSITY 2
 int eq_fluid_set_concurrency(eq_fluid* h, int mask);
 
-/* Which kernel runs lin_solve: 0 (default) = the thread-block-cluster
- * wavefront where it applies (sizes with 32 < N <= ~300 and <= 32 sweeps;
- * both kernels are bit-exact), else the multi-block wavefront; 1 = the
- * multi-block wavefront always; 2 = like 0. get_solver reports the blocks
- * per cluster the next solve uses (0 = the multi-block wavefront). */
+/* Which kernel runs lin_solve (all are bit-exact). The thread-block-cluster
+ * wavefront applies for 32 < N <= 1024 (strips of up to 64 positions on at
+ * most 16 blocks): with its strips staged in shared memory whole where they
+ * fit (<= 32 sweeps, N up to ~320), else streamed through shared-memory
+ * rings (<= 31 sweeps). 0 (default) = the staged cluster form where it
+ * applies; the streamed form only for the solves step() runs on its side
+ * streams (it holds few SMs, so it runs beside the critical path's solve);
+ * else the multi-block wavefront. 1 = the multi-block wavefront always.
+ * 2 = the cluster form (staged or streamed) wherever it applies.
+ * get_solver reports the blocks per cluster of the cluster form (0 = it
+ * does not apply); get_cluster_form its form: 0 = none, 1 = strips staged
+ * whole, 2 = strips streamed. */
 int eq_fluid_set_solver(eq_fluid* h, int solver);
 int eq_fluid_get_solver(eq_fluid* h, int* cluster_blocks);
+int eq_fluid_get_cluster_form(eq_fluid* h, int* form);
 /* Caps the cluster wavefront's barrier interval at max_m + 1 steps (0..3;
  * by default 3 steps for N >= 192 and 2 below, the fastest measured; the
  * longest interval up to the cap that fits in shared memory is used). */

@@ -1,5 +1,6 @@
-"""lin_solve by the thread-block-cluster wavefront (csrc/lscl.cuh) against the
-oracle and against the multi-block wavefront, bit for bit.
+"""lin_solve by the thread-block-cluster wavefronts (csrc/lscl.cuh: strips
+staged whole; csrc/lscs.cuh: strips streamed) against the oracle and against
+the multi-block wavefront, bit for bit.
 
 The plain handle picks the cluster form by default where it applies, so every
 other plain-handle test at those sizes runs it too; these tests also pin that
@@ -72,6 +73,78 @@ def test_cluster_lin_solve_bitexact(eqlib, size, K, mode):
     _lib.check(L.eq_fluid_lin_solve(f.handle, mode, 2, 4, a, c))
     f.synchronize()
     assert_bitexact(f.read_field(2), ref, f"multi-block lin_solve mode {mode} K {K}", size)
+    f.close()
+
+
+def form(f):
+    c = ctypes.c_int()
+    _lib.check(_lib.load().eq_fluid_get_cluster_form(f.handle, ctypes.byref(c)))
+    return c.value
+
+
+@pytest.mark.parametrize("size,K,nblocks", [(514, 20, 16), (514, 1, 16), (400, 31, 13),
+                                            (700, 13, 16), (1026, 20, 16), (1026, 2, 16)])
+@pytest.mark.parametrize("mode", [ROW, COL, PAS])
+def test_streamed_cluster_lin_solve_bitexact(eqlib, size, K, nblocks, mode):
+    """The streamed form: one position per lane (N = 398, 512), two (N = 698
+    with a shorter last strip, N = 1024), 31 sweeps (a full 1024-thread
+    block with the loader warp), every barrier interval."""
+    L = _lib.load()
+    f = Fluid(FluidConfigs(1e-4, 1e-4, False), SimulationConfigs(0.1, K, size))
+    r = oracle.OracleFluid(size, 0.1, K, 1e-4, 1e-4)
+    for rc in rects_for(size):
+        _lib.check(L.eq_fluid_fill_obstacle(f.handle, *rc))
+        r.fill_obstacle(*rc)
+    assert blocks(f) == nblocks and form(f) == 2, "the streamed cluster form should apply"
+    _lib.check(L.eq_fluid_set_solver(f.handle, 2))  # the cluster form for this solve too
+    rng = np.random.default_rng(size * 5 + K + mode)
+    n = size * size
+    x = rng.normal(size=n).astype(np.float32)
+    x0 = rng.normal(size=n).astype(np.float32)
+    a = np.float32(0.37)
+    c = np.float32(1.0) + np.float32(4.0) * a
+    ref = x.copy()
+    oracle.lin_solve(mode, ref, x0, a, c, size, K, r.cells)
+    f.write_field(4, x0)
+    for max_m in (1, 0, 2, 3):
+        _lib.check(L.eq_fluid_set_cluster_interval(f.handle, max_m))
+        f.write_field(2, x)
+        _lib.check(L.eq_fluid_lin_solve(f.handle, mode, 2, 4, a, c))
+        f.synchronize()
+        assert_bitexact(f.read_field(2), ref,
+                        f"streamed lin_solve mode {mode} K {K} interval {max_m + 1}", size)
+    f.close()
+
+
+def test_streamed_cluster_frames_match_oracle(eqlib):
+    """Three frames with sources at N = 1024: the streamed form in every solve
+    (three of them side by side in each step), then three more with the
+    default split (multi-block on the critical path, streamed on the side
+    streams)."""
+    size, K = 1026, 20
+    L = _lib.load()
+    f = Fluid(FluidConfigs(1e-5, 1e-5, False), SimulationConfigs(0.05, K, size))
+    r = oracle.OracleFluid(size, 0.05, K, 1e-5, 1e-5)
+    for rc in rects_for(size):
+        _lib.check(L.eq_fluid_fill_obstacle(f.handle, *rc))
+        r.fill_obstacle(*rc)
+    assert form(f) == 2
+    xs = np.array([300, 301, 700], dtype=np.uint32)
+    ys = np.array([420, 420, 160], dtype=np.uint32)
+    d = np.array([40.0, 10.0, 25.0], dtype=np.float32)
+    u = np.array([3.0, -2.0, 0.5], dtype=np.float32)
+    v = np.array([-1.0, 4.0, 2.5], dtype=np.float32)
+    for solver in (2, 0):
+        _lib.check(L.eq_fluid_set_solver(f.handle, solver))
+        for _ in range(3):
+            f.add_sources(xs, ys, d, u, v)
+            f.step()
+        r.run(3, np.tile(xs, (3, 1)), np.tile(ys, (3, 1)), np.tile(d, (3, 1)),
+              np.tile(u, (3, 1)), np.tile(v, (3, 1)))
+        f.synchronize()
+        for k in range(6):
+            assert_bitexact(f.read_field(k), r.fields[k],
+                            f"solver {solver} field {oracle.FIELDS[k]}", size)
     f.close()
 
 
