@@ -28,6 +28,15 @@ struct eq_grad {
   bool have_src = false;
   float* adj = nullptr;         // the six adjoint grids (anti-diagonal)
   float* work = nullptr;        // tmp, Y0, Y1, Ysum, yK (anti-diagonal)
+  float* xwork = nullptr;       // two more such sets, for backward's side streams
+  // The stream and work set the adjoint launches use: the handle's stream
+  // and `work`, except inside adj_step's side branches (the handle's side
+  // streams with a set of xwork each), forked from and joined to the stream
+  // by afork / ajoin.
+  cudaStream_t cs = nullptr;
+  float* cw = nullptr;
+  cudaEvent_t afork = nullptr;
+  cudaEvent_t ajoin[2] = {};
   float* phase = nullptr;       // 4 anti-diagonal grids for the per-phase entry points
   uint8_t* dcode = nullptr;     // boundary codes, anti-diagonal
   float* dense = nullptr;       // 12 x S x S staging
@@ -49,7 +58,7 @@ namespace {
 constexpr int kTapeFields = 5;  // vx0, vy0 (after project 1), vx, vy (after project 2), sc
 
 float* gadj(eq_grad* g, int f) { return g->adj + (size_t)f * g->dn; }
-float* gtmp(eq_grad* g) { return g->work; }
+float* gtmp(eq_grad* g) { return g->cw; }
 
 int gcheck(eq_grad* g) {
   g->launches++;
@@ -75,18 +84,18 @@ int adj_bnd(eq_grad* g, int mode, float* x) {
   float* t = gtmp(g);
   switch (mode) {
     case eqk::kRow:
-      eqk::k_adj_bnd<eqk::kRow><<<ggrd(g), gblk(), 0, h->stream>>>(x, t, g->dcode, h->rowfl, h->colfl, S, P);
+      eqk::k_adj_bnd<eqk::kRow><<<ggrd(g), gblk(), 0, g->cs>>>(x, t, g->dcode, h->rowfl, h->colfl, S, P);
       break;
     case eqk::kCol:
-      eqk::k_adj_bnd<eqk::kCol><<<ggrd(g), gblk(), 0, h->stream>>>(x, t, g->dcode, h->rowfl, h->colfl, S, P);
+      eqk::k_adj_bnd<eqk::kCol><<<ggrd(g), gblk(), 0, g->cs>>>(x, t, g->dcode, h->rowfl, h->colfl, S, P);
       break;
     default:
-      eqk::k_adj_bnd<eqk::kPassive><<<ggrd(g), gblk(), 0, h->stream>>>(x, t, g->dcode, h->rowfl, h->colfl, S, P);
+      eqk::k_adj_bnd<eqk::kPassive><<<ggrd(g), gblk(), 0, g->cs>>>(x, t, g->dcode, h->rowfl, h->colfl, S, P);
       break;
   }
   int rc = gcheck(g);
   if (rc) return rc;
-  EQ_CUDA(cudaMemcpyAsync(x, t, g->dn * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+  EQ_CUDA(cudaMemcpyAsync(x, t, g->dn * sizeof(float), cudaMemcpyDeviceToDevice, g->cs));
   return EQ_OK;
 }
 
@@ -101,7 +110,7 @@ template <int MODE>
 int launch_gs_adj(eq_grad* g, const eqk::GsAdjArgs& A) {
   const int store = g->gs_store;
   const size_t smem = eqk::gs_adj_smem_bytes(store, A.S, A.K);
-  cudaStream_t s = g->h->stream;
+  cudaStream_t s = g->cs;
   if (store == 3) {  // a cluster of g->gs_cluster blocks
     cudaEvent_t c0 = nullptr, c1 = nullptr;
     if (g->profiling) {
@@ -235,28 +244,28 @@ int adj_lin_solve(eq_grad* g, int mode, float* xb, float* x0b, float a, float c)
   if (K > (1 << 20)) return fail(EQ_ERR_ARG, "too many sweeps for the adjoint");
   const int S = (int)h->S, P = h->P;
   float* t = gtmp(g);
-  float* Y0 = g->work + g->dn;
-  float* Y1 = g->work + 2 * g->dn;
-  float* Ys = g->work + 3 * g->dn;
-  float* yK = g->work + 4 * g->dn;
+  float* Y0 = g->cw + g->dn;
+  float* Y1 = g->cw + 2 * g->dn;
+  float* Ys = g->cw + 3 * g->dn;
+  float* yK = g->cw + 4 * g->dn;
   const float cr = 1.0f / c, alpha = a * cr;
   int rc;
   if ((rc = pick_gs_store(g, S, (int)K))) return rc;
   switch (mode) {
     case eqk::kRow:
-      eqk::k_adj_bnd<eqk::kRow><<<ggrd(g), gblk(), 0, h->stream>>>(xb, t, g->dcode, h->rowfl, h->colfl, S, P);
+      eqk::k_adj_bnd<eqk::kRow><<<ggrd(g), gblk(), 0, g->cs>>>(xb, t, g->dcode, h->rowfl, h->colfl, S, P);
       break;
     case eqk::kCol:
-      eqk::k_adj_bnd<eqk::kCol><<<ggrd(g), gblk(), 0, h->stream>>>(xb, t, g->dcode, h->rowfl, h->colfl, S, P);
+      eqk::k_adj_bnd<eqk::kCol><<<ggrd(g), gblk(), 0, g->cs>>>(xb, t, g->dcode, h->rowfl, h->colfl, S, P);
       break;
     default:
-      eqk::k_adj_bnd<eqk::kPassive><<<ggrd(g), gblk(), 0, h->stream>>>(xb, t, g->dcode, h->rowfl, h->colfl, S, P);
+      eqk::k_adj_bnd<eqk::kPassive><<<ggrd(g), gblk(), 0, g->cs>>>(xb, t, g->dcode, h->rowfl, h->colfl, S, P);
       break;
   }
   if ((rc = gcheck(g))) return rc;
   // Ghost positions of Ysum and yK stay 0 (never written); their interior is
   // rewritten by every solve except Ysum accumulated in global memory.
-  if (g->gs_store < 2) EQ_CUDA(cudaMemsetAsync(Y0, 0, 3 * g->dn * sizeof(float), h->stream));
+  if (g->gs_store < 2) EQ_CUDA(cudaMemsetAsync(Y0, 0, 3 * g->dn * sizeof(float), g->cs));
   eqk::GsAdjArgs A;
   A.B = t;
   A.Y0 = Y0;
@@ -275,15 +284,15 @@ int adj_lin_solve(eq_grad* g, int mode, float* xb, float* x0b, float a, float c)
   switch (mode) {
     case eqk::kRow:
       if ((rc = launch_gs_adj<eqk::kRow>(g, A))) return rc;
-      eqk::k_gs_adj_out<eqk::kRow><<<ggrd(g), gblk(), 0, h->stream>>>(xb, t, yK, Ys, x0b, g->dcode, h->rowfl, h->colfl, S, P, alpha, cr);
+      eqk::k_gs_adj_out<eqk::kRow><<<ggrd(g), gblk(), 0, g->cs>>>(xb, t, yK, Ys, x0b, g->dcode, h->rowfl, h->colfl, S, P, alpha, cr);
       break;
     case eqk::kCol:
       if ((rc = launch_gs_adj<eqk::kCol>(g, A))) return rc;
-      eqk::k_gs_adj_out<eqk::kCol><<<ggrd(g), gblk(), 0, h->stream>>>(xb, t, yK, Ys, x0b, g->dcode, h->rowfl, h->colfl, S, P, alpha, cr);
+      eqk::k_gs_adj_out<eqk::kCol><<<ggrd(g), gblk(), 0, g->cs>>>(xb, t, yK, Ys, x0b, g->dcode, h->rowfl, h->colfl, S, P, alpha, cr);
       break;
     default:
       if ((rc = launch_gs_adj<eqk::kPassive>(g, A))) return rc;
-      eqk::k_gs_adj_out<eqk::kPassive><<<ggrd(g), gblk(), 0, h->stream>>>(xb, t, yK, Ys, x0b, g->dcode, h->rowfl, h->colfl, S, P, alpha, cr);
+      eqk::k_gs_adj_out<eqk::kPassive><<<ggrd(g), gblk(), 0, g->cs>>>(xb, t, yK, Ys, x0b, g->dcode, h->rowfl, h->colfl, S, P, alpha, cr);
       break;
   }
   return gcheck(g);
@@ -298,7 +307,7 @@ int adj_advect(eq_grad* g, int mode, float* db, float* d0b, float* ub, float* vb
   const int S = (int)h->S, N = S - 2;
   const float dt0 = h->dt * (float)(h->S - 2);
   const int threads = std::min(256, ((N + 31) / 32) * 32);
-  eqk::k_adv_adj_rows<<<N, threads, 0, h->stream>>>(db, d0b, ub, vb, d0, u, v, S, h->P, h->P, dt0);
+  eqk::k_adv_adj_rows<<<N, threads, 0, g->cs>>>(db, d0b, ub, vb, d0, u, v, S, h->P, h->P, dt0);
   return gcheck(g);
 }
 
@@ -308,14 +317,14 @@ int adj_project(eq_grad* g, float* vxb, float* vyb, float* pb, float* divb) {
   const int S = (int)h->S, P = h->P;
   int rc;
   if ((rc = adj_bnd(g, eqk::kCol, vyb)) || (rc = adj_bnd(g, eqk::kRow, vxb))) return rc;
-  eqk::k_grad_adj<<<ggrd(g), gblk(), 0, h->stream>>>(vxb, vyb, pb, S, P);
+  eqk::k_grad_adj<<<ggrd(g), gblk(), 0, g->cs>>>(vxb, vyb, pb, S, P);
   if ((rc = gcheck(g))) return rc;
   if ((rc = adj_lin_solve(g, eqk::kPassive, pb, divb, 1.0f, 4.0f))) return rc;
   if ((rc = adj_bnd(g, eqk::kPassive, pb)) || (rc = adj_bnd(g, eqk::kPassive, divb))) return rc;
-  eqk::k_div_adj<<<ggrd(g), gblk(), 0, h->stream>>>(vxb, vyb, divb, S, P);
+  eqk::k_div_adj<<<ggrd(g), gblk(), 0, g->cs>>>(vxb, vyb, divb, S, P);
   if ((rc = gcheck(g))) return rc;
   const dim3 gi = grid2d(S - 2, S - 2, gblk());
-  eqk::k_zero_interior2<<<gi, gblk(), 0, h->stream>>>(pb, divb, S, P);
+  eqk::k_zero_interior2<<<gi, gblk(), 0, g->cs>>>(pb, divb, S, P);
   return gcheck(g);
 }
 
@@ -339,16 +348,56 @@ int adj_step(eq_grad* g, const float* tp) {
   const float ad = ((h->dt * h->diff) * sf) * sf;
   const float av = ((h->dt * h->visc) * sf) * sf;
   int rc;
-  eqk::k_adj_clone<<<ggrd(g), gblk(), 0, h->stream>>>(deb, scb, S, P);
+  eqk::k_adj_clone<<<ggrd(g), gblk(), 0, g->cs>>>(deb, scb, S, P);
   if ((rc = gcheck(g))) return rc;
   if ((rc = adj_advect(g, eqk::kPassive, deb, scb, vxb, vyb, t_sc, t_vx, t_vy))) return rc;
-  if ((rc = adj_lin_solve(g, eqk::kPassive, scb, deb, ad, 1.0f + 4.0f * ad))) return rc;
+  // From here the density's diffusion^T (scb, deb) and the velocity chain
+  // (vxb, vyb, vx0b, vy0b) touch disjoint grids, and so do the last two
+  // diffusions^T: with the handle's concurrency on they run on its side
+  // streams, each with its own work set, joined at the end of the frame.
+  const bool side = h->concurrent != 0;
+  cudaStream_t mst = h->stream;
+  auto on = [&](cudaStream_t st, float* w) {
+    g->cs = st;
+    g->cw = w;
+  };
+  auto fork = [&](int k) -> int {
+    EQ_CUDA(cudaEventRecord(g->afork, mst));
+    EQ_CUDA(cudaStreamWaitEvent(h->side[k], g->afork, 0));
+    on(h->side[k], g->xwork + (size_t)k * 5 * g->dn);
+    return EQ_OK;
+  };
+  auto join = [&](int k) -> int {
+    EQ_CUDA(cudaEventRecord(g->ajoin[k], h->side[k]));
+    on(mst, g->work);
+    return EQ_OK;
+  };
+  if (side) {
+    if ((rc = fork(1))) return rc;
+    rc = adj_lin_solve(g, eqk::kPassive, scb, deb, ad, 1.0f + 4.0f * ad);
+    const int rj = join(1);
+    if (rc || (rc = rj)) return rc;
+  } else if ((rc = adj_lin_solve(g, eqk::kPassive, scb, deb, ad, 1.0f + 4.0f * ad))) {
+    return rc;
+  }
   if ((rc = adj_project(g, vxb, vyb, vx0b, vy0b))) return rc;
   if ((rc = adj_advect(g, eqk::kCol, vyb, vy0b, vx0b, vy0b, t_vy0, t_vx0, t_vy0))) return rc;
   if ((rc = adj_advect(g, eqk::kRow, vxb, vx0b, vx0b, vy0b, t_vx0, t_vx0, t_vy0))) return rc;
   if ((rc = adj_project(g, vx0b, vy0b, vxb, vyb))) return rc;
-  if ((rc = adj_lin_solve(g, eqk::kCol, vy0b, vyb, av, 1.0f + 4.0f * av))) return rc;
-  return adj_lin_solve(g, eqk::kRow, vx0b, vxb, av, 1.0f + 4.0f * av);
+  if (side) {
+    if ((rc = fork(0))) return rc;
+    rc = adj_lin_solve(g, eqk::kCol, vy0b, vyb, av, 1.0f + 4.0f * av);
+    const int rj = join(0);
+    if (rc || (rc = rj)) return rc;
+  } else if ((rc = adj_lin_solve(g, eqk::kCol, vy0b, vyb, av, 1.0f + 4.0f * av))) {
+    return rc;
+  }
+  if ((rc = adj_lin_solve(g, eqk::kRow, vx0b, vxb, av, 1.0f + 4.0f * av))) return rc;
+  if (side) {
+    EQ_CUDA(cudaStreamWaitEvent(mst, g->ajoin[0], 0));
+    EQ_CUDA(cudaStreamWaitEvent(mst, g->ajoin[1], 0));
+  }
+  return EQ_OK;
 }
 
 // The forward step with the fields each advect reads saved into tp.
@@ -495,6 +544,10 @@ void free_grad(eq_grad* g) {
   cudaFree(g->src);
   cudaFree(g->adj);
   cudaFree(g->work);
+  cudaFree(g->xwork);
+  if (g->afork) cudaEventDestroy(g->afork);
+  for (cudaEvent_t e : g->ajoin)
+    if (e) cudaEventDestroy(e);
   cudaFree(g->phase);
   cudaFree(g->dcode);
   cudaFree(g->dense);
@@ -563,6 +616,7 @@ int eq_grad_new(eq_fluid* h, int64_t max_frames, int64_t checkpoint_every, eq_gr
   if (cudaMalloc(&g->src, (size_t)max_frames * g->nn * F) != cudaSuccess ||
       cudaMalloc(&g->adj, 6 * g->dn * F) != cudaSuccess ||
       cudaMalloc(&g->work, 5 * g->dn * F) != cudaSuccess ||
+      cudaMalloc(&g->xwork, 10 * g->dn * F) != cudaSuccess ||
       cudaMalloc(&g->phase, 4 * g->dn * F) != cudaSuccess ||
       cudaMalloc(&g->dcode, g->dn) != cudaSuccess ||
       cudaMalloc(&g->dense, 12 * g->nn * F) != cudaSuccess ||
@@ -572,10 +626,19 @@ int eq_grad_new(eq_fluid* h, int64_t max_frames, int64_t checkpoint_every, eq_gr
   cudaStream_t s = h->stream;
   if (cudaMemsetAsync(g->adj, 0, 6 * g->dn * F, s) != cudaSuccess ||
       cudaMemsetAsync(g->work, 0, 5 * g->dn * F, s) != cudaSuccess ||
+      cudaMemsetAsync(g->xwork, 0, 10 * g->dn * F, s) != cudaSuccess ||
       cudaMemsetAsync(g->phase, 0, 4 * g->dn * F, s) != cudaSuccess ||
       cudaMemsetAsync(g->pstage, 0, 3 * g->grid * F, s) != cudaSuccess) {
     free_grad(g);
     return fail(EQ_ERR_CUDA, "cudaMemsetAsync");
+  }
+  g->cs = h->stream;
+  g->cw = g->work;
+  if (cudaEventCreateWithFlags(&g->afork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&g->ajoin[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&g->ajoin[1], cudaEventDisableTiming) != cudaSuccess) {
+    free_grad(g);
+    return fail(EQ_ERR_CUDA, "cudaEventCreate");
   }
   *out = g;
   return EQ_OK;
