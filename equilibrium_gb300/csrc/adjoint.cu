@@ -400,32 +400,9 @@ int adj_step(eq_grad* g, const float* tp) {
   return EQ_OK;
 }
 
-// The forward step with the fields each advect reads saved into tp.
-int step_taped(eq_grad* g, float* tp) {
-  eq_fluid* h = g->h;
-  const size_t G = g->grid, B = G * sizeof(float);
-  float* sc = h->field[EQ_FIELD_SCRATCH];
-  float* de = h->field[EQ_FIELD_DENSITY];
-  float* vx = h->field[EQ_FIELD_VX];
-  float* vy = h->field[EQ_FIELD_VY];
-  float* vx0 = h->field[EQ_FIELD_VX0];
-  float* vy0 = h->field[EQ_FIELD_VY0];
-  int rc;
-  if ((rc = launch_diffuse(h, eqk::kRow, vx0, vx, h->visc))) return rc;
-  if ((rc = launch_diffuse(h, eqk::kCol, vy0, vy, h->visc))) return rc;
-  if ((rc = launch_project(h, vx0, vy0, vx, vy))) return rc;
-  EQ_CUDA(cudaMemcpyAsync(tp, vx0, B, cudaMemcpyDeviceToDevice, h->stream));
-  EQ_CUDA(cudaMemcpyAsync(tp + G, vy0, B, cudaMemcpyDeviceToDevice, h->stream));
-  if ((rc = launch_advect(h, eqk::kRow, vx, vx0, vx0, vy0))) return rc;
-  if ((rc = launch_advect(h, eqk::kCol, vy, vy0, vx0, vy0))) return rc;
-  if ((rc = launch_project(h, vx, vy, vx0, vy0))) return rc;
-  EQ_CUDA(cudaMemcpyAsync(tp + 2 * G, vx, B, cudaMemcpyDeviceToDevice, h->stream));
-  EQ_CUDA(cudaMemcpyAsync(tp + 3 * G, vy, B, cudaMemcpyDeviceToDevice, h->stream));
-  if ((rc = launch_diffuse(h, eqk::kPassive, sc, de, h->diff))) return rc;
-  EQ_CUDA(cudaMemcpyAsync(tp + 4 * G, sc, B, cudaMemcpyDeviceToDevice, h->stream));
-  if ((rc = launch_advect(h, eqk::kPassive, de, sc, vx, vy))) return rc;
-  return launch_copy(h, sc, de);
-}
+// The forward step with the fields each advect reads saved into tp (the
+// plain step, its independent diffusions on side streams as configured).
+int step_taped(eq_grad* g, float* tp) { return launch_step(g->h, tp); }
 
 int add_frame_source(eq_grad* g, int64_t f) {
   if (!g->have_src) return EQ_OK;

@@ -572,7 +572,10 @@ int launch_copy(eq_fluid* h, float* dst, const float* src) {
 }
 
 // step (fluid.rs:437-524), with the reference's aliasing of the six arrays.
-int launch_step(eq_fluid* h) {
+// One frame (fluid.rs:437-524). With a tape, the fields each advect reads are
+// saved into it on the way (vx0, vy0 after the first project, vx, vy after
+// the second, scratch after the density diffusion: 5 pitched grids).
+int launch_step(eq_fluid* h, float* tape = nullptr) {
   int rc = upload_mask(h);
   if (rc) return rc;
   float* sc = h->field[EQ_FIELD_SCRATCH];
@@ -581,14 +584,24 @@ int launch_step(eq_fluid* h) {
   float* vy = h->field[EQ_FIELD_VY];
   float* vx0 = h->field[EQ_FIELD_VX0];
   float* vy0 = h->field[EQ_FIELD_VY0];
+  const size_t G = h->grid_elems(), GB = G * sizeof(float);
+  auto save = [&](int slot, const float* f) -> int {
+    if (tape)
+      EQ_CUDA(cudaMemcpyAsync(tape + (size_t)slot * G, f, GB, cudaMemcpyDeviceToDevice,
+                              h->stream));
+    return EQ_OK;
+  };
   if (!h->concurrent) {
     if ((rc = launch_diffuse(h, eqk::kRow, vx0, vx, h->visc))) return rc;
     if ((rc = launch_diffuse(h, eqk::kCol, vy0, vy, h->visc))) return rc;
     if ((rc = launch_project(h, vx0, vy0, vx, vy))) return rc;
+    if ((rc = save(0, vx0)) || (rc = save(1, vy0))) return rc;
     if ((rc = launch_advect(h, eqk::kRow, vx, vx0, vx0, vy0))) return rc;
     if ((rc = launch_advect(h, eqk::kCol, vy, vy0, vx0, vy0))) return rc;
     if ((rc = launch_project(h, vx, vy, vx0, vy0))) return rc;
+    if ((rc = save(2, vx)) || (rc = save(3, vy))) return rc;
     if ((rc = launch_diffuse(h, eqk::kPassive, sc, de, h->diff))) return rc;
+    if ((rc = save(4, sc))) return rc;
     if ((rc = launch_advect(h, eqk::kPassive, de, sc, vx, vy))) return rc;
     return launch_copy(h, sc, de);
   }
@@ -627,13 +640,16 @@ int launch_step(eq_fluid* h) {
   else if ((rc = launch_diffuse(h, eqk::kCol, vy0, vy, h->visc)))
     return rc;
   if ((rc = launch_project(h, vx0, vy0, vx, vy))) return rc;
+  if ((rc = save(0, vx0)) || (rc = save(1, vy0))) return rc;
   if ((rc = launch_advect(h, eqk::kRow, vx, vx0, vx0, vy0))) return rc;
   if ((rc = launch_advect(h, eqk::kCol, vy, vy0, vx0, vy0))) return rc;
   if ((rc = launch_project(h, vx, vy, vx0, vy0))) return rc;
+  if ((rc = save(2, vx)) || (rc = save(3, vy))) return rc;
   if (sideDe)
     EQ_CUDA(cudaStreamWaitEvent(h->stream, h->join_ev[1], 0));
   else if ((rc = launch_diffuse(h, eqk::kPassive, sc, de, h->diff)))
     return rc;
+  if ((rc = save(4, sc))) return rc;
   if ((rc = launch_advect(h, eqk::kPassive, de, sc, vx, vy))) return rc;
   return launch_copy(h, sc, de);
 }
