@@ -326,8 +326,9 @@ def run_precision_form(local_rank: int, frames: int, size: int = PREC_SIZE,
     storage format, its refinement statistics, and at `err_frames` the relative
     L2 density error, max-abs velocity error and post-projection divergence
     against two f64 references run on the host (in two spawned processes,
-    while the GPU runs): the reference step itself and the same step with both
-    pressure solves converged exactly."""
+    after the timed frames: the frames are host-clocked and launch-bound, so
+    they must not share the host with the references): the reference step
+    itself and the same step with both pressure solves converged exactly."""
     import concurrent.futures as cf
     import multiprocessing as mp
     import torch
@@ -336,10 +337,6 @@ def run_precision_form(local_rank: int, frames: int, size: int = PREC_SIZE,
     total = max(frames + 1, nmax)
     rects, sx, sy, sd, su, sv = precision_scene(size, nframes=total)
     pool, futs, refs = None, [], {}
-    if err_frames:
-        pool = cf.ProcessPoolExecutor(2, mp_context=mp.get_context("spawn"))
-        futs = [pool.submit(_precision_reference, (kind, size, tuple(err_frames)))
-                for kind in ("f64_reference", "f64_converged_pressure")]
     out = {"workload": f"one scene, N = {size - 2} interior, dt {PREC_DT}, diffusion = viscosity "
                        f"= {PREC_DIFF}, 20 sweeps per diffusion solve, pressure refined to a "
                        f"relative residual of {PREC_RTOL}, 4 seeded rectangles, {NSRC} seeded "
@@ -392,6 +389,9 @@ def run_precision_form(local_rank: int, frames: int, size: int = PREC_SIZE,
                                      f"({tc:.1f} s)"}
     if err_frames:
         t0 = time.perf_counter()
+        pool = cf.ProcessPoolExecutor(2, mp_context=mp.get_context("spawn"))
+        futs = [pool.submit(_precision_reference, (kind, size, tuple(err_frames)))
+                for kind in ("f64_reference", "f64_converged_pressure")]
         for f in futs:
             kind, snaps = f.result()
             refs[kind] = snaps
