@@ -29,10 +29,6 @@ struct eq_hfluid {
   std::vector<float> sd, su, sv;
   uint8_t* d_src = nullptr;
   size_t d_src_cap = 0;
-  // one refinement round after its residual (scale, zero the correction,
-  // V-cycle, update) captured once and replayed; the kernels it holds
-  cudaGraphExec_t round_exec = nullptr;
-  uint64_t round_kernels = 0;
 };
 
 namespace {
@@ -59,7 +55,6 @@ void hfree(eq_hfluid* h) {
   cudaFree(h->d_acc);
   cudaFree(h->lvblock);
   cudaFree(h->d_src);
-  if (h->round_exec) cudaGraphExecDestroy(h->round_exec);
   if (h->h_acc) cudaFreeHost(h->h_acc);
   free_handle(h->plain);
   delete h;
@@ -129,45 +124,6 @@ void h_vcycle(eq_hfluid* h, size_t l) {
   }
 }
 
-// One refinement round after the residual: the residual scaled to unit RMS
-// into the finest level's right-hand side, a V-cycle on a zero correction,
-// p += scale * correction. The scale comes from the residual's FP64 sums on
-// the device, so the ~10 launches per level are captured into a graph once
-// and replayed each round.
-template <class T>
-int h_round(eq_hfluid* h) {
-  eq_fluid* pl = h->plain;
-  cudaStream_t st = pl->stream;
-  if (!h->round_exec) {
-    const int S = (int)pl->S, P = pl->P, N = S - 2;
-    const auto& L0 = h->lv[0];
-    const uint64_t l0 = pl->launches;
-    EQ_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    eqk::k_ir_scale<T><<<h_grid(N, N), kHBlk, 0, st>>>(h->r32, S, P, h->d_acc,
-                                                       static_cast<T*>(L0.r), L0.pitch);
-    cudaMemsetAsync(L0.e, 0, (size_t)L0.pitch * L0.n * sizeof(float), st);
-    h_vcycle<T>(h, 0);
-    eqk::k_ir_update<<<h_grid(N, N), kHBlk, 0, st>>>(h->p32, S, P,
-                                                     static_cast<const float*>(L0.e), L0.pitch,
-                                                     h->d_acc);
-    cudaGraph_t graph = nullptr;
-    const cudaError_t e = cudaStreamEndCapture(st, &graph);
-    h->round_kernels = (pl->launches - l0) + 2;
-    pl->launches = l0;
-    if (e != cudaSuccess || !graph)
-      return fail(EQ_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
-    const cudaError_t ei = cudaGraphInstantiate(&h->round_exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ei != cudaSuccess) {
-      h->round_exec = nullptr;
-      return fail(EQ_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ei));
-    }
-  }
-  EQ_CUDA(cudaGraphLaunch(h->round_exec, st));
-  pl->launches += h->round_kernels;
-  return EQ_OK;
-}
-
 // project (fluid.rs:330-375) with the pressure solved by mixed-precision
 // refinement; p and div are the stored arrays the reference aliases.
 template <class T>
@@ -188,6 +144,7 @@ int h_project(eq_hfluid* h, int which, T* vx, T* vy, T* ps, T* divs) {
   eqk::k_h_widen<T><<<h_blocks(n), 256, 0, st>>>(h->p32, ps, n);
   eqk::k_ir_zero<<<h_grid(N, N), kHBlk, 0, st>>>(h->p32, S, P);
   if ((rc = check_launch(pl))) return rc;
+  const auto& L0 = h->lv[0];
   double bnorm = 0.0, rel = 0.0, prev = 0.0;
   int it = 0, slow = 0;
   for (;; ++it) {
@@ -212,8 +169,16 @@ int h_project(eq_hfluid* h, int which, T* vx, T* vy, T* ps, T* divs) {
     if (it > 0) slow = (rel > 0.5 * prev) ? slow + 1 : 0;
     if (slow >= 2) break;
     prev = rel;
-    if ((rc = h_round<T>(h))) return rc;
-    EQ_CUDA(cudaGetLastError());
+    const double scale = rn / std::sqrt(cnt);
+    eqk::k_ir_scale<T><<<h_grid(N, N), kHBlk, 0, st>>>(h->r32, S, P, (float)mean,
+                                                       (float)(1.0 / scale),
+                                                       static_cast<T*>(L0.r), L0.pitch);
+    EQ_CUDA(cudaMemsetAsync(L0.e, 0, (size_t)L0.pitch * L0.n * sizeof(float), st));
+    h_vcycle<T>(h, 0);
+    eqk::k_ir_update<<<h_grid(N, N), kHBlk, 0, st>>>(h->p32, S, P,
+                                                     static_cast<const float*>(L0.e), L0.pitch,
+                                                     (float)scale);
+    if ((rc = check_launch(pl))) return rc;
   }
   h->stats.ir_iterations[which] = it;
   h->stats.rel_residual[which] = rel;

@@ -194,43 +194,24 @@ __global__ void k_ir_residual(const float* __restrict__ p, const float* __restri
   block_add_f64x2(s1, s2, acc);
 }
 
-// A refinement round's residual statistics from the FP64 sums of the
-// residual kernel (acc[0] = sum, acc[1] = sum of squares over the N x N
-// interior): the mean, 1 / scale and scale, scale = the centred residual's
-// RMS. The host's convergence test uses the same expressions.
-__device__ __forceinline__ void ir_round_params(const double* acc, int N, float& mean_f,
-                                                float& inv_f, float& scale_f) {
-  const double cnt = (double)N * N;
-  const double mean = acc[0] / cnt;
-  const double rn = sqrt(fmax(0.0, acc[1] - cnt * mean * mean));
-  const double scale = rn / sqrt(cnt);
-  mean_f = (float)mean;
-  inv_f = (float)(1.0 / scale);
-  scale_f = (float)scale;
-}
-
 // Level-0 right-hand side: (r - mean) / scale in the storage format.
 template <class T>
-__global__ void k_ir_scale(const float* __restrict__ r, int S, int P,
-                           const double* __restrict__ acc, T* __restrict__ r0, int pitch0) {
+__global__ void k_ir_scale(const float* __restrict__ r, int S, int P, float mean, float inv_scale,
+                           T* __restrict__ r0, int pitch0) {
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
   const int N = S - 2;
   if (I >= N || J >= N) return;
-  float mean, inv_scale, scale;
-  ir_round_params(acc, N, mean, inv_scale, scale);
   hs(r0, (size_t)J * pitch0 + I, (r[(size_t)(J + 1) * P + I + 1] - mean) * inv_scale);
 }
 
-// p += scale * e0 on the interior (scale: the round's, from acc).
+// p += scale * e0 on the interior.
 __global__ void k_ir_update(float* __restrict__ p, int S, int P, const float* __restrict__ e0,
-                            int pitch0, const double* __restrict__ acc) {
+                            int pitch0, float scale) {
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
   const int N = S - 2;
   if (I >= N || J >= N) return;
-  float mean, inv_scale, scale;
-  ir_round_params(acc, N, mean, inv_scale, scale);
   const size_t q = (size_t)(J + 1) * P + I + 1;
   p[q] += scale * e0[(size_t)J * pitch0 + I];
 }
