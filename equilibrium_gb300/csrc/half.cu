@@ -98,14 +98,30 @@ template <class T>
 void h_vcycle(eq_hfluid* h, size_t l) {
   cudaStream_t st = h->plain->stream;
   const auto& L = h->lv[l];
-  h->plain->launches += (l + 1 == h->lv.size()) ? 1 : 10;
   float* e = static_cast<float*>(L.e);
   T* r = static_cast<T*>(L.r);
   const float s4 = std::ldexp(1.0f, 2 * (int)l);  // 4^l
   if (l + 1 == h->lv.size()) {
+    h->plain->launches += 1;
     eqk::k_mg_coarse<T><<<1, 1024, 0, st>>>(e, r, L.n, L.pitch, s4, 64);
     return;
   }
+  if (L.n <= 64 && h->lv.size() - l <= (size_t)eqk::kMgMaxLevels) {
+    // this level and the coarser ones in one block
+    eqk::MgLevels V;
+    V.count = (int)(h->lv.size() - l);
+    V.l0 = (int)l;
+    for (int k = 0; k < V.count; ++k) {
+      V.n[k] = h->lv[l + k].n;
+      V.pitch[k] = h->lv[l + k].pitch;
+      V.e[k] = static_cast<float*>(h->lv[l + k].e);
+      V.r[k] = h->lv[l + k].r;
+    }
+    h->plain->launches += 1;
+    eqk::k_mg_vcycle_small<T><<<1, 1024, 0, st>>>(V);
+    return;
+  }
+  h->plain->launches += 10;
   const dim3 gs = h_grid((L.n + 1) / 2, L.n);
   for (int s = 0; s < 2; ++s) {
     eqk::k_mg_smooth<T><<<gs, kHBlk, 0, st>>>(e, r, L.n, L.pitch, 0, s4);

@@ -36,10 +36,8 @@ namespace eqk {
 // One red-black colour of Gauss-Seidel on A e = rs * s4 (level of n x n
 // cells, rs stored, s4 = 4^level).
 template <class T>
-__global__ void k_mg_smooth(float* __restrict__ e, const T* __restrict__ r, int n, int pitch,
-                            int color, float s4) {
-  const int J = blockIdx.y * blockDim.y + threadIdx.y;
-  const int I2 = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void mg_smooth_cell(float* e, const T* r, int n, int pitch, int color,
+                                               float s4, int I2, int J) {
   const int I = 2 * I2 + ((J + color) & 1);
   if (I >= n || J >= n) return;
   const size_t q = (size_t)J * pitch + I;
@@ -50,6 +48,12 @@ __global__ void k_mg_smooth(float* __restrict__ e, const T* __restrict__ r, int 
   if (J > 0) { sum += e[q - pitch]; ++nin; }
   if (J < n - 1) { sum += e[q + pitch]; ++nin; }
   e[q] = (hl(r, q) * s4 + sum) / (float)nin;
+}
+template <class T>
+__global__ void k_mg_smooth(float* __restrict__ e, const T* __restrict__ r, int n, int pitch,
+                            int color, float s4) {
+  mg_smooth_cell(e, r, n, pitch, color, s4, (int)(blockIdx.x * blockDim.x + threadIdx.x),
+                 (int)(blockIdx.y * blockDim.y + threadIdx.y));
 }
 
 // (r * s4 - A e) at one cell.
@@ -70,11 +74,9 @@ __device__ __forceinline__ float mg_resid(const float* e, const T* r, int I, int
 // rc = (sum over the 2 x 2 children of the residual) / (4 s4) (the stored
 // form of the coarse right-hand side); ec = 0.
 template <class T>
-__global__ void k_mg_restrict(const float* __restrict__ e, const T* __restrict__ r, int n,
-                              int pitch, float s4, T* __restrict__ rc, float* __restrict__ ec,
-                              int nc, int pitchc) {
-  const int I = blockIdx.x * blockDim.x + threadIdx.x;
-  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void mg_restrict_cell(const float* e, const T* r, int n, int pitch,
+                                                 float s4, T* rc, float* ec, int nc, int pitchc,
+                                                 int I, int J) {
   if (I >= nc || J >= nc) return;
   float s = 0.0f;
 #pragma unroll
@@ -87,13 +89,19 @@ __global__ void k_mg_restrict(const float* __restrict__ e, const T* __restrict__
   hs(rc, (size_t)J * pitchc + I, s / (4.0f * s4));
   ec[(size_t)J * pitchc + I] = 0.0f;
 }
+template <class T>
+__global__ void k_mg_restrict(const float* __restrict__ e, const T* __restrict__ r, int n,
+                              int pitch, float s4, T* __restrict__ rc, float* __restrict__ ec,
+                              int nc, int pitchc) {
+  mg_restrict_cell(e, r, n, pitch, s4, rc, ec, nc, pitchc,
+                   (int)(blockIdx.x * blockDim.x + threadIdx.x),
+                   (int)(blockIdx.y * blockDim.y + threadIdx.y));
+}
 
 // e += bilinear interpolation of the coarse correction (weights 9/16, 3/16,
 // 3/16, 1/16; a coarse neighbour beyond the wall reflects to the parent).
-__global__ void k_mg_prolong(float* __restrict__ e, int n, int pitch, const float* __restrict__ ec,
-                             int nc, int pitchc) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void mg_prolong_cell(float* e, int n, int pitch, const float* ec, int nc,
+                                                int pitchc, int i, int j) {
   if (i >= n || j >= n) return;
   const int I = i >> 1, J = j >> 1;
   int In = I + ((i & 1) ? 1 : -1), Jn = J + ((j & 1) ? 1 : -1);
@@ -103,13 +111,18 @@ __global__ void k_mg_prolong(float* __restrict__ e, int n, int pitch, const floa
                   0.1875f * ec[(size_t)Jn * pitchc + I] + 0.0625f * ec[(size_t)Jn * pitchc + In];
   e[(size_t)j * pitch + i] += v;
 }
+__global__ void k_mg_prolong(float* __restrict__ e, int n, int pitch, const float* __restrict__ ec,
+                             int nc, int pitchc) {
+  mg_prolong_cell(e, n, pitch, ec, nc, pitchc, (int)(blockIdx.x * blockDim.x + threadIdx.x),
+                  (int)(blockIdx.y * blockDim.y + threadIdx.y));
+}
 
 // The coarsest level (n <= 32) by one block of 1024 threads in shared memory:
 // `iters` red-black sweeps from e = 0, then the mean removed (the pure
 // Neumann problem determines e only up to a constant).
 template <class T>
-__global__ void __launch_bounds__(1024) k_mg_coarse(float* __restrict__ e, const T* __restrict__ r,
-                                                    int n, int pitch, float s4, int iters) {
+__device__ __forceinline__ void mg_coarse_block(float* __restrict__ e, const T* __restrict__ r,
+                                                int n, int pitch, float s4, int iters) {
   __shared__ float se[32][33], sr[32][33];
   __shared__ float ssum[32];
   const int I = threadIdx.x & 31, J = threadIdx.x >> 5;
@@ -142,6 +155,67 @@ __global__ void __launch_bounds__(1024) k_mg_coarse(float* __restrict__ e, const
   }
   __syncthreads();
   if (in) e[(size_t)J * pitch + I] = se[J][I] - ssum[0];
+}
+template <class T>
+__global__ void __launch_bounds__(1024) k_mg_coarse(float* __restrict__ e, const T* __restrict__ r,
+                                                    int n, int pitch, float s4, int iters) {
+  mg_coarse_block(e, r, n, pitch, s4, iters);
+}
+
+// The levels of a V-cycle from level l0 down, for k_mg_vcycle_small.
+constexpr int kMgMaxLevels = 8;
+struct MgLevels {
+  int count;  // levels l0 .. l0 + count - 1 (the last one the coarsest)
+  int l0;
+  int n[kMgMaxLevels], pitch[kMgMaxLevels];
+  float* e[kMgMaxLevels];
+  void* r[kMgMaxLevels];
+};
+
+// The V-cycle's small levels (n <= 64) in one block of 1024 threads: the
+// same operations in the same order as the launches of the larger levels
+// (two red-black smoothing passes, restriction, the coarser levels, bilinear
+// prolongation, two passes in the reverse colour order; the coarsest solved
+// in shared memory), a block barrier between them. Every pass updates
+// independent cells from the same operands, so the result is the launches'.
+template <class T>
+__global__ void __launch_bounds__(1024) k_mg_vcycle_small(MgLevels V) {
+  auto smooth = [&](int k, int color) {
+    const int n = V.n[k], h2 = (n + 1) / 2;
+    const float s4 = ldexpf(1.0f, 2 * (V.l0 + k));
+    for (int q = threadIdx.x; q < h2 * n; q += blockDim.x)
+      mg_smooth_cell(V.e[k], static_cast<const T*>(V.r[k]), n, V.pitch[k], color, s4, q % h2,
+                     q / h2);
+    __syncthreads();
+  };
+  const int last = V.count - 1;
+  for (int k = 0; k < last; ++k) {
+    for (int s = 0; s < 2; ++s) {
+      smooth(k, 0);
+      smooth(k, 1);
+    }
+    const int n = V.n[k], nc = V.n[k + 1];
+    const float s4 = ldexpf(1.0f, 2 * (V.l0 + k));
+    for (int q = threadIdx.x; q < nc * nc; q += blockDim.x)
+      mg_restrict_cell(V.e[k], static_cast<const T*>(V.r[k]), n, V.pitch[k], s4,
+                       static_cast<T*>(V.r[k + 1]), V.e[k + 1], nc, V.pitch[k + 1], q % nc,
+                       q / nc);
+    __syncthreads();
+  }
+  mg_coarse_block(V.e[last], static_cast<const T*>(V.r[last]), V.n[last], V.pitch[last],
+                  ldexpf(1.0f, 2 * (V.l0 + last)), 64);
+  __syncthreads();
+  for (int k = last - 1; k >= 0; --k) {
+    const int n = V.n[k];
+    for (int q = threadIdx.x; q < n * n; q += blockDim.x)
+      mg_prolong_cell(V.e[k], n, V.pitch[k], V.e[k + 1], V.n[k + 1], V.pitch[k + 1], q % n,
+                      q / n);
+    __syncthreads();
+    for (int s = 0; s < 2; ++s) {
+      smooth(k, 1);
+      smooth(k, 0);
+    }
+  }
 }
 
 // ---- refinement on the fine grid (f32 pressure, pitched like the fields) ----
