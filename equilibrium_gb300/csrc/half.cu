@@ -77,20 +77,22 @@ int h_bnd(eq_hfluid* h, int mode, T* x) {
 int h_blocks(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 8); }
 
 // diffuse (fluid.rs:276-298): the stored x (initial guess) and x0 widened
-// into the plain handle's FP32 grids, the reference's lin_solve there, x
-// narrowed back.
+// into two of the plain handle's FP32 grids (2 stage and 2 stage + 1: one
+// pair per diffusion that may run at the same time), the reference's
+// lin_solve there on the plain handle's current stream, x narrowed back.
 template <class T>
-int h_diffuse(eq_hfluid* h, int mode, T* x, const T* x0, float diffusion) {
+int h_diffuse(eq_hfluid* h, int mode, T* x, const T* x0, float diffusion, int stage = 0) {
   eq_fluid* pl = h->plain;
   const size_t n = pl->grid_elems();
-  float* xs = pl->field[0];
-  float* x0s = pl->field[1];
-  eqk::k_h_widen<T><<<h_blocks(n), 256, 0, pl->stream>>>(xs, x, n);
-  eqk::k_h_widen<T><<<h_blocks(n), 256, 0, pl->stream>>>(x0s, x0, n);
+  float* xs = pl->field[2 * stage];
+  float* x0s = pl->field[2 * stage + 1];
+  cudaStream_t st = pl->cur;
+  eqk::k_h_widen<T><<<h_blocks(n), 256, 0, st>>>(xs, x, n);
+  eqk::k_h_widen<T><<<h_blocks(n), 256, 0, st>>>(x0s, x0, n);
   int rc = check_launch(pl);
   if (rc) return rc;
   if ((rc = launch_diffuse(pl, mode, xs, x0s, diffusion))) return rc;
-  eqk::k_h_narrow<T><<<h_blocks(n), 256, 0, pl->stream>>>(x, xs, n);
+  eqk::k_h_narrow<T><<<h_blocks(n), 256, 0, st>>>(x, xs, n);
   return check_launch(pl);
 }
 
@@ -286,13 +288,41 @@ int h_step(eq_hfluid* h) {
     h->su.clear();
     h->sv.clear();
   }
+  // The vy and the density diffusions run on the plain handle's side
+  // streams as its concurrency mask says (their own staging grids and
+  // wavefront state; joined before their results are read), the rest on
+  // its stream in the reference's order.
+  const bool sideVy = (pl->concurrent & EQ_CONC_VY) != 0;
+  const bool sideDe = (pl->concurrent & EQ_CONC_DENSITY) != 0;
+  auto on = [&](cudaStream_t st, int slot) {
+    pl->cur = st;
+    pl->cur_slot = slot;
+  };
+  auto side = [&](int k, int mode, T* x, const T* x0, float dif) -> int {
+    EQ_CUDA(cudaStreamWaitEvent(pl->side[k], pl->fork_ev, 0));
+    on(pl->side[k], k + 1);
+    int r = h_diffuse<T>(h, mode, x, x0, dif, k + 1);
+    if (!r && cudaEventRecord(pl->join_ev[k], pl->side[k]) != cudaSuccess)
+      r = fail(EQ_ERR_CUDA, "side stream event");
+    on(pl->stream, 0);
+    return r;
+  };
+  if (sideVy || sideDe) EQ_CUDA(cudaEventRecord(pl->fork_ev, pl->stream));
   if ((rc = h_diffuse<T>(h, eqk::kRow, vx0, vx, pl->visc))) return rc;
-  if ((rc = h_diffuse<T>(h, eqk::kCol, vy0, vy, pl->visc))) return rc;
+  if (sideVy && (rc = side(0, eqk::kCol, vy0, vy, pl->visc))) return rc;
+  if (sideDe && (rc = side(1, eqk::kPassive, sc, de, pl->diff))) return rc;
+  if (sideVy)
+    EQ_CUDA(cudaStreamWaitEvent(pl->stream, pl->join_ev[0], 0));
+  else if ((rc = h_diffuse<T>(h, eqk::kCol, vy0, vy, pl->visc)))
+    return rc;
   if ((rc = h_project<T>(h, 0, vx0, vy0, vx, vy))) return rc;
   if ((rc = h_advect<T>(h, eqk::kRow, vx, vx0, vx0, vy0))) return rc;
   if ((rc = h_advect<T>(h, eqk::kCol, vy, vy0, vx0, vy0))) return rc;
   if ((rc = h_project<T>(h, 1, vx, vy, vx0, vy0))) return rc;
-  if ((rc = h_diffuse<T>(h, eqk::kPassive, sc, de, pl->diff))) return rc;
+  if (sideDe)
+    EQ_CUDA(cudaStreamWaitEvent(pl->stream, pl->join_ev[1], 0));
+  else if ((rc = h_diffuse<T>(h, eqk::kPassive, sc, de, pl->diff)))
+    return rc;
   if ((rc = h_advect<T>(h, eqk::kPassive, de, sc, vx, vy))) return rc;
   const size_t n = pl->grid_elems();
   eqk::k_h_copy<T><<<h_blocks(n), 256, 0, pl->stream>>>(sc, de, n);
