@@ -138,6 +138,7 @@ def load(path: str = LIB_PATH):
         "eq_batch_read_cells": (i32, [H, i64, P, u64]),
         "eq_batch_set_sources": (i32, [H, i64, i64, P, P, P, P, P]),
         "eq_batch_read_field": (i32, [H, i64, i32, P, u64]),
+        "eq_batch_read_fields": (i32, [H, i32, P, u64]),
         "eq_batch_write_field": (i32, [H, i64, i32, P, u64]),
         "eq_batch_step": (i32, [H, i64]),
         "eq_batch_step_eager": (i32, [H, i64]),

@@ -92,6 +92,17 @@ class Batch:
                                               out.size))
         return out
 
+    def read_fields(self, field: int, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """One field of every scene: their dense size*size arrays concatenated in
+        scene order (`out` may be a preallocated float32 array, e.g. pinned)."""
+        n = sum(self._size(s) ** 2 for s in range(len(self)))
+        if out is None:
+            out = np.empty(n, dtype=np.float32)
+        if out.dtype != np.float32 or out.size != n or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous float32 array of the total cell count")
+        check(_lib.load().eq_batch_read_fields(self.handle, field, out.ctypes.data, out.size))
+        return out
+
     def write_field(self, scene: int, field: int, values: np.ndarray):
         v = np.ascontiguousarray(values, dtype=np.float32).reshape(-1)
         check(_lib.load().eq_batch_write_field(self.handle, scene, field, v.ctypes.data,

@@ -45,6 +45,12 @@ struct eq_batch {
   float* d_sval = nullptr;  // d, u, v (3 x total)
   int64_t src_cap = 0;
 
+  // eq_batch_read_fields: every scene's dense field (device staging) and the
+  // scenes' offsets in it, allocated on first use
+  float* d_dense = nullptr;
+  unsigned long long* d_doff = nullptr;
+  uint64_t dense_total = 0;
+
   int nwmax = 20;  // sweeps per wavefront pass = warps per block
   int bps = 1;     // blocks per SM
   int num_sms = 0;
@@ -74,6 +80,8 @@ void batch_free(eq_batch* b) {
   batch_drop_graph(b);
   if (b->arena2 && b->arena2 != b->arena) cudaFree(b->arena2);
   cudaFree(b->arena);
+  cudaFree(b->d_dense);
+  cudaFree(b->d_doff);
   cudaFree(b->marena);
   cudaFree(b->d_desc);
   cudaFree(b->d_order);
@@ -616,6 +624,53 @@ int eq_batch_read_field(eq_batch* b, int64_t scene, int field, float* host, uint
 int eq_batch_write_field(eq_batch* b, int64_t scene, int field, const float* host,
                          uint64_t n) {
   return batch_field_copy(b, scene, field, const_cast<float*>(host), n, false);
+}
+
+int eq_batch_read_fields(eq_batch* b, int field, float* host, uint64_t n) {
+  int rc;
+  if ((rc = batch_check(b)) || (rc = check_field(field))) return rc;
+  if (!host) return fail(EQ_ERR_ARG, "null host buffer");
+  if (!b->d_doff) {
+    std::vector<unsigned long long> off(b->n);
+    uint64_t t = 0;
+    for (int64_t s = 0; s < b->n; ++s) {
+      off[s] = t;
+      t += (uint64_t)b->desc[s].S * b->desc[s].S;
+    }
+    if (cudaMalloc(&b->d_doff, b->n * sizeof(unsigned long long)) != cudaSuccess) {
+      b->d_doff = nullptr;
+      return fail(EQ_ERR_OOM, "cudaMalloc (dense offsets)");
+    }
+    if (cudaMalloc(&b->d_dense, t * sizeof(float)) != cudaSuccess) {
+      cudaFree(b->d_doff);
+      b->d_doff = nullptr;
+      b->d_dense = nullptr;
+      return fail(EQ_ERR_OOM, "cudaMalloc (dense staging)");
+    }
+    EQ_CUDA(cudaMemcpy(b->d_doff, off.data(), b->n * sizeof(unsigned long long),
+                       cudaMemcpyHostToDevice));
+    b->dense_total = t;
+  }
+  if (n != b->dense_total) return fail(EQ_ERR_ARG, "element count must be the sum of size*size");
+  // density (1) and scratch (0) live in arena2 in their own format
+  const bool scalar = field < 2;
+  const void* arena = scalar ? b->arena2 : b->arena;
+  const bool half = (scalar ? b->esize2 : b->esize) == 2;
+  const unsigned blocks = (unsigned)b->n;
+  if (!half)
+    eqk::k_batch_gather_dense<<<blocks, 256, 0, b->stream>>>(
+        static_cast<const float*>(arena), b->d_desc, b->d_doff, field, b->d_dense);
+  else if (b->storage == EQ_STORE_BF16)
+    eqk::k_batch_gather_dense<<<blocks, 256, 0, b->stream>>>(
+        static_cast<const __nv_bfloat16*>(arena), b->d_desc, b->d_doff, field, b->d_dense);
+  else
+    eqk::k_batch_gather_dense<<<blocks, 256, 0, b->stream>>>(
+        static_cast<const __half*>(arena), b->d_desc, b->d_doff, field, b->d_dense);
+  EQ_CUDA(cudaGetLastError());
+  b->launches++;
+  EQ_CUDA(cudaMemcpyAsync(host, b->d_dense, n * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
+  EQ_CUDA(cudaStreamSynchronize(b->stream));
+  return EQ_OK;
 }
 
 int eq_batch_set_tuning(eq_batch* b, int sweeps_per_pass, int blocks_per_sm) {

@@ -496,6 +496,24 @@ __global__ void __launch_bounds__(672, 1) k_batch_run(BatchArgs A, BOpList L) {
   }
 }
 
+// One field of every scene, dense (size x size, row-major) and in scene
+// order, from the arena's anti-diagonal layout: block s copies scene s to
+// out + doff[s].
+template <class ST>
+__global__ void k_batch_gather_dense(const ST* __restrict__ arena, const BScene* __restrict__ sc,
+                                     const unsigned long long* __restrict__ doff, int field,
+                                     float* __restrict__ out) {
+  const BScene d = sc[blockIdx.x];
+  const ST* src = arena + d.foff + (size_t)field * d.fstride;
+  float* dst = out + doff[blockIdx.x];
+  const int S = d.S, P = d.P;
+  const size_t n = (size_t)S * S;
+  for (size_t q = threadIdx.x; q < n; q += blockDim.x) {
+    const int j = (int)(q / S), i = (int)(q - (size_t)j * S);
+    dst[q] = hl(src, dg_at(i, j, P));
+  }
+}
+
 // The frame kernel's instances are compiled in batch_kernels.cu (one
 // translation unit per storage format, built in parallel); every other
 // includer only declares them.

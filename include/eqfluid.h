@@ -294,6 +294,10 @@ int eq_batch_set_sources(eq_batch* b, int64_t scene, int64_t n, const uint32_t* 
 int eq_batch_read_field(eq_batch* b, int64_t scene, int field, float* host, uint64_t n);
 int eq_batch_write_field(eq_batch* b, int64_t scene, int field, const float* host,
                          uint64_t n);
+/* One field of every scene at once: dense size*size copies in scene order,
+ * n = the sum of size*size (synchronous; one device-side layout conversion
+ * and one device-to-host copy, fastest into pinned host memory). */
+int eq_batch_read_fields(eq_batch* b, int field, float* host, uint64_t n);
 
 /* `nframes` frames of every scene: one persistent kernel launch per frame
  * (thread blocks take scenes from a work queue, largest first), the whole

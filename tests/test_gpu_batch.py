@@ -179,6 +179,26 @@ def test_batch_autotune_keeps_state(eqlib):
     b.close()
 
 
+@pytest.mark.parametrize("storage", ["f32", "f16", "bf16", "f16_scalars"])
+def test_batch_read_fields_matches_per_scene_reads(eqlib, storage):
+    """eq_batch_read_fields: every scene's field in scene order, the same
+    values as the per-scene reads, for every field and storage format."""
+    rng = np.random.default_rng(17)
+    cfgs = [SceneConfig(s, 0.1, 4) for s in (20, 34, 66, 41, 130)]
+    b = Batch(cfgs, storage=storage)
+    for sidx, c in enumerate(cfgs):
+        for f in range(6):
+            b.write_field(sidx, f, rng.uniform(-2, 2, c.size * c.size).astype(np.float32))
+    b.step(1)
+    for f in range(6):
+        whole = b.read_fields(f)
+        expect = np.concatenate([b.read_field(sidx, f) for sidx in range(len(cfgs))])
+        assert np.array_equal(whole.view(np.uint32), expect.view(np.uint32)), f"field {f}"
+    with pytest.raises(ValueError):
+        b.read_fields(0, np.empty(3, dtype=np.float32))
+    b.close()
+
+
 def test_batch_rejects_bad_arguments(eqlib):
     with pytest.raises(_lib.EqError):
         Batch([SceneConfig(19)])
