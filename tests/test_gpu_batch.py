@@ -220,7 +220,7 @@ def test_batch_rejects_bad_arguments(eqlib):
 # frame alone gives 6e-3 / 2e-3), the third is diffusion-dominated.
 # With only density and scratch in FP16 (velocities FP32) the error stays at
 # the FP16 rounding of the density itself (about 2e-4 here), within the 1e-3
-# the benchmark spec sets for the FP16 batch.
+# relative L2 density error that the FP16 batch is held to.
 HALF_TOL = {"f16": (0.1, 0.05, 2e-3), "bf16": (0.5, 0.3, 2e-2),
             "f16_scalars": (1e-3, 1e-3, 1e-3)}
 
