@@ -27,10 +27,14 @@
 // previous value, (h-1, 31)'s for l = 0, h > 0, and for (0, 0) the lower
 // block's pushed halo value.
 //
-// The last sweep writes its raw values of interior cells straight to x; the
-// staging copies of x run at least L (K-1) diagonals ahead of those writes
-// in every block, so no staged value is overwritten first. The caller's
-// set_boundaries pass then makes x the reference's array.
+// The last sweep writes its raw values of interior cells straight to x. The
+// staged initial x is read at the block's own positions, at je + 1 (the
+// upper neighbour's first position, which that block, m steps behind,
+// writes later) and on the frame (never written); the lower halo column is
+// read only at the frame, its other values arriving by the neighbour's push.
+// Every copy that is read lands before its cell's write (checked on the CPU
+// with these step formulas), and the caller's set_boundaries pass then makes
+// x the reference's array.
 #pragma once
 #include <cooperative_groups.h>
 
