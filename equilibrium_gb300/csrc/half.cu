@@ -522,4 +522,9 @@ int eq_hfluid_launch_count(const eq_hfluid* h, uint64_t* count) {
   return EQ_OK;
 }
 
+int eq_hfluid_set_concurrency(eq_hfluid* h, int mask) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  return eq_fluid_set_concurrency(h->plain, mask);
+}
+
 }  // extern "C"

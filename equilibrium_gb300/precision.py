@@ -71,6 +71,10 @@ class HalfFluid:
         check(_lib.load().eq_hfluid_launch_count(self.handle, ctypes.byref(c)))
         return c.value
 
+    def set_concurrency(self, mask: int):
+        """Which diffusions run on side streams (bit 1: vy, bit 2: density)."""
+        check(_lib.load().eq_hfluid_set_concurrency(self.handle, mask))
+
 
 def rel_l2(a: np.ndarray, ref: np.ndarray) -> float:
     """||a - ref||_2 / ||ref||_2 over the interior cells."""

@@ -385,6 +385,9 @@ int eq_hfluid_write_field(eq_hfluid* h, int field, const float* host, uint64_t n
 int eq_hfluid_stats(const eq_hfluid* h, eq_hstats* out);
 int eq_hfluid_get_stream(eq_hfluid* h, void** stream);
 int eq_hfluid_launch_count(const eq_hfluid* h, uint64_t* count);
+/* Which diffusions of a step run on side streams (EQ_CONC_* bits, as
+ * eq_fluid_set_concurrency; default both). */
+int eq_hfluid_set_concurrency(eq_hfluid* h, int mask);
 
 /* ---- the differentiation form: adjoint of the frame step --------------- */
 

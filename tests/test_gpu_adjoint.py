@@ -218,6 +218,32 @@ def test_backward_more_cases(eqlib, size, K, frames, every, vel, store):
     f.close()
 
 
+def test_backward_concurrency_matches_one_stream(eqlib):
+    """The backward's side-stream solves (the handle's concurrency on, the
+    default) give the one-stream backward's gradients, up to the summation
+    order of advect^T's float atomics; the forward runs are bit-identical
+    (the final states), the losses equal up to their FP64 atomic sum."""
+    size, frames = 66, 6
+    rects = [(size // 4, size // 3, size // 4 + 5, size // 3 + 4), (size // 2, 2, size // 2 + 3, 9)]
+    out = []
+    for mask in (0, 3):
+        f, of, init, src, target = problem(size, frames, rects, seed=3)
+        assert _lib.load().eq_fluid_set_concurrency(f.handle, mask) == 0
+        g = Recorder(f, frames, 2)
+        g.forward(src)
+        loss = g.l2_loss(target)
+        gi, gs = g.backward()
+        out.append((loss, gi, gs, [f.read_field(k) for k in range(6)]))
+        g.close()
+        f.close()
+    (l0, gi0, gs0, fin0), (l1, gi1, gs1, fin1) = out
+    assert abs(l1 - l0) <= 1e-12 * abs(l0)  # an FP64 atomic sum: its order varies
+    for k in range(6):
+        assert np.array_equal(fin0[k], fin1[k]), k
+    assert rel(gi1[2], gi0[2]) < 1e-5 and rel(gi1[3], gi0[3]) < 1e-5
+    assert rel(gs1, gs0) < 1e-5
+
+
 def test_backward_explicit_adjoint_and_linearity(eqlib):
     """backward(adj_final) with the l2 seed given explicitly equals the seeded
     call; scaling the seed scales every gradient."""

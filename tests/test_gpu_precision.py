@@ -100,3 +100,21 @@ def test_rejects_bad_arguments(eqlib):
         HalfFluid(S, DT, K, DIFF, VISC, "f8")
     with pytest.raises(_lib.EqError):
         HalfFluid(S, DT, K, DIFF, VISC, pressure_rtol=0.0)
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+def test_concurrent_diffusions_match_one_stream(eqlib, storage):
+    """The step's vy and density diffusions on side streams (the default) give
+    the one-stream step's fields; only the FP64 norms' summation order can
+    differ, so the fields agree to far below the storage rounding."""
+    out = []
+    for mask in (0, 3):
+        g = HalfFluid(S, DT, K, DIFF, VISC, storage)
+        g.set_concurrency(mask)
+        g.fill_obstacle(*RECT)
+        for _ in range(3):
+            g.step()
+        out.append([g.read_field(f) for f in range(6)])
+        g.close()
+    for f in range(6):
+        assert rel_l2(out[1][f], out[0][f]) < 1e-6, f
