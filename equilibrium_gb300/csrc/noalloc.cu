@@ -1,18 +1,19 @@
 // lin_solve without any allocation, for callers that cannot allocate device
-// memory: code that runs while a CUDA stream capture is open (cudaMalloc is
-// not allowed there), frame loops that must never take the implicit device
-// synchronisation a cudaMalloc/cudaFree can cause, and hosts whose GPU memory
-// is owned by another allocator with a fixed budget. The caller passes its
-// own device grids; every scratch buffer the wavefront needs lives in one
-// file-scope static device array, sized for grids of at most
-// kNaMaxSize x kNaMaxSize cells (about 3.2 MB, held by every GPU that loads
-// this library until the process exits).
+// memory: a solver embedded in a host application that owns all device memory
+// through its own allocator or a fixed budget (a render engine, a framework
+// with a caching allocator) and forbids its plugins to call cudaMalloc, and
+// frame loops that must not take the device-wide synchronisation a
+// cudaMalloc / cudaFree can cause (this entry point synchronises only the
+// caller's stream). The caller passes its own device grids; every scratch
+// buffer the wavefront needs lives in one file-scope static device array,
+// sized for grids of at most kNaMaxSize x kNaMaxSize cells (about 3.2 MB,
+// held by every GPU that loads this library until the process exits).
 //
 // Set-up: the first call on a device (with that device current) looks up the
 // array's device address with cudaGetSymbolAddress and clears it; make that
 // first call before any stream capture begins. Every call shares the array,
-// so calls that overlap on the GPU (two streams, two threads) race; callers
-// serialise them.
+// which keeps the last call's contents, so calls that overlap on the GPU (two
+// streams, two threads) race; callers serialise them.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -140,13 +141,22 @@ extern "C" int eq_lin_solve_noalloc(int mode, float* x, const float* x0, const u
   k_na_flags<<<(2 * S + 127) / 128, 128, 0, stream>>>(cells, S, P, rowfl, colfl, err);
   k_na_codes<<<dim3((S + 127) / 128, S), 128, 0, stream>>>(cells, colfl, S, P, code);
   if (cudaGetLastError() != cudaSuccess) return EQ_ERR_CUDA;
+  // The frame check's verdict before anything writes x: a mask whose frame is
+  // not all walls returns EQ_ERR_ARG with x untouched.
+  int herr = 0;  // the device error word, read into this stack variable
+  if (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+      cudaStreamSynchronize(stream) != cudaSuccess)
+    return EQ_ERR_CUDA;
+  if (herr != 0) return herr;
 
   const float c_recip = 1.0f / c;
   for (int64_t done = 0; done < iters; done += kNaSweeps) {
     const int Kc = (int)((iters - done) < kNaSweeps ? (iters - done) : kNaSweeps);
-    if (g_na_tag[dev] > 0xF0000000u) {  // tags would wrap: clear the tagged grids
-      if (cudaMemsetAsync(wt, 0, 2 * g * sizeof(unsigned long long), stream) != cudaSuccess ||
-          cudaMemsetAsync(edge, 0, kOffCode - kOffEdge, stream) != cudaSuccess)
+    if (g_na_tag[dev] > 0xF0000000u) {
+      // tags would wrap: clear the whole tagged region (the grids and edge
+      // rows of every size and pitch an earlier call used), not just this
+      // call's part of it
+      if (cudaMemsetAsync(base + kOffWt, 0, kOffCode - kOffWt, stream) != cudaSuccess)
         return EQ_ERR_CUDA;
       g_na_tag[dev] = 1;
     }
@@ -182,7 +192,6 @@ extern "C" int eq_lin_solve_noalloc(int mode, float* x, const float* x0, const u
       eqk::k_lin_solve<eqk::kPassive><<<ntasks, 32, 0, stream>>>(A);
     if (cudaGetLastError() != cudaSuccess) return EQ_ERR_CUDA;
   }
-  int herr = 0;  // the device error word, read into this stack variable
   if (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
       cudaStreamSynchronize(stream) != cudaSuccess)
     return EQ_ERR_CUDA;

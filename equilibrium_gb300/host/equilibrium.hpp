@@ -4,7 +4,7 @@
 // equilibrium::Panic.
 //
 //   configs.rs:5-60        -> SimulationConfigs, FluidConfigs (defaults kept)
-//   obstacle.rs:89-154     -> Rectangle (validated in the constructor)
+//   obstacle.rs:29-87     -> Rectangle (validated in the constructor)
 //   fluid.rs:10-17         -> ContainerWall
 //   fluid.rs:51-620        -> Fluid (new, default, step, fill_obstacle,
 //                             add_density, add_velocity, clone, pub fields)

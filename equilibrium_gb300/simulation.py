@@ -4,7 +4,7 @@ Same names, argument meanings and error behaviour as the reference's Rust
 module ``src/simulation`` (vkabadzhova/equilibrium):
 
 * ``SimulationConfigs`` / ``FluidConfigs``      -- configs.rs:5-60
-* ``Rectangle`` (panics -> ``InvalidRectangle``) -- obstacle.rs:89-154
+* ``Rectangle`` (panics -> ``InvalidRectangle``) -- obstacle.rs:29-87
 * ``ContainerWall``                              -- fluid.rs:10-17
 * ``Fluid`` (new / default / step / fill_obstacle / add_noise / clone, pub
   fields density, velocities_x, velocities_y, cells_type) -- fluid.rs:51-620
@@ -61,7 +61,7 @@ class FluidConfigs:
 
 
 class Rectangle:
-    """Axis-parallel rectangle obstacle (obstacle.rs:89-154)."""
+    """Axis-parallel rectangle obstacle (obstacle.rs:29-87)."""
 
     def __init__(self, down_left_point: Point, up_right_point: Point,
                  fluid_container_size: int):

@@ -15,7 +15,7 @@
  * On the device the rows are padded to a 128-byte pitch.
  *
  * Errors. Every function returns EQ_OK (0) or a positive EQ_ERR_* code; the
- * reference panics in the same places (Rectangle::new, obstacle.rs:126-128),
+ * reference panics in the same places (Rectangle::new, obstacle.rs:67),
  * which a Rust wrapper reproduces by panicking on a non-zero return.
  * eq_last_error() gives a message for the calling thread's last failure.
  *
@@ -151,7 +151,7 @@ int eq_fluid_run_device_sources(eq_fluid* h, int64_t nframes, int64_t nsrc,
                                 const float* d_density, const float* d_vx,
                                 const float* d_vy);
 
-/* ---- obstacles (fluid.rs:610-619, obstacle.rs:115-147) ------------------ */
+/* ---- obstacles (fluid.rs:610-619, obstacle.rs:55-87) ------------------ */
 
 /* Rectangle::new validation: EQ_OK if dl.x < ur.x, dl.y < ur.y and all four
  * coordinates are < size, else EQ_ERR_ARG (the reference panics). */
@@ -463,20 +463,24 @@ int eq_grad_project_adj(eq_grad* g, float* vxb, float* vyb, float* pb, float* di
 
 /* No counterpart in the reference. lin_solve (the same kernels, the same
  * bit-exact result as eq_fluid_lin_solve) for callers that cannot allocate
- * device memory: code inside an open CUDA stream capture, where cudaMalloc is
- * not allowed; frame loops that must not take the implicit device
- * synchronisation cudaMalloc / cudaFree can cause; hosts whose GPU memory is
- * owned by another allocator. The caller passes device pointers to x (in/out),
- * x0 and the wall mask (1 = DefaultWall, ghost frame all walls), each `size`
- * rows with a row pitch of `pitch` elements (pitch % 4 == 0, buffers 16-byte
- * aligned), and the stream to run on (NULL = legacy default stream).
+ * device memory: a solver embedded in a host application that owns all device
+ * memory through its own allocator or a fixed budget (a render engine, a
+ * framework with a caching allocator) and does not let its plugins call
+ * cudaMalloc; frame loops that must not take the device-wide synchronisation
+ * cudaMalloc / cudaFree can cause (this call synchronises only `stream`).
+ * The caller passes device pointers to x (in/out), x0 and the wall mask
+ * (1 = DefaultWall, ghost frame all walls), each `size` rows with a row pitch
+ * of `pitch` elements (pitch % 4 == 0, buffers 16-byte aligned), and the
+ * stream to run on (NULL = legacy default stream).
  * All scratch lives in one static device array sized for
  * size <= 258 and pitch <= 288 (about 3.2 MB per GPU that loads the library,
  * held until exit); larger grids return EQ_ERR_ARG. The first call on a device
  * (that device current) looks the array up and clears it: make it before any
- * stream capture. Every call shares the array, so calls that overlap on the
- * GPU race. Synchronises `stream` before returning (to report the device
- * error word: EQ_ERR_TIMEOUT, or EQ_ERR_ARG if the frame is not all walls). */
+ * stream capture. Every call shares the array, which keeps the last call's
+ * contents, so calls that overlap on the GPU race. Synchronises `stream`
+ * after the mask check (EQ_ERR_ARG if the frame is not all walls, returned
+ * before x is touched) and before returning (EQ_ERR_TIMEOUT from the device
+ * error word; x is then undefined). */
 int eq_lin_solve_noalloc(int mode, float* x, const float* x0, const uint8_t* cells,
                          uint32_t size, uint32_t pitch, int64_t iters, float a, float c,
                          void* stream);

@@ -292,7 +292,7 @@ inline void fill_obstacle(uint8_t* cells, uint32_t size, int64_t x0, int64_t y0,
     for (int64_t y = y0; y < y1; ++y) cells[idx(x, y, size)] = kWall;
 }
 
-// Rectangle::are_all_points_valid (obstacle.rs:134-147).
+// Rectangle::are_all_points_valid (obstacle.rs:74-87).
 inline bool rectangle_valid(int64_t dlx, int64_t dly, int64_t urx, int64_t ury,
                             int64_t size) {
   return dlx != urx && dly != ury && dlx < urx && dly < ury && dlx < size &&

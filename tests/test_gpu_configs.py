@@ -158,14 +158,15 @@ def test_current_simulation_frame_loop(eqlib):
 
 
 def test_cpp_host_mirror_runs_reference_unit_tests(eqlib, tmp_path):
-    """Compiles equilibrium_gb300/host/mirror_check.cpp (the reference's unit
-    tests restated on the C++ mirror) against libeqfluid.so and runs it."""
+    """Compiles tests/mirror_check.cpp (the reference's unit tests restated on
+    the C++ mirror) against libeqfluid.so and runs it."""
     import subprocess
     root = os.path.dirname(HERE)
     libdir = os.path.join(root, "equilibrium_gb300")
     exe = str(tmp_path / "mirror_check")
-    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", root, "-o", exe,
-                           os.path.join(libdir, "host", "mirror_check.cpp"), "-L", libdir,
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", root, "-I",
+                           os.path.join(libdir, "host"), "-o", exe,
+                           os.path.join(HERE, "mirror_check.cpp"), "-L", libdir,
                            "-leqfluid", f"-Wl,-rpath,{libdir}",
                            "-Wl,-rpath,/usr/local/cuda/lib64"])
     out = subprocess.run([exe], capture_output=True, text=True, timeout=300)
