@@ -25,7 +25,7 @@ UNITS = [("eqfluid.cu", ())] + [("batch_kernels.cu", (f"-DEQ_BATCH_STORE={st}",)
 SOURCES = sorted({u for u, _ in UNITS})
 HEADERS = ["common.cuh", "kernels.cuh", "linsolve.cuh", "noalloc.cu", "wave.cuh", "batch.cuh",
            "batch.cu", "half.cuh", "mg.cuh", "half.cu", "store.cuh",
-           "frame.cuh", "frame.cu", "adjoint.cuh", "adjoint.cu", "lscl.cuh", "lscs.cuh"]
+           "frame.cuh", "frame.cu", "adjoint.cuh", "adjoint.cu", "lscl.cuh", "lscs.cuh", "lssw.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: device FP stays un-contracted even outside the explicitly

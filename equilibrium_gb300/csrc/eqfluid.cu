@@ -22,6 +22,7 @@
 #include "linsolve.cuh"
 #include "lscl.cuh"
 #include "lscs.cuh"
+#include "lssw.cuh"
 
 namespace {
 
@@ -127,6 +128,10 @@ struct eq_fluid {
   uint8_t* cs_strip = nullptr;
   int cs_C = 0, cs_J = 0;
   int cl_mmax = -1;   // cap on cl_m; -1: 2 for N >= 192, else 1 (the fastest, measured)
+  // the strip wavefront (lssw.cuh), one set per stream slot: tagged exports
+  // [strips-1][sweeps][records][4] and counters (ticket, done, epoch)
+  unsigned long long* sw_edge[3] = {};
+  unsigned* sw_ctr[3] = {};
 
   size_t grid_elems() const { return (size_t)P * S; }
 };
@@ -432,11 +437,80 @@ int launch_lin_solve_cluster(eq_fluid* h, int mode, float* x, const float* x0, f
   return launch_bnd(h, mode, x);
 }
 
+// lin_solve by the strip wavefront (lssw.cuh), kSwMaxK sweeps per launch,
+// each launch finished by set_boundaries of its last sweep.
+int launch_lin_solve_sw(eq_fluid* h, int mode, float* x, const float* x0, float a,
+                        float c_recip) {
+  static std::atomic<uint64_t> raised{0};
+  const uint64_t bit = h->device < 64 ? (1ull << h->device) : 0ull;
+  if (!bit || !(raised.load() & bit)) {
+    const int bytes = (int)eqk::ls_sw_layout(eqk::kSwMaxK).total;
+    EQ_CUDA(cudaFuncSetAttribute(eqk::k_ls_sw<eqk::kRow>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    EQ_CUDA(cudaFuncSetAttribute(eqk::k_ls_sw<eqk::kCol>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    EQ_CUDA(cudaFuncSetAttribute(eqk::k_ls_sw<eqk::kPassive>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    raised.fetch_or(bit);
+  }
+  const int S = (int)h->S;
+  const int sl = h->cur_slot;
+  for (int64_t done = 0; done < h->frames; done += eqk::kSwMaxK) {
+    const int Kc = (int)std::min<int64_t>(eqk::kSwMaxK, h->frames - done);
+    EQ_CUDA(cudaMemsetAsync(h->sw_ctr[sl], 0, 2 * sizeof(unsigned), h->cur));
+    eqk::LsSwArgs A;
+    A.x = x;
+    A.x0 = x0;
+    A.code = h->code;
+    A.rowfl = h->rowfl;
+    A.colfl = h->colfl;
+    A.edge = h->sw_edge[sl];
+    A.ctr = h->sw_ctr[sl];
+    A.err = h->err;
+    A.spin_limit = h->spin_limit;
+    A.S = S;
+    A.P = h->P;
+    A.K = Kc;
+    A.B = eqk::ls_sw_strips(S, Kc);
+    A.RE = eqk::ls_sw_records(S);
+    A.a = a;
+    A.cr = c_recip;
+    const size_t smem = eqk::ls_sw_layout(Kc).total;
+    const dim3 grid((unsigned)A.B), block(32u * (unsigned)(Kc + 1));
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (h->profiling) {
+      EQ_CUDA(cudaEventCreate(&ev0));
+      EQ_CUDA(cudaEventCreate(&ev1));
+      EQ_CUDA(cudaEventRecord(ev0, h->cur));
+    }
+    switch (mode) {
+      case eqk::kRow:
+        eqk::k_ls_sw<eqk::kRow><<<grid, block, smem, h->cur>>>(A);
+        break;
+      case eqk::kCol:
+        eqk::k_ls_sw<eqk::kCol><<<grid, block, smem, h->cur>>>(A);
+        break;
+      default:
+        eqk::k_ls_sw<eqk::kPassive><<<grid, block, smem, h->cur>>>(A);
+        break;
+    }
+    int rc = check_launch(h);
+    if (rc) return rc;
+    if (h->profiling) {
+      EQ_CUDA(cudaEventRecord(ev1, h->cur));
+      h->ls_events.emplace_back(ev0, ev1);
+    }
+    if ((rc = launch_bnd(h, mode, x))) return rc;
+  }
+  return EQ_OK;
+}
+
 // lin_solve (fluid.rs:301-325) on device grids.
 int launch_lin_solve(eq_fluid* h, int mode, float* x, const float* x0, float a, float c) {
   const int64_t K = h->frames;
   if (K <= 0) return EQ_OK;
   const float c_recip = 1.0f / c;  // fluid.rs:311, IEEE f32 division
+  if (h->solver == 3) return launch_lin_solve_sw(h, mode, x, x0, a, c_recip);
   if (h->solver != 1) {
     // The staged cluster form is the fastest kernel where it applies. The
     // streamed one is slower alone than the multi-block wavefront but holds
@@ -701,6 +775,10 @@ void free_handle(eq_fluid* h) {
     if (h->join_ev[k]) cudaEventDestroy(h->join_ev[k]);
   }
   if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+  for (int k = 0; k < 3; ++k) {
+    cudaFree(h->sw_edge[k]);
+    cudaFree(h->sw_ctr[k]);
+  }
   cudaFree(h->err);
   cudaFree(h->d_src);
   if (h->h_src) cudaFreeHost(h->h_src);
@@ -783,6 +861,20 @@ int alloc_handle(uint32_t size, int device, eq_fluid** out) {
         cudaMemsetAsync(h->xedge[k], 0, ntasks * h->P * 8, h->stream) != cudaSuccess ||
         cudaMemsetAsync(h->xcounters[k], 0, 2 * sizeof(unsigned), h->stream) != cudaSuccess)
       return bail(EQ_ERR_CUDA, "cudaMemsetAsync");
+  }
+  {
+    // strip wavefront exports for the longest launch (kSwMaxK sweeps), per slot
+    const int Bs = eqk::ls_sw_strips((int)size, eqk::kSwMaxK);
+    const size_t words =
+        (size_t)std::max(Bs - 1, 1) * eqk::kSwMaxK * eqk::ls_sw_records((int)size) * 4;
+    for (int k = 0; k < 3; ++k) {
+      if (cudaMalloc(&h->sw_edge[k], words * 8) != cudaSuccess ||
+          cudaMalloc(&h->sw_ctr[k], 4 * sizeof(unsigned)) != cudaSuccess)
+        return bail(EQ_ERR_OOM, "cudaMalloc (strip wavefront state)");
+      if (cudaMemsetAsync(h->sw_edge[k], 0, words * 8, h->stream) != cudaSuccess ||
+          cudaMemsetAsync(h->sw_ctr[k], 0, 4 * sizeof(unsigned), h->stream) != cudaSuccess)
+        return bail(EQ_ERR_CUDA, "cudaMemsetAsync");
+    }
   }
   h->host_cells.assign((size_t)size * size, 0);
   *out = h;
@@ -1261,7 +1353,7 @@ int eq_fluid_set_concurrency(eq_fluid* h, int mask) {
 
 int eq_fluid_set_solver(eq_fluid* h, int solver) {
   if (!h) return fail(EQ_ERR_ARG, "null handle");
-  if (solver < 0 || solver > 2) return fail(EQ_ERR_ARG, "solver must be 0, 1 or 2");
+  if (solver < 0 || solver > 3) return fail(EQ_ERR_ARG, "solver must be 0, 1, 2 or 3");
   h->solver = solver;
   return EQ_OK;
 }
