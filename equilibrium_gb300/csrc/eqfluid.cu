@@ -41,6 +41,7 @@ int fail(int code, const std::string& msg) {
   } while (0)
 
 constexpr int kMaxSweepsPerLaunch = 64;
+constexpr int kSwMaxGroups = 5;  // sweep groups per strip of the strip wavefront
 constexpr long long kDefaultSpinLimit = 1ll << 22;
 
 }  // namespace
@@ -131,7 +132,9 @@ struct eq_fluid {
   // the strip wavefront (lssw.cuh), one set per stream slot: tagged exports
   // [strips-1][sweeps][records][4] and counters (ticket, done, epoch)
   unsigned long long* sw_edge[3] = {};
+  unsigned long long* sw_gexp[3] = {};  // group exports [strips][groups-1][records+1][36]
   unsigned* sw_ctr[3] = {};
+  int sw_groups = 0;  // sweep groups per strip (0: by size)
 
   size_t grid_elems() const { return (size_t)P * S; }
 };
@@ -437,6 +440,33 @@ int launch_lin_solve_cluster(eq_fluid* h, int mode, float* x, const float* x0, f
   return launch_bnd(h, mode, x);
 }
 
+// Sweep groups of the strip wavefront for K sweeps on this grid: blocks of
+// one strip share its sweeps so that about one block per SM works on a solve.
+int sw_groups_for(const eq_fluid* h, int K) {
+  int G = h->sw_groups;
+  if (G <= 0) {
+    const int B = eqk::ls_sw_strips((int)h->S, K);
+    G = std::max(1, std::min(kSwMaxGroups, 152 / std::max(B, 1)));
+  }
+  G = std::min(G, std::min(K, kSwMaxGroups));
+  const int KG = (K + G - 1) / G;
+  return (K + KG - 1) / KG;  // groups that hold a sweep
+}
+
+// Whether the strip wavefront's shared memory fits at this grid size (its
+// frame rows grow with the size; more sweep groups shrink the rest).
+bool sw_fits(const eq_fluid* h) {
+  int optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const int K = (int)std::min<int64_t>(eqk::kSwMaxK, std::max<int64_t>(h->frames, 1));
+  const int G = sw_groups_for(h, K);
+  return eqk::ls_sw_layout((K + G - 1) / G, (int)h->S).total <= (size_t)optin;
+}
+
 // lin_solve by the strip wavefront (lssw.cuh), kSwMaxK sweeps per launch,
 // each launch finished by set_boundaries of its last sweep.
 int launch_lin_solve_sw(eq_fluid* h, int mode, float* x, const float* x0, float a,
@@ -444,19 +474,22 @@ int launch_lin_solve_sw(eq_fluid* h, int mode, float* x, const float* x0, float 
   static std::atomic<uint64_t> raised{0};
   const uint64_t bit = h->device < 64 ? (1ull << h->device) : 0ull;
   if (!bit || !(raised.load() & bit)) {
-    const int bytes = (int)eqk::ls_sw_layout(eqk::kSwMaxK).total;
+    int optin = 0;
+    EQ_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
     EQ_CUDA(cudaFuncSetAttribute(eqk::k_ls_sw<eqk::kRow>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     EQ_CUDA(cudaFuncSetAttribute(eqk::k_ls_sw<eqk::kCol>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     EQ_CUDA(cudaFuncSetAttribute(eqk::k_ls_sw<eqk::kPassive>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     raised.fetch_or(bit);
   }
   const int S = (int)h->S;
   const int sl = h->cur_slot;
   for (int64_t done = 0; done < h->frames; done += eqk::kSwMaxK) {
     const int Kc = (int)std::min<int64_t>(eqk::kSwMaxK, h->frames - done);
+    const int G = sw_groups_for(h, Kc);
+    const int KG = (Kc + G - 1) / G;
     EQ_CUDA(cudaMemsetAsync(h->sw_ctr[sl], 0, 2 * sizeof(unsigned), h->cur));
     eqk::LsSwArgs A;
     A.x = x;
@@ -465,6 +498,7 @@ int launch_lin_solve_sw(eq_fluid* h, int mode, float* x, const float* x0, float 
     A.rowfl = h->rowfl;
     A.colfl = h->colfl;
     A.edge = h->sw_edge[sl];
+    A.gexp = h->sw_gexp[sl];
     A.ctr = h->sw_ctr[sl];
     A.err = h->err;
     A.spin_limit = h->spin_limit;
@@ -472,11 +506,13 @@ int launch_lin_solve_sw(eq_fluid* h, int mode, float* x, const float* x0, float 
     A.P = h->P;
     A.K = Kc;
     A.B = eqk::ls_sw_strips(S, Kc);
+    A.G = G;
+    A.KG = KG;
     A.RE = eqk::ls_sw_records(S);
     A.a = a;
     A.cr = c_recip;
-    const size_t smem = eqk::ls_sw_layout(Kc).total;
-    const dim3 grid((unsigned)A.B), block(32u * (unsigned)(Kc + 1));
+    const size_t smem = eqk::ls_sw_layout(KG, S).total;
+    const dim3 grid((unsigned)(A.B * G)), block(32u * (unsigned)(KG + 2));
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     if (h->profiling) {
       EQ_CUDA(cudaEventCreate(&ev0));
@@ -510,7 +546,7 @@ int launch_lin_solve(eq_fluid* h, int mode, float* x, const float* x0, float a, 
   const int64_t K = h->frames;
   if (K <= 0) return EQ_OK;
   const float c_recip = 1.0f / c;  // fluid.rs:311, IEEE f32 division
-  if (h->solver == 3) return launch_lin_solve_sw(h, mode, x, x0, a, c_recip);
+  if (h->solver == 3 && sw_fits(h)) return launch_lin_solve_sw(h, mode, x, x0, a, c_recip);
   if (h->solver != 1) {
     // The staged cluster form is the fastest kernel where it applies. The
     // streamed one is slower alone than the multi-block wavefront but holds
@@ -777,6 +813,7 @@ void free_handle(eq_fluid* h) {
   if (h->fork_ev) cudaEventDestroy(h->fork_ev);
   for (int k = 0; k < 3; ++k) {
     cudaFree(h->sw_edge[k]);
+    cudaFree(h->sw_gexp[k]);
     cudaFree(h->sw_ctr[k]);
   }
   cudaFree(h->err);
@@ -867,11 +904,15 @@ int alloc_handle(uint32_t size, int device, eq_fluid** out) {
     const int Bs = eqk::ls_sw_strips((int)size, eqk::kSwMaxK);
     const size_t words =
         (size_t)std::max(Bs - 1, 1) * eqk::kSwMaxK * eqk::ls_sw_records((int)size) * 4;
+    const size_t gwords = (size_t)Bs * (kSwMaxGroups - 1) *
+                          (eqk::ls_sw_records((int)size) + 1) * eqk::kSwGrpWords;
     for (int k = 0; k < 3; ++k) {
       if (cudaMalloc(&h->sw_edge[k], words * 8) != cudaSuccess ||
+          cudaMalloc(&h->sw_gexp[k], gwords * 8) != cudaSuccess ||
           cudaMalloc(&h->sw_ctr[k], 4 * sizeof(unsigned)) != cudaSuccess)
         return bail(EQ_ERR_OOM, "cudaMalloc (strip wavefront state)");
       if (cudaMemsetAsync(h->sw_edge[k], 0, words * 8, h->stream) != cudaSuccess ||
+          cudaMemsetAsync(h->sw_gexp[k], 0, gwords * 8, h->stream) != cudaSuccess ||
           cudaMemsetAsync(h->sw_ctr[k], 0, 4 * sizeof(unsigned), h->stream) != cudaSuccess)
         return bail(EQ_ERR_CUDA, "cudaMemsetAsync");
     }
@@ -1355,6 +1396,13 @@ int eq_fluid_set_solver(eq_fluid* h, int solver) {
   if (!h) return fail(EQ_ERR_ARG, "null handle");
   if (solver < 0 || solver > 3) return fail(EQ_ERR_ARG, "solver must be 0, 1, 2 or 3");
   h->solver = solver;
+  return EQ_OK;
+}
+
+int eq_fluid_set_strip_groups(eq_fluid* h, int groups) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  if (groups < 0 || groups > kSwMaxGroups) return fail(EQ_ERR_ARG, "groups must be 0..5");
+  h->sw_groups = groups;
   return EQ_OK;
 }
 

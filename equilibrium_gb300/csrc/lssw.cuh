@@ -1,47 +1,60 @@
-// lin_solve (fluid.rs:301-325) as one persistent launch over strips of rows,
-// bit-exactly: the strip wavefront.
+// lin_solve (fluid.rs:301-325) as one persistent launch over strips of rows
+// and groups of sweeps, bit-exactly: the strip wavefront.
 //
-// Decomposition. Block b owns, for every sweep k of the launch, the 32 rows
-//   j = j0(b, k) + l,  j0(b, k) = 32 b - 2 k,  l = lane,
-// of its sweep warp k (warp K is the copy warp). A sweep's rows shift up by
-// two per sweep, so every value a block needs from another block comes from
-// block b-1 (never b+1): blocks take their strip from an atomic ticket, wait
-// only for lower tickets, and need no co-residency.
+// Decomposition. The launch covers K sweeps. Block (b, g) owns strip b for
+// the sweeps k in [g KG, g KG + nk) (sweep group g): its sweep warp kk
+// (k = g KG + kk) updates the 32 rows
+//   j = j0(b, k) + l,  j0(b, k) = 32 b - 2 k,  l = lane.
+// A sweep's rows shift up by two per sweep, so every value a block needs
+// from another block comes from block (b-1, g) (the halo of the same sweeps)
+// or (b, g-1) (the previous sweep of the first warp): blocks take (b, g) from
+// an atomic ticket (b major), wait only for lower tickets and need no
+// co-residency.
 //
-// Schedule. Sweep warp k works on local diagonal d = tau - kLg k at block step
-// tau; lane l updates cell (i, j) = (d - l, j0 + l), so lane l trails lane
+// Schedule. Sweep warp kk works on local diagonal d = tau - kSwLg kk at block
+// step tau; lane l updates cell (i, j) = (d - l, j0 + l), so lane l trails lane
 // l-1 by one step (Gauss-Seidel order along every row and down every column).
 // The sweep-k value of an interior cell is
 //   raw(i, j) = (x0 + a*(((R + L) + D) + U)) * (1/c)
 // with L = this lane's previous value, U = lane l-1's previous value (a
-// shuffle; lane 0: block b-1's row j0 - 1, imported), and R = post(i+1, j),
+// shuffle; lane 0: strip b-1's row j0 - 1, imported), and R = post(i+1, j),
 // D = post(i, j+1) of sweep k-1 after its set_boundaries, read from sweep k-1's
-// ring of post values in shared memory (the first sweep reads the initial x
-// from a ring of copied rows). post is written one step late: at step d the
-// lane knows raw(i, j), raw(i-1, j), raw(i-2, j), raw(i-1, j-1) (last step's
-// U) and raw(i-1, j+1) (lane l+1's value, a shuffle), which is everything the
-// per-cell boundary code of (i-1, j) can ask for. Frame rows are lanes too
-// (their "value" is the frame cell as the sweep sees it); frame columns are
-// the steps i = 0 and i = S-1 of each row. The last sweep writes its raw
-// interior values to x; the caller's set_boundaries pass (with corners) then
-// makes x the reference's array.
+// ring of post values in shared memory (the group's first sweep reads the
+// previous group's exported ring, or for the first group the initial x from a
+// ring of copied rows). post is written one step late: at step d the lane
+// knows raw(i, j), raw(i-1, j), raw(i-2, j), raw(i-1, j-1) (last step's U) and
+// raw(i-1, j+1) (lane l+1's value, a shuffle), everything the boundary code of
+// (i-1, j) can ask for. Frame rows are lanes too (their value is the frame
+// cell as the sweep sees it); frame columns are the steps i = 0 and i = S-1
+// of each row. The last sweep writes its raw interior values to x; the
+// caller's set_boundaries pass (with corners) then makes x the reference's
+// array.
 //
-// Block-to-block values. Lanes 30 and 31 of every sweep warp export, per
-// diagonal, lane 31's value and both lanes' post values as 64-bit words
-// (value | tag << 32) that block b+1's sweep warp k polls with relaxed loads,
-// issued kSwAHI periods ahead, and copies into its own ring (positions -2,
-// -1) and lane-0 U ring. Lane 31 cannot finish a post value that needs the
-// next block's row (AdjustColumn, wall below); block b+1's lane 0 overwrites
-// it in its ring. The tag is the launch's epoch (a device word the last block
-// advances), so a captured graph replays without clearing anything.
+// Steps. Inside a warp's fast range (every grid row of the warp an interior
+// row at 2 <= i <= N) a step is the update and one post store; the general
+// rules (frame columns, boundary codes, the lane-0 fix) run only on the steps
+// that need them, decided by one warp vote.
 //
-// Staging. The copy warp streams x0 and the codes of the block's rows, and the
-// initial x rows the first sweep reads, into shared-memory rings: per row one
-// aligned 16-byte chunk (4 columns) per period, issued kSwAH periods before
-// its first use. All warps meet at one block barrier per period of kSwQ
-// steps; every cross-warp value is written at least one barrier before it is
-// read and its slot is reused only after its last read (the schedule is
-// checked on the CPU with these formulas).
+// Block-to-block values, as 64-bit words (value | tag << 32) polled with
+// relaxed loads issued two periods ahead and copied into shared memory:
+// * halo: lanes 30 and 31 of sweep warp k export per diagonal
+//   [post30, -, uval31, post31] for strip b+1's sweep warp k (its ring
+//   positions -2, -1 and lane-0 U ring). Lane 31 cannot finish a post value
+//   that needs the next strip's row (AdjustColumn, wall below); strip b+1's
+//   lane 0 overwrites it in its ring.
+// * group: the last sweep warp of group g exports its post ring row per
+//   diagonal (positions -2 .. 31) for group g+1's first sweep, read by an
+//   import warp.
+// The tag is the launch's epoch (a device word the last block advances), so
+// a captured graph replays without clearing anything.
+//
+// Staging. A copy warp streams x0 and the codes of the block's rows, and the
+// initial x rows the first group's first sweep reads, into shared-memory
+// rings: per row one aligned 16-byte chunk (4 columns) per period, issued
+// kSwAH periods before its first use. All warps meet at one block barrier per
+// period of kSwQ steps; every cross-warp value is written at least one
+// barrier before it is read and its slot is reused only after its last read
+// (the schedule is checked on the CPU with these formulas).
 //
 // Safety. Every wait is bounded (spin budget); a timeout sets the device error
 // word and the block's abort flag, and all warps leave the period loop at the
@@ -52,14 +65,16 @@
 
 namespace eqk {
 
-constexpr int kSwQ = 4;      // steps per period (one block barrier per period)
-constexpr int kSwLg = 4;     // steps between consecutive sweeps (>= kSwQ)
-constexpr int kSwRD = 16;    // diagonals kept per sweep ring
-constexpr int kSwRW = 36;    // floats per ring row: positions -2 .. 33
-constexpr int kSwPC = 128;   // columns of the x0 / code rings
-constexpr int kSwPX = 32;    // columns of the initial-x ring
-constexpr int kSwAH = 3;     // a chunk copy is issued kSwAH periods before its use
-constexpr int kSwMaxK = 20;  // sweeps per launch
+constexpr int kSwQ = 4;       // steps per period (one block barrier per period)
+constexpr int kSwLg = 4;      // steps between consecutive sweeps (>= kSwQ)
+constexpr int kSwRD = 16;     // diagonals kept per sweep ring
+constexpr int kSwRW = 36;     // floats per ring row: positions -2 .. 33
+constexpr int kSwPC = 128;    // columns of the x0 / code rings
+constexpr int kSwPX = 32;     // columns of the initial-x ring
+constexpr int kSwAH = 3;      // a chunk copy is issued kSwAH periods before its use
+constexpr int kSwMaxK = 20;   // sweeps per launch
+constexpr int kSwMaxKG = 20;  // sweeps per block
+constexpr int kSwGrpWords = 36;  // words per group-export record (34 used)
 static_assert(kSwLg >= kSwQ, "a ring value must be one barrier old when read");
 
 struct LsSwArgs {
@@ -68,11 +83,12 @@ struct LsSwArgs {
   const uint8_t* code;
   const uint8_t* rowfl;
   const uint8_t* colfl;
-  unsigned long long* edge;  // [B-1][K][RE][4] tagged exports
+  unsigned long long* edge;  // [B-1][K][RE][4] halo exports
+  unsigned long long* gexp;  // [B][G-1][RE+1][kSwGrpWords] group exports
   unsigned* ctr;             // [0] ticket, [1] done (zeroed per launch), [2] epoch
   int* err;
   long long spin_limit;
-  int S, P, K, B, RE;
+  int S, P, K, B, G, KG, RE;
   float a, cr;
 };
 
@@ -80,17 +96,21 @@ __host__ __device__ inline int ls_sw_strips(int S, int K) { return (S + 2 * (K -
 __host__ __device__ inline int ls_sw_records(int S) { return S + 32; }
 
 struct LsSwLayout {  // byte offsets in one block's shared memory
-  size_t vr, ui, x0r, cr, xr, total;
+  size_t vr, ui, vp, x0r, cr, xr, xt, xb, cf, total;
 };
-__host__ __device__ inline LsSwLayout ls_sw_layout(int K) {
-  const size_t nrw = 32 + 2 * (size_t)(K - 1);
+__host__ __device__ inline LsSwLayout ls_sw_layout(int KG, int S) {
+  const size_t nrw = 32 + 2 * (size_t)(KG - 1);
   LsSwLayout L;
-  L.vr = 0;                                                  // K RD RW floats
-  L.ui = L.vr + (size_t)K * kSwRD * kSwRW * 4;               // K RD floats
-  L.x0r = ((L.ui + (size_t)K * kSwRD * 4) + 15) / 16 * 16;  // nrw PC floats
-  L.cr = L.x0r + nrw * kSwPC * 4;                            // nrw PC bytes
-  L.xr = L.cr + nrw * kSwPC;                                 // 33 PX floats
-  L.total = L.xr + 33 * kSwPX * 4;
+  L.vr = 0;                                        // KG RD RW floats
+  L.ui = L.vr + (size_t)KG * kSwRD * kSwRW * 4;     // KG RD floats
+  L.vp = L.ui + (size_t)KG * kSwRD * 4;             // RD RW floats
+  L.x0r = (L.vp + (size_t)kSwRD * kSwRW * 4 + 15) / 16 * 16;  // nrw PC floats
+  L.cr = L.x0r + nrw * kSwPC * 4;                  // nrw PC bytes
+  L.xr = L.cr + nrw * kSwPC;                       // 33 PX floats
+  L.xt = L.xr + 33 * kSwPX * 4;                    // S floats: frame row 0
+  L.xb = L.xt + (size_t)S * 4;                     // S floats: frame row S-1
+  L.cf = L.xb + (size_t)S * 4;                     // S bytes: column has fluid
+  L.total = (L.cf + (size_t)S + 15) / 16 * 16;
   return L;
 }
 
@@ -104,11 +124,17 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_relaxed_u64_sw(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+// Exports: each 64-bit element is one single-copy-atomic word (value | tag).
+__device__ __forceinline__ void sw_st1(unsigned long long* p, float v, unsigned tag) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p),
+               "l"((unsigned long long)__float_as_uint(v) | ((unsigned long long)tag << 32))
+               : "memory");
 }
-__device__ __forceinline__ unsigned long long sw_pack(float v, unsigned tag) {
-  return (unsigned long long)__float_as_uint(v) | ((unsigned long long)tag << 32);
+__device__ __forceinline__ void sw_st2(unsigned long long* p, float v0, float v1, unsigned tag) {
+  asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p),
+               "l"((unsigned long long)__float_as_uint(v0) | ((unsigned long long)tag << 32)),
+               "l"((unsigned long long)__float_as_uint(v1) | ((unsigned long long)tag << 32))
+               : "memory");
 }
 
 // The Gauss-Seidel update; the FMA build contracts x0 + a*sum.
@@ -120,48 +146,207 @@ __device__ __forceinline__ float gs_update(float x0, float a, float sum, float c
 #endif
 }
 
+// One sweep warp's state and constants.
+struct SwWarp {
+  // lane state: the value at the previous step (L), the one before, last
+  // step's U and the code of the previous cell
+  float vcur, vprev, uprev;
+  unsigned cprev;
+  // lane constants
+  int lane, j, S, N, k;
+  bool interior, top, bot, idle, pasRow;
+  float xL, xR, a, cr;
+  const float* prev;   // previous sweep's ring (or the previous group's)
+  float* own;          // this sweep's ring
+  const float* ui;     // lane-0 U ring
+  const float* x0row;  // x0 ring row of this lane's row
+  const uint8_t* crow;
+  const float* xrl;    // first sweep of the first group: initial-x ring rows
+  const float* xrd;
+  const float* xt;     // frame rows and column flags in shared memory
+  const float* xb;
+  const uint8_t* cf;
+  unsigned long long* edgeOut;  // halo export (lanes 30, 31), null if none
+  unsigned long long* gexpOut;  // group export, null if none
+  float* xlast;                 // x + j P - lane for the last sweep, else null
+  bool hasFrame;
+  unsigned tag;
+};
+
+template <int MODE, bool FAST, bool FIRSTX>
+__device__ __forceinline__ void sw_step(SwWarp& w, int d) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = w.lane;
+  const int i = d - lane;
+  const int ro = ((d - 1) & (kSwRD - 1)) * kSwRW;
+  float R, D;
+  if (FIRSTX) {
+    R = w.xrl[(i + 1) & (kSwPX - 1)];
+    D = w.xrd[i & (kSwPX - 1)];
+  } else {
+    R = w.prev[ro + lane];
+    D = w.prev[ro + lane + 1];
+  }
+  const float Ui = w.ui[(d - 1) & (kSwRD - 1)];
+  float U = __shfl_up_sync(FULL, w.vcur, 1);
+  if (lane == 0) U = Ui;
+  const int ci = i & (kSwPC - 1);
+  const float X0 = w.x0row[ci];
+  const unsigned cd = w.crow[ci];
+  const float gs = gs_update(X0, w.a, fadd(fadd(fadd(R, w.vcur), D), U), w.cr);
+  const bool fix = MODE == kCol && lane == 0 && (cd & kCodeAboveDown) != 0 &&
+                   (w.interior || w.bot) && (unsigned)(i - 1) < (unsigned)w.N;
+  bool general = !FAST;
+  if (FAST && MODE != kPassive) {
+    const unsigned actMask =
+        MODE == kRow ? (unsigned)(kCodeRowLeft | kCodeRowRight) : (unsigned)(kCodeColUp | kCodeColDown);
+    general = __any_sync(FULL, w.interior && (((w.cprev & actMask) != 0u) || fix));
+  }
+  float vnew, post;
+  const int S = w.S, N = w.N;
+  if (!general) {
+    vnew = gs;
+    post = w.vcur;
+    if (w.hasFrame) {  // frame-row lanes: the frame cell as the sweep sees it
+      const bool fl = w.top || w.bot;
+      const int ic = min(max(i, 0), S - 1);
+      if (fl) {
+        const float xf = w.top ? w.xt[ic] : w.xb[ic];
+        vnew = (unsigned)i < (unsigned)S
+                   ? ((MODE == kPassive && w.top && w.k > 0 && w.cf[ic]) ? D : xf)
+                   : w.vcur;
+      }
+      if (MODE == kPassive) {
+        const float vdown = __shfl_down_sync(FULL, vnew, 1);
+        const int im1 = min(max(i - 1, 0), S - 1);
+        if (fl && (unsigned)(i - 2) < (unsigned)N && w.cf[im1]) post = w.top ? vdown : w.uprev;
+      }
+    }
+  } else {
+    // ---- the general rules, every lane
+    vnew = w.vcur;
+    if (w.interior) {
+      if ((unsigned)(i - 1) < (unsigned)N)
+        vnew = gs;
+      else if (i == 0)
+        vnew = (MODE == kPassive && w.k > 0 && w.pasRow) ? R : w.xL;
+      else if (i == S - 1)
+        vnew = w.xR;
+    } else if (w.top || w.bot) {
+      if ((unsigned)i < (unsigned)S) {
+        const float xf = w.top ? w.xt[i] : w.xb[i];
+        vnew = (MODE == kPassive && w.top && w.k > 0 && w.cf[i]) ? D : xf;
+      }
+    } else {
+      vnew = 0.0f;
+    }
+    const float vdown = __shfl_down_sync(FULL, vnew, 1);
+    const int im1 = i - 1;
+    post = w.vcur;
+    if (w.interior) {
+      if ((unsigned)(im1 - 1) < (unsigned)N) {
+        if (MODE == kRow)
+          post = (w.cprev & kCodeRowRight) ? -vnew : ((w.cprev & kCodeRowLeft) ? -w.vprev : w.vcur);
+        else if (MODE == kCol)
+          post = (w.cprev & kCodeColUp) ? -w.uprev : ((w.cprev & kCodeColDown) ? -vdown : w.vcur);
+      } else if (im1 == 0) {
+        post = w.pasRow ? vnew : w.vcur;
+      } else if (im1 == S - 1) {
+        post = w.pasRow ? w.vprev : w.vcur;
+      }
+    } else if (w.top || w.bot) {
+      if (MODE == kPassive && (unsigned)(im1 - 1) < (unsigned)N && w.cf[im1])
+        post = w.top ? vdown : w.uprev;
+    } else {
+      post = 0.0f;
+    }
+  }
+  float* const wrow = w.own + ro;
+  wrow[lane + 2] = post;
+  float pm1 = 0.0f;  // position -1 of this diagonal (lane 0): the fix, or the imported value
+  if (MODE == kCol && fix) wrow[1] = -vnew;
+  if (w.edgeOut && d >= 1) {  // lanes 30, 31: record d-1 = [post30, -, uval31, post31]
+    if (lane >= 30)
+      sw_st2(w.edgeOut + (size_t)(d - 1) * 4, lane == 31 ? w.vcur : post, post, w.tag);
+  }
+  if (w.gexpOut) {  // record d: word p + 2 = position p of diagonal d-1
+    unsigned long long* const rec = w.gexpOut + (size_t)d * kSwGrpWords;
+    sw_st1(rec + lane + 2, post, w.tag);
+    if (lane < 2) {
+      pm1 = (MODE == kCol && fix) ? -vnew : wrow[1 - lane];
+      sw_st1(rec + (1 - lane), pm1, w.tag);
+    }
+  }
+  if (w.xlast && w.interior && (unsigned)(i - 1) < (unsigned)N) w.xlast[d] = vnew;
+  w.vprev = w.vcur;
+  w.vcur = vnew;
+  w.uprev = U;
+  w.cprev = cd;
+}
+
 template <int MODE>
-__global__ void __launch_bounds__(32 * (kSwMaxK + 1), 1) k_ls_sw(LsSwArgs A) {
+__global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
   extern __shared__ __align__(16) unsigned char ls_sw_smem[];
   // abort flags by period parity: set during period cp in s_abort[cp & 1] and
   // read by every thread after that period's barrier (nobody writes that slot
   // again before the next barrier), so all warps leave at the same barrier
-  __shared__ int s_b, s_abort[2];
+  __shared__ int s_t, s_abort[2];
   __shared__ unsigned s_tag;
   const unsigned FULL = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int K = A.K, S = A.S, P = A.P, N = S - 2, B = A.B;
+  const int K = A.K, S = A.S, P = A.P, N = S - 2, B = A.B, G = A.G, KG = A.KG;
   if (threadIdx.x == 0) {
-    s_b = (int)atomicAdd(&A.ctr[0], 1u);
+    s_t = (int)atomicAdd(&A.ctr[0], 1u);
     s_tag = ld_relaxed_u32(&A.ctr[2]) + 1u;
     s_abort[0] = s_abort[1] = 0;
   }
   __syncthreads();
-  const int b = s_b;
+  const int t = s_t;
   const unsigned tag = s_tag;
-  if (b >= B) {  // counters not reset: never index past the strips
+  if (t >= B * G) {  // counters not reset: never index past the blocks
     if (threadIdx.x == 0) atomicExch(A.err, 5 /* EQ_ERR_STATE */);
     return;
   }
-  const LsSwLayout lay = ls_sw_layout(K);
+  const int b = t / G, g = t - (t / G) * G;
+  const int kF = g * KG, nk = min(K - kF, KG);
+  const int jb = 32 * b - 2 * kF;  // first row of the group's first sweep
+  const int nrw = 32 + 2 * (nk - 1);
+  const int rA = jb - 2 * (nk - 1);  // first row of the block's rings
+  const int T = S + 32 + kSwLg * (nk - 1);
+  const int NP = (T + kSwQ - 1) / kSwQ;
+  auto rows_active = [&](int k) {  // sweep k's rows of strip b meet the grid
+    const int j0 = 32 * b - 2 * k;
+    return j0 <= S - 1 && j0 + 31 >= 0;
+  };
+  const LsSwLayout lay = ls_sw_layout(KG, S);
   float* const VR = reinterpret_cast<float*>(ls_sw_smem + lay.vr);
   float* const UI = reinterpret_cast<float*>(ls_sw_smem + lay.ui);
+  float* const VP = reinterpret_cast<float*>(ls_sw_smem + lay.vp);
   float* const X0R = reinterpret_cast<float*>(ls_sw_smem + lay.x0r);
   uint8_t* const CR = ls_sw_smem + lay.cr;
   float* const XR = reinterpret_cast<float*>(ls_sw_smem + lay.xr);
-  const int nrw = 32 + 2 * (K - 1);
-  const int rA = 32 * b - 2 * (K - 1);  // first row of the block's rings
-  const int T = S + 32 + kSwLg * (K - 1);
-  const int NP = (T + kSwQ - 1) / kSwQ;
+  float* const XT = reinterpret_cast<float*>(ls_sw_smem + lay.xt);
+  float* const XB = reinterpret_cast<float*>(ls_sw_smem + lay.xb);
+  uint8_t* const CF = ls_sw_smem + lay.cf;
+  // frame rows and column flags, where a sweep of this block holds a frame row
+  if (rA <= 0 || jb + 31 >= S - 1) {
+    for (int q = threadIdx.x; q < S; q += blockDim.x) {
+      XT[q] = A.x[q];
+      XB[q] = A.x[(size_t)(S - 1) * P + q];
+      CF[q] = A.colfl[q];
+    }
+  }
+  const unsigned long long* const gexpIn =
+      g > 0 ? A.gexp + ((size_t)b * (G - 1) + (g - 1)) * (A.RE + 1) * kSwGrpWords : nullptr;
 
-  if (warp == K) {
-    // ---- the copy warp: x0 / code rows and the first sweep's initial-x rows
+  if (warp == KG) {
+    // ---- the copy warp: x0 / code rows and the first group's initial-x rows
     auto issue = [&](int cp) {
       const int u = cp + kSwAH;  // use period
       for (int q = lane; q < nrw; q += 32) {
         const int r = rA + q;
         if (r < 0 || r > S - 1) continue;
-        const int dr = 32 * b - r;
+        const int dr = jb - r;
         const int kmin = dr > 0 ? (dr + 1) >> 1 : 0;
         const int off = dr - (kSwLg + 2) * kmin;
         const int n = u + ((off + 3) >> 2);
@@ -170,12 +355,14 @@ __global__ void __launch_bounds__(32 * (kSwMaxK + 1), 1) k_ls_sw(LsSwArgs A) {
         cp_async16(&X0R[q * kSwPC + sc], A.x0 + (size_t)r * P + 4 * n, true);
         cp_async4(&CR[q * kSwPC + sc], A.code + (size_t)r * P + 4 * n, true);
       }
-      for (int q = lane; q < 33; q += 32) {
-        const int r = 32 * b + q;
-        if (r > S - 1) continue;
-        const int n = u + 1 - ((q + 3) >> 2);
-        if (n < 0 || 4 * n >= P) continue;
-        cp_async16(&XR[q * kSwPX + ((4 * n) & (kSwPX - 1))], A.x + (size_t)r * P + 4 * n, true);
+      if (g == 0) {
+        for (int q = lane; q < 33; q += 32) {
+          const int r = jb + q;
+          if (r > S - 1) continue;
+          const int n = u + 1 - ((q + 3) >> 2);
+          if (n < 0 || 4 * n >= P) continue;
+          cp_async16(&XR[q * kSwPX + ((4 * n) & (kSwPX - 1))], A.x + (size_t)r * P + 4 * n, true);
+        }
       }
       cp_async_commit();
     };
@@ -191,39 +378,135 @@ __global__ void __launch_bounds__(32 * (kSwMaxK + 1), 1) k_ls_sw(LsSwArgs A) {
       }
     }
     cp_async_wait<0>();
+  } else if (warp == KG + 1) {
+    // ---- the group import warp: the previous group's last sweep, per period
+    // 4 records x 34 words (positions -2 .. 31) of the diagonals d - 1 the
+    // first sweep reads in that period; slot s of lane l is word l + 32 s
+    const bool on = g > 0 && rows_active(kF);
+    auto rec_of = [&](int u, int s) { return u * kSwQ + (lane + 32 * s) / 34; };
+    auto ok_of = [&](int u, int s) {
+      const int w = lane + 32 * s, r = rec_of(u, s);
+      return on && w < 4 * 34 && r >= 0 && r <= S + 31;
+    };
+    auto addr_of = [&](int u, int s) {
+      const int w = lane + 32 * s;
+      return gexpIn + (size_t)rec_of(u, s) * kSwGrpWords + (w % 34);
+    };
+    auto load = [&](int u, unsigned long long* v) {
+#pragma unroll
+      for (int s = 0; s < 5; ++s) v[s] = ok_of(u, s) ? ld_relaxed_u64(addr_of(u, s)) : 0ull;
+    };
+    auto store = [&](int u, unsigned long long* v) -> bool {
+      bool bad = false;
+#pragma unroll
+      for (int s = 0; s < 5; ++s) bad |= ok_of(u, s) && (unsigned)(v[s] >> 32) != tag;
+      long long tries = 0;
+      unsigned ns = 32;
+      while (__any_sync(FULL, bad)) {
+        if (++tries > A.spin_limit) {
+          if (lane == 0) atomicExch(A.err, 3 /* EQ_ERR_TIMEOUT */);
+          return false;
+        }
+        if ((tries & 63) == 0 && __any_sync(FULL, ld_relaxed_i32(A.err) != 0)) return false;
+        __nanosleep(ns);
+        ns = ns < 256 ? ns * 2 : 256;
+        bad = false;
+#pragma unroll
+        for (int s = 0; s < 5; ++s) {
+          if (ok_of(u, s) && (unsigned)(v[s] >> 32) != tag) {
+            v[s] = ld_relaxed_u64(addr_of(u, s));
+            bad |= (unsigned)(v[s] >> 32) != tag;
+          }
+        }
+      }
+#pragma unroll
+      for (int s = 0; s < 5; ++s) {
+        if (ok_of(u, s)) {
+          const int w = lane + 32 * s;
+          const int r = rec_of(u, s);  // diagonal r - 1
+          VP[((r - 1) & (kSwRD - 1)) * kSwRW + (w % 34)] =
+              __uint_as_float((unsigned)(v[s] & 0xffffffffull));
+        }
+      }
+      return true;
+    };
+    unsigned long long w0[5], w1[5], w2[5];
+    load(0, w0);
+    const bool ok0 = store(0, w0);
+    load(1, w0);
+    load(2, w1);
+    if (!ok0) s_abort[1] = 1;
+    __syncthreads();
+    if (!s_abort[1]) {
+      for (int cp = 0; cp < NP; ++cp) {
+        if (!store(cp + 1, w0)) s_abort[cp & 1] = 1;
+        load(cp + 3, w2);
+#pragma unroll
+        for (int s = 0; s < 5; ++s) {
+          w0[s] = w1[s];
+          w1[s] = w2[s];
+        }
+        __syncthreads();
+        if (s_abort[cp & 1]) break;
+      }
+    }
   } else {
-    // ---- sweep warp k
-    const int k = warp;
-    const int j0 = 32 * b - 2 * k, j = j0 + lane;
-    const bool interior = j >= 1 && j <= N, top = j == 0, bot = j == S - 1;
-    const bool idle = !(interior || top || bot);
-    const bool active = j0 <= S - 1 && j0 + 31 >= 0;
-    const bool hasFrame = __any_sync(FULL, top || bot);
-    const bool last = k == K - 1;
-    float* const VRk = VR + (size_t)k * kSwRD * kSwRW;
-    const float* const VRp = VR + (size_t)(k > 0 ? k - 1 : 0) * kSwRD * kSwRW;
-    float* const UIk = UI + (size_t)k * kSwRD;
-    const int rrow = 2 * (K - 1 - k) + lane;
-    const float* const X0row = X0R + rrow * kSwPC;
-    const uint8_t* const CRrow = CR + rrow * kSwPC;
-    const float* const XRl = XR + lane * kSwPX;
-    const float* const XRd = XR + (lane + 1) * kSwPX;
-    const float a = A.a, cr = A.cr;
-    // per-lane constants: the row's frame columns and its Passive flag
-    const float xL = interior ? A.x[(size_t)j * P] : 0.0f;
-    const float xR = interior ? A.x[(size_t)j * P + (S - 1)] : 0.0f;
-    const bool pasRow = MODE == kPassive && interior && A.rowfl[j] != 0;
-    const float* const xFrame = A.x + (bot ? (size_t)(S - 1) * P : 0);
-    // imports from block b-1's sweep warp k: lane t < 12 holds word t % 3 of
-    // record t / 3 (diagonal offset) of each period
-    const int jp = 32 * (b - 1) - 2 * k;
-    const bool impOn = b > 0 && jp <= S - 1 && jp + 31 >= 0;
+    // ---- sweep warp kk (k = kF + kk); warps past nk only meet the barriers
+    const int kk = warp, k = kF + kk;
+    const bool real = kk < nk;
+    const bool exportGroup = real && g < G - 1 && kk == nk - 1;
+    const bool runs = real && (rows_active(k) || (exportGroup && rows_active(k + 1)));
+    SwWarp W;
+    W.lane = lane;
+    W.S = S;
+    W.N = N;
+    W.k = k;
+    const int j0 = jb - 2 * kk;
+    W.j = j0 + lane;
+    W.interior = W.j >= 1 && W.j <= N;
+    W.top = W.j == 0;
+    W.bot = W.j == S - 1;
+    W.idle = !(W.interior || W.top || W.bot);
+    W.hasFrame = __any_sync(FULL, W.top || W.bot);
+    W.pasRow = MODE == kPassive && W.interior && A.rowfl[W.j] != 0;
+    W.xL = W.interior ? A.x[(size_t)W.j * P] : 0.0f;
+    W.xR = W.interior ? A.x[(size_t)W.j * P + (S - 1)] : 0.0f;
+    W.a = A.a;
+    W.cr = A.cr;
+    const int kr = real ? kk : 0;
+    W.own = VR + (size_t)kr * kSwRD * kSwRW;
+    W.prev = kk > 0 ? VR + (size_t)(kk - 1) * kSwRD * kSwRW : VP;
+    W.ui = UI + (size_t)kr * kSwRD;
+    const int rrow = 2 * (nk - 1 - kr) + lane;
+    W.x0row = X0R + (real ? rrow : 0) * kSwPC;
+    W.crow = CR + (real ? rrow : 0) * kSwPC;
+    W.xrl = XR + lane * kSwPX;
+    W.xrd = XR + (lane + 1) * kSwPX;
+    W.xt = XT;
+    W.xb = XB;
+    W.cf = CF;
+    W.edgeOut = (real && b < B - 1 && lane >= 30)
+                    ? A.edge + ((size_t)b * K + k) * A.RE * 4 + (lane == 30 ? 0 : 2)
+                    : nullptr;
+    W.gexpOut = exportGroup ? A.gexp + ((size_t)b * (G - 1) + g) * (A.RE + 1) * kSwGrpWords
+                            : nullptr;
+    W.xlast = (real && k == K - 1) ? A.x + (size_t)max(W.j, 0) * P - lane : nullptr;
+    W.tag = tag;
+    W.vcur = W.vprev = W.uprev = 0.0f;
+    W.cprev = 0u;
+    const bool firstX = g == 0 && kk == 0;
+    // fast range: every interior lane at 2 <= i <= N
+    const int lA = max(0, 1 - j0), lB = min(31, N - j0);
+    const int dF0 = lA <= lB ? lB + 2 : 1 << 30, dF1 = lA <= lB ? lA + N : -(1 << 30);
+    // halo imports from strip b-1's sweep warp k: lane t < 12 holds word
+    // {0, 2, 3}[t % 3] of record t / 3 of each period
+    const int jp = 32 * (b - 1) - 2 * k;  // strip b-1's rows of sweep k (the producer)
+    const bool impOn = real && b > 0 && jp <= S - 1 && jp + 31 >= 0;
+    const int iq = lane / 3, iwi = lane - 3 * (lane / 3);
+    const int iw = iwi == 0 ? 0 : iwi + 1;
     const unsigned long long* const edgeIn =
         impOn ? A.edge + ((size_t)(b - 1) * K + k) * A.RE * 4 : nullptr;
-    unsigned long long* const edgeOut =
-        (b < B - 1) ? A.edge + ((size_t)b * K + k) * A.RE * 4 : nullptr;
-    const int iq = lane / 3, iw = lane - 3 * (lane / 3);
-    auto imp_dd = [&](int u) { return u * kSwQ - kSwLg * k - 1 + iq; };
+    auto imp_dd = [&](int u) { return u * kSwQ - kSwLg * kk - 1 + iq; };
     auto imp_ok = [&](int u) {
       const int dd = imp_dd(u);
       return impOn && lane < 12 && dd >= -1 && dd <= S - 2;
@@ -231,7 +514,8 @@ __global__ void __launch_bounds__(32 * (kSwMaxK + 1), 1) k_ls_sw(LsSwArgs A) {
     auto imp_load = [&](int u) -> unsigned long long {
       return imp_ok(u) ? ld_relaxed_u64(edgeIn + (size_t)(imp_dd(u) + 32) * 4 + iw) : 0ull;
     };
-    // check and store the words of use period u (w: loaded earlier); false on timeout
+    float* const VRk = W.own;
+    float* const UIk = UI + (size_t)kr * kSwRD;
     auto imp_store = [&](int u, unsigned long long w) -> bool {
       const bool need = imp_ok(u);
       bool bad = need && (unsigned)(w >> 32) != tag;
@@ -253,139 +537,49 @@ __global__ void __launch_bounds__(32 * (kSwMaxK + 1), 1) k_ls_sw(LsSwArgs A) {
       if (need) {
         const int s = imp_dd(u) & (kSwRD - 1);
         const float v = __uint_as_float((unsigned)(w & 0xffffffffull));
-        if (iw == 0)
+        if (iw == 2)
           UIk[s] = v;
         else
-          VRk[s * kSwRW + (iw - 1)] = v;
+          VRk[s * kSwRW + (iw == 0 ? 0 : 1)] = v;
       }
       return true;
     };
-    bool ok = true;
-    unsigned long long w0 = imp_load(0);
-    ok = imp_store(0, w0);  // the prologue: imports of period 0
-    w0 = imp_load(1);
-    unsigned long long w1 = imp_load(2);
-    if (!ok) s_abort[1] = 1;  // the prologue counts as period -1
+    unsigned long long h0 = imp_load(0);
+    const bool ok0 = imp_store(0, h0);  // the prologue: imports of period 0
+    h0 = imp_load(1);
+    unsigned long long h1 = imp_load(2);
+    if (!ok0) s_abort[1] = 1;  // the prologue counts as period -1
     __syncthreads();
-    const bool go = !s_abort[1];
-
-    float vcur = 0.0f, vprev = 0.0f, uprev = 0.0f;
-    unsigned cprev = 0;
-    const unsigned actMask =
-        MODE == kRow ? (kCodeRowLeft | kCodeRowRight) : MODE == kCol ? (kCodeColUp | kCodeColDown) : 0u;
-    for (int cp = 0; go && cp < NP; ++cp) {
-      bool fine = imp_store(cp + 1, w0);
-      if (!fine) s_abort[cp & 1] = 1;
-      w0 = w1;
-      w1 = imp_load(cp + 3);
-      if (active && fine) {
+    if (!s_abort[1]) {
+      for (int cp = 0; cp < NP; ++cp) {
+        const bool fine = imp_store(cp + 1, h0);
+        if (!fine) s_abort[cp & 1] = 1;
+        h0 = h1;
+        h1 = imp_load(cp + 3);
+        if (runs && fine) {
+          const int dp = cp * kSwQ - kSwLg * kk;
+          if (dp >= dF0 && dp + kSwQ - 1 <= dF1) {
+            if (firstX) {
 #pragma unroll
-        for (int t = 0; t < kSwQ; ++t) {
-          const int d = cp * kSwQ + t - kSwLg * k;
-          if (d < 0 || d > S + 31) continue;
-          const int i = d - lane;
-          float R, D;
-          if (k > 0) {
-            const float* const row = VRp + ((d - 1) & (kSwRD - 1)) * kSwRW;
-            R = row[lane];
-            D = row[lane + 1];
-          } else {
-            R = XRl[(i + 1) & (kSwPX - 1)];
-            D = XRd[i & (kSwPX - 1)];
-          }
-          const float Ui = UIk[(d - 1) & (kSwRD - 1)];
-          float U = __shfl_up_sync(FULL, vcur, 1);
-          if (lane == 0) U = Ui;
-          const int ci = i & (kSwPC - 1);
-          const float X0 = X0row[ci];
-          const unsigned cd = CRrow[ci];
-          const float gs = gs_update(X0, a, fadd(fadd(fadd(R, vcur), D), U), cr);
-          const bool fix = MODE == kCol && lane == 0 && (cd & kCodeAboveDown) != 0;
-          const bool fastL = idle || top || bot ||
-                             (interior && (unsigned)(i - 2) <= (unsigned)(N - 2) &&
-                              (cprev & actMask) == 0u && !fix);
-          float vnew, post;
-          if (__all_sync(FULL, fastL)) {
-            vnew = gs;
-            post = vcur;
-            if (hasFrame) {  // frame-row lanes: the frame cell as the sweep sees it
-              const bool fl = top || bot;
-              const bool inr = (unsigned)i < (unsigned)S;
-              const int ic = min(max(i, 0), S - 1);
-              float xf = 0.0f;
-              unsigned cf = 0, cfp = 0;
-              if (fl) {
-                xf = xFrame[ic];
-                if (MODE == kPassive) {
-                  cf = A.colfl[ic];
-                  cfp = A.colfl[min(max(i - 1, 0), S - 1)];
-                }
-              }
-              if (fl) vnew = inr ? ((MODE == kPassive && top && k > 0 && cf) ? D : xf) : vcur;
-              if (MODE == kPassive) {
-                const float vdown = __shfl_down_sync(FULL, vnew, 1);
-                const bool pc = (unsigned)(i - 2) <= (unsigned)(N - 1) && cfp != 0u;
-                if (fl) post = pc ? (top ? vdown : uprev) : vcur;
-              } else if (fl) {
-                post = vcur;
-              }
+              for (int q = 0; q < kSwQ; ++q) sw_step<MODE, true, true>(W, dp + q);
+            } else {
+#pragma unroll
+              for (int q = 0; q < kSwQ; ++q) sw_step<MODE, true, false>(W, dp + q);
             }
           } else {
-            // ---- the general rules, every lane
-            vnew = vcur;
-            if (interior) {
-              if ((unsigned)(i - 1) < (unsigned)N)
-                vnew = gs;
-              else if (i == 0)
-                vnew = (MODE == kPassive && k > 0 && pasRow) ? R : xL;
-              else if (i == S - 1)
-                vnew = xR;
-            } else if (top || bot) {
-              if ((unsigned)i < (unsigned)S) {
-                const float xf = xFrame[i];
-                vnew = (MODE == kPassive && top && k > 0 && A.colfl[i]) ? D : xf;
-              }
-            } else {
-              vnew = 0.0f;
-            }
-            const float vdown = __shfl_down_sync(FULL, vnew, 1);
-            const int im1 = i - 1;
-            post = vcur;
-            if (interior) {
-              if ((unsigned)(im1 - 1) < (unsigned)N) {
-                if (MODE == kRow)
-                  post = (cprev & kCodeRowRight) ? -vnew : ((cprev & kCodeRowLeft) ? -vprev : vcur);
-                else if (MODE == kCol)
-                  post = (cprev & kCodeColUp) ? -uprev : ((cprev & kCodeColDown) ? -vdown : vcur);
-              } else if (im1 == 0) {
-                post = pasRow ? vnew : vcur;
-              } else if (im1 == S - 1) {
-                post = pasRow ? vprev : vcur;
-              }
-            } else if (top || bot) {
-              if (MODE == kPassive && (unsigned)(im1 - 1) < (unsigned)N && A.colfl[im1])
-                post = top ? vdown : uprev;
-            } else {
-              post = 0.0f;
+            for (int q = 0; q < kSwQ; ++q) {
+              const int d = dp + q;
+              if (d < 0 || d > S + 31) continue;
+              if (firstX)
+                sw_step<MODE, false, true>(W, d);
+              else
+                sw_step<MODE, false, false>(W, d);
             }
           }
-          float* const wrow = VRk + ((d - 1) & (kSwRD - 1)) * kSwRW;
-          wrow[lane + 2] = post;
-          if (fix && (interior || bot) && (unsigned)(i - 1) < (unsigned)N) wrow[1] = -vnew;
-          if (edgeOut) {
-            if (lane == 31) st_relaxed_u64_sw(edgeOut + (size_t)d * 4, sw_pack(vnew, tag));
-            if (lane >= 30 && d >= 1)
-              st_relaxed_u64_sw(edgeOut + (size_t)(d - 1) * 4 + (lane - 29), sw_pack(post, tag));
-          }
-          if (last && interior && (unsigned)(i - 1) < (unsigned)N) A.x[(size_t)j * P + i] = vnew;
-          vprev = vcur;
-          vcur = vnew;
-          uprev = U;
-          cprev = cd;
         }
+        __syncthreads();
+        if (s_abort[cp & 1]) break;
       }
-      __syncthreads();
-      if (s_abort[cp & 1]) break;
     }
   }
   // ---- completion: the last block to finish advances the epoch
@@ -393,7 +587,7 @@ __global__ void __launch_bounds__(32 * (kSwMaxK + 1), 1) k_ls_sw(LsSwArgs A) {
   if (threadIdx.x == 0) {
     __threadfence();
     const unsigned prev = atom_add_acq_rel_u32(&A.ctr[1], 1u);
-    if (prev == (unsigned)B - 1u) atomicAdd(&A.ctr[2], 1u);
+    if (prev == (unsigned)(B * G) - 1u) atomicAdd(&A.ctr[2], 1u);
   }
 }
 

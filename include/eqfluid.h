@@ -515,6 +515,8 @@ int eq_fluid_set_concurrency(eq_fluid* h, int mask);
  * streams (it holds few SMs, so it runs beside the critical path's solve);
  * else the multi-block wavefront. 1 = the multi-block wavefront always.
  * 2 = the cluster form (staged or streamed) wherever it applies.
+ * 3 = the strip wavefront (one launch per 20 sweeps over 32-row strips and
+ * groups of sweeps, blocks chained through tagged exports; any size).
  * get_solver reports the blocks per cluster of the cluster form (0 = it
  * does not apply); get_cluster_form its form: 0 = none, 1 = strips staged
  * whole, 2 = strips streamed. */
@@ -525,6 +527,10 @@ int eq_fluid_get_cluster_form(eq_fluid* h, int* form);
  * by default 3 steps for N >= 192 and 2 below, the fastest measured; the
  * longest interval up to the cap that fits in shared memory is used). */
 int eq_fluid_set_cluster_interval(eq_fluid* h, int max_m);
+/* Sweep groups per strip of the strip wavefront (solver 3): each strip's
+ * sweeps of one launch are split over `groups` blocks (1..5; 0 = by grid
+ * size, about one block per SM). */
+int eq_fluid_set_strip_groups(eq_fluid* h, int groups);
 
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their own
  * work or events against the handle's launches. */

@@ -64,6 +64,30 @@ def test_strip_lin_solve_bitexact(eqlib, size, K, mode):
     f.close()
 
 
+@pytest.mark.parametrize("size,K,groups", [(66, 20, 1), (66, 20, 3), (97, 13, 2), (258, 20, 5),
+                                           (514, 20, 2), (1026, 20, 1), (1026, 20, 4),
+                                           (1026, 7, 5)])
+@pytest.mark.parametrize("mode", [ROW, COL, PAS])
+def test_strip_lin_solve_groups_bitexact(eqlib, size, K, groups, mode):
+    """Every split of a strip's sweeps over blocks gives the same bits."""
+    L = _lib.load()
+    f, r, rng = scene(size, K, size * 11 + K + mode + groups)
+    _lib.check(L.eq_fluid_set_strip_groups(f.handle, groups))
+    n = size * size
+    x = rng.normal(size=n).astype(np.float32)
+    x0 = rng.normal(size=n).astype(np.float32)
+    a = np.float32(0.61)
+    c = np.float32(1.0) + np.float32(4.0) * a
+    ref = x.copy()
+    oracle.lin_solve(mode, ref, x0, a, c, size, K, r.cells)
+    f.write_field(2, x)
+    f.write_field(4, x0)
+    _lib.check(L.eq_fluid_lin_solve(f.handle, mode, 2, 4, a, c))
+    f.synchronize()
+    assert_bitexact(f.read_field(2), ref, f"strip groups {groups} size {size} mode {mode}", size)
+    f.close()
+
+
 def test_strip_lin_solve_repeated_launches(eqlib):
     """Thirty solves on the same buffers, each from fresh inputs: every launch
     must ignore the previous launch's exports (the epoch tag)."""
