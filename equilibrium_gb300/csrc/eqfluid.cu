@@ -42,6 +42,7 @@ int fail(int code, const std::string& msg) {
 
 constexpr int kMaxSweepsPerLaunch = 64;
 constexpr int kSwMaxGroups = 5;  // sweep groups per strip of the strip wavefront
+constexpr int kSwStaticSmem = 1024;  // reserved beside its dynamic shared memory
 constexpr long long kDefaultSpinLimit = 1ll << 22;
 
 }  // namespace
@@ -464,7 +465,7 @@ bool sw_fits(const eq_fluid* h) {
   }
   const int K = (int)std::min<int64_t>(eqk::kSwMaxK, std::max<int64_t>(h->frames, 1));
   const int G = sw_groups_for(h, K);
-  return eqk::ls_sw_layout((K + G - 1) / G, (int)h->S).total <= (size_t)optin;
+  return eqk::ls_sw_layout((K + G - 1) / G, (int)h->S).total <= (size_t)(optin - kSwStaticSmem);
 }
 
 // lin_solve by the strip wavefront (lssw.cuh), kSwMaxK sweeps per launch,
@@ -476,12 +477,13 @@ int launch_lin_solve_sw(eq_fluid* h, int mode, float* x, const float* x0, float 
   if (!bit || !(raised.load() & bit)) {
     int optin = 0;
     EQ_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+    const int dyn = optin - kSwStaticSmem;  // room for the kernel's static shared words
     EQ_CUDA(cudaFuncSetAttribute(eqk::k_ls_sw<eqk::kRow>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
     EQ_CUDA(cudaFuncSetAttribute(eqk::k_ls_sw<eqk::kCol>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
     EQ_CUDA(cudaFuncSetAttribute(eqk::k_ls_sw<eqk::kPassive>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
     raised.fetch_or(bit);
   }
   const int S = (int)h->S;
