@@ -71,7 +71,9 @@ constexpr int kSwRD = 16;     // diagonals kept per sweep ring
 constexpr int kSwRW = 36;     // floats per ring row: positions -2 .. 33
 constexpr int kSwPC = 128;    // columns of the x0 / code rings
 constexpr int kSwPX = 32;     // columns of the initial-x ring
-constexpr int kSwAH = 3;      // a chunk copy is issued kSwAH periods before its use
+constexpr int kSwAH = 5;      // a chunk copy is issued kSwAH periods before its use
+constexpr int kSwAHI = 4;     // an import load is checked kSwAHI periods after its issue
+constexpr int kSwSlack = 6;   // a block starts once its producers are this many periods ahead
 constexpr int kSwMaxK = 20;   // sweeps per launch
 constexpr int kSwMaxKG = 20;  // sweeps per block
 constexpr int kSwGrpWords = 36;  // words per group-export record (34 used)
@@ -430,22 +432,30 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
       }
       return true;
     };
-    unsigned long long w0[5], w1[5], w2[5];
-    load(0, w0);
-    const bool ok0 = store(0, w0);
-    load(1, w0);
-    load(2, w1);
+    // loads in flight: wv[q] holds the words of use period cp + 1 + q
+    unsigned long long wv[kSwAHI][5];
+    load(0, wv[0]);
+    bool ok0 = store(0, wv[0]);
+    // start only once the previous group is kSwSlack periods ahead, so that
+    // the loads issued kSwAHI periods early find their words written
+    if (ok0 && on) {
+      const int us = min(1 + kSwSlack, (S + 31) / kSwQ);
+      unsigned long long ws[5];
+      load(us, ws);
+      ok0 = store(us, ws);
+    }
+#pragma unroll
+    for (int q = 0; q < kSwAHI; ++q) load(1 + q, wv[q]);
     if (!ok0) s_abort[1] = 1;
     __syncthreads();
     if (!s_abort[1]) {
       for (int cp = 0; cp < NP; ++cp) {
-        if (!store(cp + 1, w0)) s_abort[cp & 1] = 1;
-        load(cp + 3, w2);
+        if (!store(cp + 1, wv[0])) s_abort[cp & 1] = 1;
 #pragma unroll
-        for (int s = 0; s < 5; ++s) {
-          w0[s] = w1[s];
-          w1[s] = w2[s];
-        }
+        for (int q = 0; q + 1 < kSwAHI; ++q)
+#pragma unroll
+          for (int s = 0; s < 5; ++s) wv[q][s] = wv[q + 1][s];
+        load(cp + 1 + kSwAHI, wv[kSwAHI - 1]);
         __syncthreads();
         if (s_abort[cp & 1]) break;
       }
@@ -544,18 +554,25 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
       }
       return true;
     };
-    unsigned long long h0 = imp_load(0);
-    const bool ok0 = imp_store(0, h0);  // the prologue: imports of period 0
-    h0 = imp_load(1);
-    unsigned long long h1 = imp_load(2);
+    unsigned long long hv[kSwAHI];  // hv[q]: the words of use period cp + 1 + q
+    bool ok0 = imp_store(0, imp_load(0));  // the prologue: imports of period 0
+    // start only once strip b-1 is kSwSlack periods ahead, so that the loads
+    // issued kSwAHI periods early find their words written
+    if (ok0 && impOn) {
+      const int us = min(1 + kSwSlack, (S - 1 + kSwLg * kk) / kSwQ);
+      if (us >= 1) ok0 = imp_store(us, imp_load(us));
+    }
+#pragma unroll
+    for (int q = 0; q < kSwAHI; ++q) hv[q] = imp_load(1 + q);
     if (!ok0) s_abort[1] = 1;  // the prologue counts as period -1
     __syncthreads();
     if (!s_abort[1]) {
       for (int cp = 0; cp < NP; ++cp) {
-        const bool fine = imp_store(cp + 1, h0);
+        const bool fine = imp_store(cp + 1, hv[0]);
         if (!fine) s_abort[cp & 1] = 1;
-        h0 = h1;
-        h1 = imp_load(cp + 3);
+#pragma unroll
+        for (int q = 0; q + 1 < kSwAHI; ++q) hv[q] = hv[q + 1];
+        hv[kSwAHI - 1] = imp_load(cp + 1 + kSwAHI);
         if (runs && fine) {
           const int dp = cp * kSwQ - kSwLg * kk;
           if (dp >= dF0 && dp + kSwQ - 1 <= dF1) {
