@@ -120,6 +120,7 @@ def load(path: str = LIB_PATH):
         "eq_fluid_get_cluster_form": (i32, [H, ctypes.POINTER(ctypes.c_int)]),
         "eq_fluid_set_cluster_interval": (i32, [H, i32]),
         "eq_fluid_set_strip_groups": (i32, [H, i32]),
+        "eq_fluid_set_strip_slack": (i32, [H, i32]),
         "eq_fluid_get_stream": (i32, [H, PP]),
         "eq_fluid_set_profiling": (i32, [H, i32]),
         "eq_fluid_kernel_stats": (i32, [H, i32, ctypes.POINTER(ctypes.c_double),

@@ -136,6 +136,7 @@ struct eq_fluid {
   unsigned long long* sw_gexp[3] = {};  // group exports [strips][groups-1][records+1][36]
   unsigned* sw_ctr[3] = {};
   int sw_groups = 0;  // sweep groups per strip (0: by size)
+  int sw_slack = 0;   // periods a block's producers must be ahead before it starts
 
   size_t grid_elems() const { return (size_t)P * S; }
 };
@@ -511,6 +512,7 @@ int launch_lin_solve_sw(eq_fluid* h, int mode, float* x, const float* x0, float 
     A.G = G;
     A.KG = KG;
     A.RE = eqk::ls_sw_records(S);
+    A.slack = h->sw_slack;
     A.a = a;
     A.cr = c_recip;
     const size_t smem = eqk::ls_sw_layout(KG, S).total;
@@ -1405,6 +1407,13 @@ int eq_fluid_set_strip_groups(eq_fluid* h, int groups) {
   if (!h) return fail(EQ_ERR_ARG, "null handle");
   if (groups < 0 || groups > kSwMaxGroups) return fail(EQ_ERR_ARG, "groups must be 0..5");
   h->sw_groups = groups;
+  return EQ_OK;
+}
+
+int eq_fluid_set_strip_slack(eq_fluid* h, int periods) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  if (periods < 0 || periods > 64) return fail(EQ_ERR_ARG, "periods must be 0..64");
+  h->sw_slack = periods;
   return EQ_OK;
 }
 

@@ -73,7 +73,6 @@ constexpr int kSwPC = 128;    // columns of the x0 / code rings
 constexpr int kSwPX = 32;     // columns of the initial-x ring
 constexpr int kSwAH = 5;      // a chunk copy is issued kSwAH periods before its use
 constexpr int kSwAHI = 4;     // an import load is checked kSwAHI periods after its issue
-constexpr int kSwSlack = 6;   // a block starts once its producers are this many periods ahead
 constexpr int kSwMaxK = 20;   // sweeps per launch
 constexpr int kSwMaxKG = 20;  // sweeps per block
 constexpr int kSwGrpWords = 36;  // words per group-export record (34 used)
@@ -91,6 +90,7 @@ struct LsSwArgs {
   int* err;
   long long spin_limit;
   int S, P, K, B, G, KG, RE;
+  int slack;  // a block starts once its producers are this many periods ahead
   float a, cr;
 };
 
@@ -398,7 +398,9 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
 #pragma unroll
       for (int s = 0; s < 5; ++s) v[s] = ok_of(u, s) ? ld_relaxed_u64(addr_of(u, s)) : 0ull;
     };
-    auto store = [&](int u, unsigned long long* v) -> bool {
+    // spin until the words of use period u carry the launch's tag (bounded);
+    // with put, copy them into the previous-sweep ring
+    auto settle = [&](int u, unsigned long long* v, bool put) -> bool {
       bool bad = false;
 #pragma unroll
       for (int s = 0; s < 5; ++s) bad |= ok_of(u, s) && (unsigned)(v[s] >> 32) != tag;
@@ -423,7 +425,7 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
       }
 #pragma unroll
       for (int s = 0; s < 5; ++s) {
-        if (ok_of(u, s)) {
+        if (put && ok_of(u, s)) {
           const int w = lane + 32 * s;
           const int r = rec_of(u, s);  // diagonal r - 1
           VP[((r - 1) & (kSwRD - 1)) * kSwRW + (w % 34)] =
@@ -435,14 +437,14 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
     // loads in flight: wv[q] holds the words of use period cp + 1 + q
     unsigned long long wv[kSwAHI][5];
     load(0, wv[0]);
-    bool ok0 = store(0, wv[0]);
-    // start only once the previous group is kSwSlack periods ahead, so that
+    bool ok0 = settle(0, wv[0], true);
+    // start only once the previous group is A.slack periods ahead, so that
     // the loads issued kSwAHI periods early find their words written
     if (ok0 && on) {
-      const int us = min(1 + kSwSlack, (S + 31) / kSwQ);
+      const int us = min(1 + A.slack, (S + 31) / kSwQ);
       unsigned long long ws[5];
       load(us, ws);
-      ok0 = store(us, ws);
+      ok0 = settle(us, ws, false);
     }
 #pragma unroll
     for (int q = 0; q < kSwAHI; ++q) load(1 + q, wv[q]);
@@ -450,7 +452,7 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
     __syncthreads();
     if (!s_abort[1]) {
       for (int cp = 0; cp < NP; ++cp) {
-        if (!store(cp + 1, wv[0])) s_abort[cp & 1] = 1;
+        if (!settle(cp + 1, wv[0], true)) s_abort[cp & 1] = 1;
 #pragma unroll
         for (int q = 0; q + 1 < kSwAHI; ++q)
 #pragma unroll
@@ -526,7 +528,9 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
     };
     float* const VRk = W.own;
     float* const UIk = UI + (size_t)kr * kSwRD;
-    auto imp_store = [&](int u, unsigned long long w) -> bool {
+    // spin until the words of use period u carry the launch's tag (bounded);
+    // with put, copy them into the rings
+    auto imp_store = [&](int u, unsigned long long w, bool put = true) -> bool {
       const bool need = imp_ok(u);
       bool bad = need && (unsigned)(w >> 32) != tag;
       long long tries = 0;
@@ -544,7 +548,7 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
           bad = (unsigned)(w >> 32) != tag;
         }
       }
-      if (need) {
+      if (put && need) {
         const int s = imp_dd(u) & (kSwRD - 1);
         const float v = __uint_as_float((unsigned)(w & 0xffffffffull));
         if (iw == 2)
@@ -556,11 +560,11 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
     };
     unsigned long long hv[kSwAHI];  // hv[q]: the words of use period cp + 1 + q
     bool ok0 = imp_store(0, imp_load(0));  // the prologue: imports of period 0
-    // start only once strip b-1 is kSwSlack periods ahead, so that the loads
+    // start only once strip b-1 is A.slack periods ahead, so that the loads
     // issued kSwAHI periods early find their words written
     if (ok0 && impOn) {
-      const int us = min(1 + kSwSlack, (S - 1 + kSwLg * kk) / kSwQ);
-      if (us >= 1) ok0 = imp_store(us, imp_load(us));
+      const int us = min(1 + A.slack, (S - 1 + kSwLg * kk) / kSwQ);
+      if (us >= 1) ok0 = imp_store(us, imp_load(us), false);
     }
 #pragma unroll
     for (int q = 0; q < kSwAHI; ++q) hv[q] = imp_load(1 + q);

@@ -531,6 +531,10 @@ int eq_fluid_set_cluster_interval(eq_fluid* h, int max_m);
  * sweeps of one launch are split over `groups` blocks (1..5; 0 = by grid
  * size, about one block per SM). */
 int eq_fluid_set_strip_groups(eq_fluid* h, int groups);
+/* Periods (of 4 wavefront steps) a strip-wavefront block waits, before its
+ * first step, for the blocks it reads from to be ahead of it (0..64; 0 by
+ * default). */
+int eq_fluid_set_strip_slack(eq_fluid* h, int periods);
 
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their own
  * work or events against the handle's launches. */

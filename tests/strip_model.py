@@ -1,0 +1,317 @@
+"""A CPU model of the strip-wavefront lin_solve kernel (csrc/lssw.cuh), lane
+by lane, used to check its schedule and index formulas against the oracle.
+
+Block (b, g) owns strip b and the sweeps [g KG, g KG + nk). The model
+follows the kernel's per-period order (chunk copies issued at the period's
+start, imports, then each sweep warp's steps) and every shared-memory slot
+carries the key of the value it holds and the first period in which a read
+may see it; each read that the result depends on checks both, so a value
+read before its barrier, or after its slot was reused, fails the check.
+"""
+import numpy as np
+
+ROW, COL, PAS = 0, 1, 2
+C_WALL, C_RL, C_RR, C_CD, C_CU, C_AD, C_CF = 1, 2, 4, 8, 16, 32, 64
+F = np.float32
+
+
+class Cfg:
+    """The kernel's constants (lssw.cuh kSw*)."""
+    Q = 4     # steps per period
+    LG = 4    # steps between consecutive sweeps
+    RD = 16   # diagonals per sweep ring
+    RW = 36   # floats per ring row (positions -2 .. 33)
+    PC = 128  # columns of the x0 / code rings
+    PX = 32   # columns of the initial-x ring
+    AH = 5    # a chunk copy is issued AH periods before its use period
+
+
+def derive_codes(cells, S):
+    """The per-cell boundary codes of the host's derive_codes."""
+    N = S - 2
+    wall = lambda i, j: cells[j * S + i] != 0
+    code = np.zeros((S, S), np.uint8)
+    rowfl = np.zeros(S, np.uint8)
+    colfl = np.zeros(S, np.uint8)
+    for j in range(S):
+        for i in range(S):
+            c = 0
+            w = wall(i, j)
+            if w:
+                c |= C_WALL
+            if not w and 1 <= i <= N and 1 <= j <= N:
+                rowfl[j] = colfl[i] = 1
+                if wall(i + 1, j):
+                    c |= C_RR
+                elif wall(i - 1, j):
+                    c |= C_RL
+                if wall(i, j - 1):
+                    c |= C_CU
+                elif wall(i, j + 1):
+                    c |= C_CD
+            if j >= 2 and j - 1 <= N and 1 <= i <= N and w and not wall(i, j - 1) \
+                    and not wall(i, j - 2):
+                c |= C_AD
+            code[j, i] |= c
+    for i in range(S):
+        if colfl[i]:
+            code[:, i] |= C_CF
+    return code, rowfl, colfl
+
+
+class Tracked:
+    """Shared memory whose slots remember (key, first period a read may see it)."""
+
+    def __init__(self, shape, dtype):
+        self.v = np.zeros(shape, dtype)
+        self.key = np.empty(shape, object)
+        self.vfrom = np.full(shape, 1 << 30, np.int64)
+
+    def write(self, idx, val, key, vfrom):
+        self.v[idx] = val
+        self.key[idx] = key
+        self.vfrom[idx] = vfrom
+
+    def read(self, idx, key, period, use, what):
+        if use:
+            if self.key[idx] != key:
+                raise AssertionError(f"{what}: slot {idx} holds {self.key[idx]}, wanted {key}")
+            if self.vfrom[idx] > period:
+                raise AssertionError(f"{what}: {key} read in period {period}, valid from "
+                                     f"{self.vfrom[idx]}")
+        return self.v[idx]
+
+
+def strips(S, K):
+    return (S + 2 * (K - 1) + 31) // 32
+
+
+def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
+    """One launch over K sweeps in G sweep groups: x with the last sweep's raw
+    interior values (the caller then applies set_boundaries), and the number
+    of (warp, step)s and of those on the fast path."""
+    Q, LG, RD, PC, PX, AH = cfg.Q, cfg.LG, cfg.RD, cfg.PC, cfg.PX, cfg.AH
+    N = S - 2
+    a = F(a)
+    cr = F(F(1.0) / F(c))
+    code, rowfl, colfl = derive_codes(cells, S)
+    xin = x.reshape(S, S).copy()
+    xout = x.reshape(S, S).copy()
+    x0g = x0.reshape(S, S)
+    B = strips(S, K)
+    KG = (K + G - 1) // G
+    G = (K + KG - 1) // KG
+    RE = S + 32
+    TAG = 7
+    edge = np.zeros((B, K, RE, 4), np.float32)  # [post30, -, uval31, post31]
+    etag = np.zeros((B, K, RE, 4), np.int64)
+    gexp = np.zeros((B, G, RE + 1, 36), np.float32)  # record d: positions -2..31 of d-1
+    gtag = np.zeros((B, G, RE + 1, 36), np.int64)
+    lanes = np.arange(32)
+    steps = fast = 0
+
+    def act(bb, k):
+        j0 = 32 * bb - 2 * k
+        return j0 <= S - 1 and j0 + 31 >= 0
+
+    for b in range(B):
+        for g in range(G):
+            kF = g * KG
+            nk = min(K, kF + KG) - kF
+            jb = 32 * b - 2 * kF
+            nrw = 32 + 2 * (nk - 1)
+            rA = jb - 2 * (nk - 1)
+            NP = (S + 32 + LG * (nk - 1) + Q - 1) // Q
+            VR = Tracked((nk, RD, cfg.RW), np.float32)
+            UI = Tracked((nk, RD), np.float32)
+            VP = Tracked((RD, cfg.RW), np.float32)
+            X0R = Tracked((nrw, PC), np.float32)
+            CR = Tracked((nrw, PC), np.uint8)
+            XR = Tracked((33, PX), np.float32)
+
+            def load_chunks(cp):
+                u = cp + AH
+                for q in range(nrw):
+                    r = rA + q
+                    if r < 0 or r > S - 1:
+                        continue
+                    dr = jb - r
+                    kmin = (dr + 1) >> 1 if dr > 0 else 0
+                    n = u + ((dr - (LG + 2) * kmin + 3) >> 2)
+                    if n < 0 or 4 * n >= P:
+                        continue
+                    for e in range(4):
+                        col = 4 * n + e
+                        X0R.write((q, col % PC), x0g[r, col] if col < S else F(0),
+                                  ("x0", r, col), u)
+                        CR.write((q, col % PC), code[r, col] if col < S else 0,
+                                 ("cd", r, col), u)
+                if g == 0:
+                    for q in range(33):
+                        r = jb + q
+                        if r > S - 1:
+                            continue
+                        n = u + 1 - ((q + 3) >> 2)
+                        if n < 0 or 4 * n >= P:
+                            continue
+                        for e in range(4):
+                            col = 4 * n + e
+                            XR.write((q, col % PX), xin[r, col] if col < S else F(0),
+                                     ("x", r, col), u)
+
+            def halo_import(kk, cp):
+                k = kF + kk
+                if b == 0 or not act(b - 1, k):
+                    return
+                lo = (cp + 1) * Q - LG * kk - 1
+                for dd in range(lo, lo + Q):
+                    if dd < -1 or dd > S - 2:
+                        continue
+                    rec = dd + 32
+                    assert (etag[b - 1, k, rec, [0, 2, 3]] == TAG).all(), ("halo", b, k, rec)
+                    s = dd % RD
+                    VR.write((kk, s, 0), edge[b - 1, k, rec, 0], ("vr", k, dd, -2), cp + 1)
+                    UI.write((kk, s), edge[b - 1, k, rec, 2], ("ui", k, dd), cp + 1)
+                    VR.write((kk, s, 1), edge[b - 1, k, rec, 3], ("vr", k, dd, -1), cp + 1)
+
+            def group_import(cp):
+                if g == 0 or not act(b, kF):
+                    return
+                for d in range((cp + 1) * Q, (cp + 2) * Q):
+                    if d < 0 or d > S + 31:
+                        continue
+                    assert (gtag[b, g - 1, d, :34] == TAG).all(), ("group", b, g, d)
+                    for p in range(-2, 32):
+                        VP.write(((d - 1) % RD, p + 2), gexp[b, g - 1, d, p + 2],
+                                 ("vr", kF - 1, d - 1, p), cp + 1)
+
+            for cp in range(-AH - 1, 0):
+                load_chunks(cp)
+            for kk in range(nk):
+                halo_import(kk, -1)
+            group_import(-1)
+            vcur = np.zeros((nk, 32), np.float32)
+            vprev = np.zeros((nk, 32), np.float32)
+            uprev = np.zeros((nk, 32), np.float32)
+            cprev = np.zeros((nk, 32), np.uint8)
+            for cp in range(NP):
+                load_chunks(cp)
+                group_import(cp)
+                for kk in range(nk):
+                    halo_import(kk, cp)
+                    k = kF + kk
+                    # a group's last sweep also runs (all lanes idle) when only the
+                    # next group's first sweep has grid rows: it forwards the halo
+                    if not act(b, k) and not (g < G - 1 and kk == nk - 1 and act(b, k + 1)):
+                        continue
+                    j0 = jb - 2 * kk
+                    j = j0 + lanes
+                    interior = (j >= 1) & (j <= N)
+                    top, bot = j == 0, j == S - 1
+                    idle = ~(interior | top | bot)
+                    il = np.nonzero(interior)[0]
+                    dF0 = il.max() + 2 if il.size else 1 << 30
+                    dF1 = il.min() + N if il.size else -(1 << 30)
+                    for t in range(Q):
+                        d = cp * Q + t - LG * kk
+                        if d < 0 or d > S + 31:
+                            continue
+                        steps += 1
+                        i = d - lanes
+                        jj, ii = np.clip(j, 0, S - 1), np.clip(i, 0, S - 1)
+                        gsl = interior & (i >= 1) & (i <= N)
+                        useR = gsl | (interior & (i == 0) & (mode == PAS) & (k > 0) &
+                                      (rowfl[jj] != 0))
+                        useD = gsl | (top & (i >= 0) & (i <= S - 1) & (mode == PAS) & (k > 0) &
+                                      (colfl[ii] != 0))
+                        R = np.zeros(32, np.float32)
+                        D = np.zeros(32, np.float32)
+                        for l in range(32):
+                            if kk > 0:
+                                sl = (kk - 1, (d - 1) % RD)
+                                R[l] = VR.read(sl + (l,), ("vr", k - 1, d - 1, l - 2), cp, useR[l], "R")
+                                D[l] = VR.read(sl + (l + 1,), ("vr", k - 1, d - 1, l - 1), cp, useD[l], "D")
+                            elif g > 0:
+                                sl = ((d - 1) % RD,)
+                                R[l] = VP.read(sl + (l,), ("vr", k - 1, d - 1, l - 2), cp, useR[l], "R")
+                                D[l] = VP.read(sl + (l + 1,), ("vr", k - 1, d - 1, l - 1), cp, useD[l], "D")
+                            else:
+                                R[l] = XR.read((l, (i[l] + 1) % PX), ("x", j[l], i[l] + 1), cp, useR[l], "XR")
+                                D[l] = XR.read((l + 1, i[l] % PX), ("x", j[l] + 1, i[l]), cp, useD[l], "XR")
+                        U = np.empty(32, np.float32)
+                        U[1:] = vcur[kk, :-1]
+                        U[0] = UI.read((kk, (d - 1) % RD), ("ui", k, d - 1), cp, bool(gsl[0]), "UI")
+                        X0 = np.zeros(32, np.float32)
+                        cd = np.zeros(32, np.uint8)
+                        useC = (interior | bot) & (i >= 1) & (i <= N)
+                        for l in range(32):
+                            rr = 2 * (nk - 1 - kk) + l
+                            X0[l] = X0R.read((rr, i[l] % PC), ("x0", j[l], i[l]), cp, bool(gsl[l]), "X0")
+                            cd[l] = CR.read((rr, i[l] % PC), ("cd", j[l], i[l]), cp, bool(useC[l]), "CD")
+                        with np.errstate(all="ignore"):
+                            gs = ((X0 + a * (((R + vcur[kk]) + D) + U)) * cr).astype(np.float32)
+                        vc = vcur[kk]
+                        vnew = np.where(gsl, gs, vc)
+                        i0 = interior & (i == 0)
+                        vnew = np.where(i0 & (mode == PAS) & (k > 0) & (rowfl[jj] != 0), R,
+                                        np.where(i0, xin[jj, 0], vnew))
+                        vnew = np.where(interior & (i == S - 1), xin[jj, S - 1], vnew)
+                        inr = (i >= 0) & (i <= S - 1)
+                        vtop = np.where((mode == PAS) & (k > 0) & (colfl[ii] != 0), D, xin[0, ii])
+                        vnew = np.where(top & inr, vtop, vnew)
+                        vnew = np.where(bot & inr, xin[S - 1, ii], vnew)
+                        vnew = np.where(idle, F(0), vnew).astype(np.float32)
+                        vdown = np.append(vnew[1:], vnew[31]).astype(np.float32)
+                        im1 = i - 1
+                        if mode == ROW:
+                            pin = np.where(cprev[kk] & C_RR, -vnew,
+                                           np.where(cprev[kk] & C_RL, -vprev[kk], vc))
+                        elif mode == COL:
+                            pin = np.where(cprev[kk] & C_CU, -uprev[kk],
+                                           np.where(cprev[kk] & C_CD, -vdown, vc))
+                        else:
+                            pin = vc
+                        post = np.where(interior & (im1 >= 1) & (im1 <= N), pin, vc)
+                        pasrow = (mode == PAS) & (rowfl[jj] != 0)
+                        post = np.where(interior & (im1 == 0) & pasrow, vnew, post)
+                        post = np.where(interior & (im1 == S - 1) & pasrow, vprev[kk], post)
+                        cfp = (mode == PAS) & (colfl[np.clip(im1, 0, S - 1)] != 0) & \
+                              (im1 >= 1) & (im1 <= N)
+                        post = np.where(top & cfp, vdown, post)
+                        post = np.where(bot & cfp, uprev[kk], post)
+                        post = np.where(idle, F(0), post).astype(np.float32)
+                        # the fast path: every interior lane at 2 <= i <= N and no
+                        # boundary action or lane-0 fix; it must give the same bits
+                        actm = {ROW: C_RR | C_RL, COL: C_CU | C_CD, PAS: 0}[mode]
+                        fix0 = mode == COL and bool(cd[0] & C_AD) and bool(interior[0])
+                        if dF0 <= d <= dF1 and not (interior & ((cprev[kk] & actm) != 0)).any() \
+                                and not fix0:
+                            fast += 1
+                            assert np.array_equal(vnew[interior].view(np.uint32),
+                                                  gs[interior].view(np.uint32))
+                            assert np.array_equal(post[interior].view(np.uint32),
+                                                  vc[interior].view(np.uint32))
+                        s = (d - 1) % RD
+                        for l in range(32):
+                            VR.write((kk, s, l + 2), post[l], ("vr", k, d - 1, l), cp + 1)
+                        fixv = None
+                        if mode == COL and (interior[0] or bot[0]) and 1 <= i[0] <= N \
+                                and (cd[0] & C_AD):
+                            fixv = -vnew[0]
+                            VR.write((kk, s, 1), fixv, ("vr", k, d - 1, -1), cp + 1)
+                        if b < B - 1 and d >= 1:
+                            edge[b, k, d - 1, [0, 2, 3]] = (post[30], vc[31], post[31])
+                            etag[b, k, d - 1, [0, 2, 3]] = TAG
+                        if g < G - 1 and kk == nk - 1:
+                            gexp[b, g, d, 2:34] = post
+                            gexp[b, g, d, 0] = VR.v[kk, s, 0]
+                            gexp[b, g, d, 1] = fixv if fixv is not None else VR.v[kk, s, 1]
+                            gtag[b, g, d, :34] = TAG
+                        if k == K - 1:
+                            for l in np.nonzero(gsl)[0]:
+                                xout[j[l], i[l]] = vnew[l]
+                        vprev[kk] = vc
+                        vcur[kk] = vnew
+                        uprev[kk] = U
+                        cprev[kk] = cd
+    return xout.reshape(-1), steps, fast

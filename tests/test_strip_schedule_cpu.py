@@ -1,0 +1,43 @@
+"""The strip wavefront's schedule (csrc/lssw.cuh), checked on the CPU: a
+lane-by-lane model with the kernel's step, ring and copy formulas
+(tests/strip_model.py) must reproduce the oracle's lin_solve bit for bit,
+every read must see a value written at least one barrier earlier into a slot
+not yet reused, and the fast path must give the general rules' bits."""
+import numpy as np
+import pytest
+
+import oracle
+from tests import strip_model as M
+from tests.util import random_rects
+
+
+def _case(S, K, mode, seed, G):
+    rng = np.random.default_rng(seed)
+    cells = np.zeros((S, S), np.uint8)
+    cells[0, :] = cells[-1, :] = cells[:, 0] = cells[:, -1] = 1
+    for x0, y0, x1, y1 in random_rects(rng, S, 4):
+        cells[y0:y1, x0:x1] = 1
+    cells = cells.reshape(-1)
+    x = rng.uniform(-1, 1, S * S).astype(np.float32)
+    x0 = rng.uniform(-1, 1, S * S).astype(np.float32)
+    a = float(rng.uniform(0.05, 2.0))
+    c = float(np.float32(1.0) + np.float32(4.0) * np.float32(a))
+    if mode == M.PAS and seed % 2 == 0:
+        a, c = 1.0, 4.0
+    P = ((S + 31) // 32) * 32
+    want = x.copy()
+    oracle.lin_solve(mode, want, x0, a, c, S, K, cells)
+    got, steps, fast = M.run(mode, x, x0, cells, S, P, K, a, c, G=G)
+    oracle.set_boundaries(mode, got, S, cells)
+    return int((got.view(np.uint32) != want.view(np.uint32)).sum()), steps, fast
+
+
+# sizes from the smallest grid to several strips, sweep counts that leave the
+# last group short, groups from one to five sweeps each
+@pytest.mark.parametrize("S,K,G", [(20, 1, 1), (20, 3, 2), (37, 5, 3), (40, 4, 4),
+                                   (66, 6, 2), (45, 9, 3), (70, 20, 5)])
+@pytest.mark.parametrize("mode", [M.ROW, M.COL, M.PAS])
+def test_strip_model_matches_oracle(S, K, G, mode):
+    diff, steps, fast = _case(S, K, mode, S + K + mode, G)
+    assert diff == 0
+    assert steps > 0
