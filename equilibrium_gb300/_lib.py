@@ -11,6 +11,7 @@ import re
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 LIB_PATH = os.path.join(HERE, "libeqfluid.so")
+LIB_FMA_PATH = os.path.join(HERE, "libeqfluid_fma.so")
 HEADER = os.path.join(ROOT, "include", "eqfluid.h")
 
 EQ_OK, EQ_ERR_ARG, EQ_ERR_CUDA, EQ_ERR_TIMEOUT, EQ_ERR_OOM, EQ_ERR_STATE = range(6)
@@ -54,6 +55,7 @@ class FluidConfigsC(ctypes.Structure):
 
 
 _lib = None
+_others = {}  # libraries loaded from other paths (the FMA build)
 
 
 def header_functions() -> list[str]:
@@ -67,8 +69,10 @@ def header_functions() -> list[str]:
 def load(path: str = LIB_PATH):
     """Load the library and declare signatures. Raises if it is missing."""
     global _lib
-    if _lib is not None:
+    if path == LIB_PATH and _lib is not None:
         return _lib
+    if path in _others:
+        return _others[path]
     if not os.path.exists(path):
         raise RuntimeError(
             f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
@@ -195,11 +199,20 @@ def load(path: str = LIB_PATH):
         fn = getattr(L, name)
         fn.restype = res
         fn.argtypes = args
-    _lib = L
+    if path == LIB_PATH:
+        _lib = L
+    else:
+        _others[path] = L
     return L
 
 
-def check(rc: int):
+def load_fma():
+    """The library built with FMA contraction (libeqfluid_fma.so): the plain
+    form's arithmetic with a*b+c fused, within 1e-6 relative of the reference."""
+    return load(LIB_FMA_PATH)
+
+
+def check(rc: int, lib=None):
     if rc != EQ_OK:
-        msg = load().eq_last_error()
+        msg = (lib or load()).eq_last_error()
         raise EqError(rc, msg.decode() if msg else "")

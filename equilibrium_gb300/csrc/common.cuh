@@ -27,9 +27,17 @@ constexpr uint8_t kCodeColMask = kCodeColDown | kCodeColUp;
 
 // Explicitly rounded IEEE operations: never contracted into FMA whatever the
 // compiler's --fmad setting, so results match the reference's f32 bit for bit.
+// The FMA build (EQ_FMA, compiled with --fmad=true) uses plain operators
+// instead, which the compiler may fuse into a*b+c with one rounding.
+#if defined(EQ_FMA) && EQ_FMA
+__device__ __forceinline__ float fadd(float a, float b) { return a + b; }
+__device__ __forceinline__ float fsub(float a, float b) { return a - b; }
+__device__ __forceinline__ float fmul(float a, float b) { return a * b; }
+#else
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+#endif
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 
 // Rust's f32::clamp (NaN passes through).

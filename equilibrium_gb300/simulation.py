@@ -105,11 +105,11 @@ class Fluid:
 
     def __init__(self, init_fluid: Optional[FluidConfigs] = None,
                  init_simulation: Optional[SimulationConfigs] = None, device: int = -1,
-                 _handle=None):
+                 _handle=None, lib=None):
         self.fluid_configs = init_fluid if init_fluid is not None else FluidConfigs()
         self.simulation_configs = (init_simulation if init_simulation is not None
                                    else SimulationConfigs())
-        self._L = _lib.load()
+        self._L = lib if lib is not None else _lib.load()
         if _handle is not None:
             self._h = _handle
             return

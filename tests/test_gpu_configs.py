@@ -10,6 +10,7 @@ import pytest
 import oracle
 from equilibrium_gb300 import _lib
 from equilibrium_gb300.simulation import Fluid, FluidConfigs, SimulationConfigs
+from tests.util import small_workload
 
 pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -42,29 +43,12 @@ def test_golden_fixture(eqlib, path):
     g.close()
 
 
-def _centre_patch_sources(rng, size, nframes):
-    c = size // 2
-    xs, ys = np.meshgrid(np.arange(c - 2, c + 3), np.arange(c - 2, c + 3))
-    xs = np.broadcast_to(xs.reshape(-1), (nframes, 25)).astype(np.uint32).copy()
-    ys = np.broadcast_to(ys.reshape(-1), (nframes, 25)).astype(np.uint32).copy()
-    d = rng.uniform(0, 100, (nframes, 25)).astype(np.float32)
-    u = rng.uniform(-5, 5, (nframes, 25)).astype(np.float32)
-    v = rng.uniform(-5, 5, (nframes, 25)).astype(np.float32)
-    return xs, ys, d, u, v
-
-
 def test_small_workload_100_frames_bitexact(eqlib):
     """N=64 interior, dt=0.1, diff=visc=1e-4, 20 sweeps, 100 frames, sources on
     the 5x5 centre patch every frame, one seeded rectangle of ~10% area."""
-    size, iters, dt, dv = 66, 20, 0.1, 1e-4
-    rng = np.random.default_rng(1)
-    w = h = 20  # 400 cells of 4096 interior cells ~ 10%
-    x0 = int(rng.integers(1, size - 1 - w))
-    y0 = int(rng.integers(1, size - 1 - h))
-    while abs(x0 + w / 2 - size / 2) < 14 and abs(y0 + h / 2 - size / 2) < 14:
-        x0 = int(rng.integers(1, size - 1 - w))
-        y0 = int(rng.integers(1, size - 1 - h))
-    xs, ys, d, u, v = _centre_patch_sources(rng, size, 100)
+    size, iters, dt, dv, rect, xs, ys, d, u, v = small_workload(100)
+    x0, y0, x1, y1 = rect
+    w, h = x1 - x0, y1 - y0
     g = gpu_fluid(size, iters, dt, dv, dv)
     assert eqlib.eq_fluid_fill_obstacle(g.handle, x0, y0, x0 + w, y0 + h) == 0
     r = oracle.OracleFluid(size, dt, iters, dv, dv)

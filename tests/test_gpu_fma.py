@@ -1,0 +1,122 @@
+"""The FMA build of the plain form (libeqfluid_fma.so: the same kernels with
+a*b+c fused by the compiler, --fmad=true) against the reference's f32 step
+(the oracle): every phase and whole frames within 1e-6 relative (L2 norm of
+the difference over the L2 norm of the reference, per field, ghost cells
+included), where the --fmad=false build is bit-exact."""
+import numpy as np
+import pytest
+
+import oracle
+from equilibrium_gb300 import _lib
+from equilibrium_gb300.simulation import Fluid, FluidConfigs, SimulationConfigs
+from tests.util import random_rects, small_workload
+
+pytestmark = pytest.mark.gpu
+
+ROW, COL, PAS = _lib.MODE_ADJUST_ROW, _lib.MODE_ADJUST_COLUMN, _lib.MODE_PASSIVE
+TOL = 1e-6
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a))
+
+
+@pytest.fixture(scope="module")
+def fma(eqlib):
+    return _lib.load_fma()
+
+
+def pair(fma, size, K, seed, dt=0.1, dv=1e-4, nrect=5, randomize=True):
+    f = Fluid(FluidConfigs(dv, dv, False), SimulationConfigs(dt, K, size), lib=fma)
+    r = oracle.OracleFluid(size, dt, K, dv, dv)
+    rng = np.random.default_rng(seed)
+    for rc in random_rects(rng, size, nrect):
+        _lib.check(fma.eq_fluid_fill_obstacle(f.handle, *rc), fma)
+        r.fill_obstacle(*rc)
+    if randomize:
+        n = size * size
+        for k in range(6):
+            lo, hi = (-1.0, 1.0) if k >= 2 else (0.0, 2.0)
+            r.fields[k][:] = rng.uniform(lo, hi, n).astype(np.float32)
+            f.write_field(k, r.fields[k])
+    return f, r
+
+
+@pytest.mark.parametrize("solver", [0, 3])
+@pytest.mark.parametrize("mode", [ROW, COL, PAS])
+def test_fma_lin_solve(fma, mode, solver):
+    size, K = 130, 20
+    f, r = pair(fma, size, K, 11 + mode)
+    _lib.check(fma.eq_fluid_set_solver(f.handle, solver), fma)
+    a = np.float32(0.37) if mode != PAS else np.float32(1.0)
+    c = np.float32(1.0) + np.float32(4.0) * a if mode != PAS else np.float32(4.0)
+    _lib.check(fma.eq_fluid_lin_solve(f.handle, mode, 2, 4, a, c), fma)
+    ref = r.fields[2].copy()
+    oracle.lin_solve(mode, ref, r.fields[4], a, c, size, K, r.cells)
+    e = rel(f.read_field(2), ref)
+    assert e <= TOL, (mode, solver, e)
+    f.close()
+
+
+@pytest.mark.parametrize("mode", [ROW, COL, PAS])
+def test_fma_advect(fma, mode):
+    size = 130
+    f, r = pair(fma, size, 20, 21 + mode)
+    _lib.check(fma.eq_fluid_advect(f.handle, mode, 1, 0, 2, 3), fma)
+    d = r.fields[1].copy()
+    oracle.advect(mode, d, r.fields[0], r.fields[2], r.fields[3], size, 0.1, r.cells)
+    e = rel(f.read_field(1), d)
+    assert e <= TOL, (mode, e)
+    f.close()
+
+
+def test_fma_project(fma):
+    size, K = 130, 20
+    f, r = pair(fma, size, K, 31)
+    _lib.check(fma.eq_fluid_project(f.handle, 2, 3, 4, 5), fma)
+    vx, vy, p, dv = (r.fields[k].copy() for k in (2, 3, 4, 5))
+    oracle.project(vx, vy, p, dv, size, K, r.cells)
+    for k, want in ((2, vx), (3, vy), (4, p), (5, dv)):
+        e = rel(f.read_field(k), want)
+        assert e <= TOL, (k, e)
+    f.close()
+
+
+def test_fma_small_workload_frames(fma):
+    """The N = 64 workload: frames 1 and 3 within the bound."""
+    size, iters, dt, dv, rect, xs, ys, d, u, v = small_workload(3)
+    f = Fluid(FluidConfigs(dv, dv, False), SimulationConfigs(dt, iters, size), lib=fma)
+    _lib.check(fma.eq_fluid_fill_obstacle(f.handle, *rect), fma)
+    r = oracle.OracleFluid(size, dt, iters, dv, dv)
+    r.fill_obstacle(*rect)
+    for fr in range(3):
+        f.add_sources(xs[fr], ys[fr], d[fr], u[fr], v[fr])
+        f.step()
+        r.run(1, xs[fr:fr + 1], ys[fr:fr + 1], d[fr:fr + 1], u[fr:fr + 1], v[fr:fr + 1])
+        if fr in (0, 2):
+            for k in range(6):
+                e = rel(f.read_field(k), r.fields[k])
+                assert e <= TOL, (fr + 1, oracle.FIELDS[k], e)
+    f.close()
+
+
+def test_fma_large_workload_frame(fma):
+    """The N = 1024 workload, one frame."""
+    import bench
+    rects, sx, sy, sd, su, sv = bench.scene(bench.SEED, 1)
+    f = Fluid(FluidConfigs(bench.DIFF, bench.VISC, False),
+              SimulationConfigs(bench.DT, bench.ITERS, bench.SIZE), lib=fma)
+    r = oracle.OracleFluid(bench.SIZE, bench.DT, bench.ITERS, bench.DIFF, bench.VISC)
+    for rc in rects:
+        _lib.check(fma.eq_fluid_fill_obstacle(f.handle, *rc), fma)
+        r.fill_obstacle(*rc)
+    f.add_sources(sx[0], sy[0], sd[0], su[0], sv[0])
+    f.step()
+    r.run(1, sx, sy, sd, su, sv)
+    for k in range(6):
+        e = rel(f.read_field(k), r.fields[k])
+        assert e <= TOL, (oracle.FIELDS[k], e)
+    f.close()

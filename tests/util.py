@@ -72,3 +72,34 @@ class Pair:
 
     def close(self):
         self.gpu.close()
+
+
+def small_workload(nframes: int):
+    """The N = 64 workload: size 66, dt 0.1, diffusion = viscosity = 1e-4, 20
+    sweeps; one seeded rectangle of ~10 % of the interior (kept off the centre)
+    and sources on the 5x5 centre patch every frame (density U[0, 100],
+    velocity U[-5, 5]). Returns (size, iters, dt, diff, rect, sx, sy, sd, su, sv)."""
+    size, iters, dt, dv = 66, 20, 0.1, 1e-4
+    rng = np.random.default_rng(1)
+    w = h = 20  # 400 cells of 4096 interior cells ~ 10%
+    x0 = int(rng.integers(1, size - 1 - w))
+    y0 = int(rng.integers(1, size - 1 - h))
+    while abs(x0 + w / 2 - size / 2) < 14 and abs(y0 + h / 2 - size / 2) < 14:
+        x0 = int(rng.integers(1, size - 1 - w))
+        y0 = int(rng.integers(1, size - 1 - h))
+    c = size // 2
+    xs, ys = np.meshgrid(np.arange(c - 2, c + 3), np.arange(c - 2, c + 3))
+    xs = np.broadcast_to(xs.reshape(-1), (nframes, 25)).astype(np.uint32).copy()
+    ys = np.broadcast_to(ys.reshape(-1), (nframes, 25)).astype(np.uint32).copy()
+    d = rng.uniform(0, 100, (nframes, 25)).astype(np.float32)
+    u = rng.uniform(-5, 5, (nframes, 25)).astype(np.float32)
+    v = rng.uniform(-5, 5, (nframes, 25)).astype(np.float32)
+    return size, iters, dt, dv, (x0, y0, x0 + w, y0 + h), xs, ys, d, u, v
+
+
+def state_hashes(fields) -> list:
+    """sha256 of each of the six fields' float32 bytes (field order of the
+    reference's struct: scratch, density, vx, vy, vx0, vy0)."""
+    import hashlib
+    return [hashlib.sha256(np.ascontiguousarray(f, dtype=np.float32).tobytes()).hexdigest()
+            for f in fields]
