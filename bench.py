@@ -116,17 +116,28 @@ def cells_total(cfgs):
 
 
 def run_batched_form(local_rank: int, frames: int, plain_sample: int = 12, storage: str = "f32",
-                     autotune: bool = True, err_sample: int = 0):
+                     autotune: bool = True, err_sample: int = 0, rank: int = 0, world: int = 1,
+                     reduce_max=None, reduce_sum=None):
     """The batched form on the many-scene workload: one persistent launch per
     frame (graph-replayed), autotuned; timed with CUDA events on the batch's
     stream (inputs ~4.6 GB, far larger than L2). Also the plain kernels looped
-    scene by scene over a sample of the same scenes, for comparison."""
+    scene by scene over a sample of the same scenes, for comparison.
+
+    With world > 1 ranks (one GPU each) the scenes are split by
+    batch.partition_scenes (no data shared, no collective on the data path):
+    each rank builds and steps only its own scenes, and the value is all
+    ranks' cells over the slowest rank's frame time (weak in the scenes per
+    rank). Only rank 0 runs the end-to-end, looped-plain and CPU legs."""
     import torch
     from equilibrium_gb300 import _lib
-    from equilibrium_gb300.batch import Batch, SceneConfig
+    from equilibrium_gb300.batch import Batch, SceneConfig, partition_scenes
     from equilibrium_gb300.simulation import Fluid, FluidConfigs, SimulationConfigs
     L = _lib.load()
-    cfgs, rects = batch_workload()
+    all_cfgs, all_rects = batch_workload()
+    parts, loads = partition_scenes(all_cfgs, world)
+    mine = parts[rank]
+    cfgs = [all_cfgs[q] for q in mine]
+    rects = [all_rects[q] for q in mine]
     b = Batch([SceneConfig(*c) for c in cfgs], device=local_rank, storage=storage)
     for sidx, rr in enumerate(rects):
         for r in rr:
@@ -150,9 +161,15 @@ def run_batched_form(local_rank: int, frames: int, plain_sample: int = 12, stora
     torch.cuda.synchronize()
     launches = b.launch_count() - c0
     ms = statistics.mean(a.elapsed_time(e) for a, e in ev)
+    local_cells = cells
+    if world > 1:  # all ranks' cells over the slowest rank's frame time
+        ms = reduce_max(ms)
+        cells = int(round(reduce_sum(float(cells))))
     value = cells / (ms / 1e3)
     out = {"value": cells / (ms / 1e3), "unit": "cell-steps/s", "ms_per_frame": ms,
-           "frames_timed": frames, "scenes": len(cfgs), "interior_cells": cells,
+           "frames_timed": frames, "scenes": len(all_cfgs), "interior_cells": cells,
+           "ranks": world, "scenes_per_rank": [len(p) for p in parts],
+           "work_imbalance": max(loads) / (sum(loads) / world) - 1.0,
            "dtype": "f32" if storage == "f32" else f"{storage} storage, f32 arithmetic",
            "workload": f"{len(cfgs)} scenes, N log-uniform in [32, 512], dt U[0.02, 0.2], "
                        "diffusion and viscosity log-uniform [1e-6, 1e-3], 20 sweeps, 0-8 "
@@ -164,12 +181,16 @@ def run_batched_form(local_rank: int, frames: int, plain_sample: int = 12, stora
                         "achieved": BYTES_BY_STORAGE[storage] * cells / (ms / 1e3) / 1e9,
                         "unit": "GB/s",
                         "bytes_per_cell_frame": BYTES_BY_STORAGE[storage]}}
+    if rank != 0:
+        b.close()
+        return out
     if storage == "f32":
         # end to end: one frame through the C ABI, then every scene's three pub
         # fields read back to (pinned) host memory, one field of all scenes per
         # call
         host = [torch.empty(cells_total(cfgs), dtype=torch.float32).pin_memory().numpy()
                 for _ in range(3)]
+        # (rank 0's own scenes: the e2e number is rank 0's cells over its time)
         b.read_fields(_lib.FIELD_DENSITY, host[0])  # first use allocates its device staging
         b.synchronize()
         t0 = time.perf_counter()
@@ -178,7 +199,7 @@ def run_batched_form(local_rank: int, frames: int, plain_sample: int = 12, stora
         for f, buf in zip((_lib.FIELD_DENSITY, _lib.FIELD_VX, _lib.FIELD_VY), host):
             d2h += b.read_fields(f, buf).nbytes
         e2e_s = time.perf_counter() - t0
-        out["e2e"] = {"value": cells / e2e_s, "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
+        out["e2e"] = {"value": local_cells / e2e_s, "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
                       "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3}
         out["bit_exact"] = "per scene, vs the reference step (tests/test_gpu_batch.py)"
     b.close()
@@ -1091,6 +1112,20 @@ def run_ours(args):
     e2e_value, e2e_s = replicas_value(sum(e2e_times), args.steps, world, reduce_max)
     assert np.isfinite(outs[0].numpy()).all()
 
+    # the batched form shards by scene: every rank steps its own part
+    sharded = None
+    if args.forms and world > 1:
+        def reduce_sum(x):
+            import torch.distributed as dist
+            t = torch.tensor([x], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.SUM)
+            return float(t.item())
+        try:
+            sharded = run_batched_form(local_rank, args.batch_frames, rank=rank, world=world,
+                                       reduce_max=reduce_max, reduce_sum=reduce_sum)
+        except Exception as e:  # reported by rank 0, never silently replaced
+            sharded = {"error": f"{type(e).__name__}: {e}"}
+
     if rank != 0:
         return
     hbm, peak_kind = peaks()
@@ -1136,7 +1171,8 @@ def run_ours(args):
                 r = {"error": f"{type(e).__name__}: {e}"}
             forms[name] = r
 
-        form("batched", lambda: run_batched_form(local_rank, args.batch_frames))
+        form("batched", lambda: sharded if sharded is not None
+             else run_batched_form(local_rank, args.batch_frames))
         form("batched_f16", lambda: run_batched_form(local_rank, args.batch_frames, 0, "f16",
                                                      autotune=False, err_sample=24))
         form("batched_f16_scalars", lambda: run_batched_form(

@@ -158,3 +158,29 @@ class Batch:
         c = ctypes.c_uint64()
         check(_lib.load().eq_batch_launch_count(self.handle, ctypes.byref(c)))
         return c.value
+
+
+def partition_scenes(scenes: Sequence, world: int):
+    """Splits a batch's scenes over `world` ranks (one GPU each) with no data
+    shared between ranks: greedy largest-first bin packing by each scene's
+    work, size^2 x sweeps (every scene is an independent Fluid, as each
+    simulation thread of the reference owns its own, renderer.rs:126-128).
+    Scenes are SceneConfig or (size, dt, sweeps, ...) tuples. Returns the
+    scene indices of each rank (ascending) and each rank's total work; the
+    same inputs give the same split on every rank."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+
+    def work(sc):
+        size, sweeps = (sc.size, sc.frames) if isinstance(sc, SceneConfig) else (sc[0], sc[2])
+        return int(size) ** 2 * max(int(sweeps), 1)
+
+    cost = [work(sc) for sc in scenes]
+    order = sorted(range(len(cost)), key=lambda q: (-cost[q], q))
+    loads = [0] * world
+    parts: List[List[int]] = [[] for _ in range(world)]
+    for q in order:
+        r = min(range(world), key=lambda k: (loads[k], k))
+        parts[r].append(q)
+        loads[r] += cost[q]
+    return [sorted(p) for p in parts], loads

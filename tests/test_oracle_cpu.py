@@ -168,3 +168,21 @@ def test_noise_angle_is_deterministic_and_bounded():
     a = [L.eq_noise_angle(np.float32(dt)) for dt in (0.02, 0.05, 0.1, 0.02)]
     assert a[0] == a[3]
     assert all(abs(x) <= 6.28 * 2 * 1.5 for x in a)
+
+
+def test_long_horizon_hashes_reproduce_on_this_host():
+    """The committed long-horizon fixture's N = 64 checkpoints are the oracle's
+    state on this host too (the 1000-frame N = 1024 run is regenerated by
+    tests/golden/make_long_hashes.py, tens of minutes)."""
+    import json
+    from tests.util import small_workload, state_hashes
+    c = json.load(open(os.path.join(HERE, "golden", "long_horizon_hashes.json")))["n64"]
+    size, iters, dt, dv, rect, xs, ys, d, u, v = small_workload(100)
+    assert c["rects"] == [list(rect)] and c["size"] == size
+    f = oracle.OracleFluid(size, dt, iters, dv, dv)
+    f.fill_obstacle(*rect)
+    done = 0
+    for fr in (1, 10, 100):
+        f.run(fr - done, xs[done:fr], ys[done:fr], d[done:fr], u[done:fr], v[done:fr])
+        done = fr
+        assert state_hashes(f.fields) == c["checkpoints"][str(fr)], fr
