@@ -962,6 +962,74 @@ def cpu_baseline_run(nframes: int):
                       f"({secs:.1f} s, oracle/ C++ restatement, -O3 -ffp-contract=off)"}
 
 
+def parity_check(local_rank: int, frames=(1, 10, 100)):
+    """The headline workload's state after 1, 10 and 100 frames (a fresh
+    handle, the step() the timed region runs, sources of the 1000-frame draw)
+    against the oracle's hashes in tests/golden/long_horizon_hashes.json:
+    all six fields with ghost cells, bit for bit."""
+    from equilibrium_gb300 import _lib
+    from equilibrium_gb300.simulation import Fluid, FluidConfigs, SimulationConfigs
+    from tests.util import state_hashes
+    L = _lib.load()
+    with open(os.path.join(ROOT, "tests", "golden", "long_horizon_hashes.json")) as fh:
+        c = json.load(fh)["n1024"]
+    rects, sx, sy, sd, su, sv = scene(SEED, c["frames"])
+    f = Fluid(FluidConfigs(DIFF, VISC, False), SimulationConfigs(DT, ITERS, SIZE),
+              device=local_rank)
+    for r in rects:
+        _lib.check(L.eq_fluid_fill_obstacle(f.handle, *r))
+    done, bad = 0, []
+    for fr in frames:
+        for q in range(done, fr):
+            f.add_sources(sx[q], sy[q], sd[q], su[q], sv[q])
+            f.step()
+        done = fr
+        f.synchronize()
+        got = state_hashes([f.read_field(k) for k in range(6)])
+        if got != c["checkpoints"][str(fr)]:
+            bad.append(fr)
+    f.close()
+    return {"status": "bit-exact" if not bad else f"differs at frames {bad}",
+            "frames_checked": list(frames), "fields": "all six, ghost cells included",
+            "reference": "oracle state hashes, tests/golden/long_horizon_hashes.json "
+                         "(the 1000-frame hash is checked by tests/test_gpu_long_horizon.py)"}
+
+
+def summarize(line):
+    """A compact per-form digest, last in the JSON line: value (cell-steps/s),
+    ratio to the plain form, fraction of the HBM roofline, accuracy."""
+    def g(d, *ks):
+        for k in ks:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return d
+
+    def r3(x):
+        return float(f"{x:.3g}") if isinstance(x, (int, float)) else x
+
+    out = {"plain": {"value": r3(line["value"]), "e2e": r3(g(line, "e2e", "value")),
+                     "frame_frac": r3(g(line, "roofline", "frame_roofline_frac")),
+                     "parity": g(line, "parity", "status")}}
+    forms = line.get("forms", {})
+    for name in ("batched", "batched_f16", "batched_f16_scalars"):
+        fm = forms.get(name)
+        if fm:
+            out[name] = {"value": r3(fm.get("value")), "vs_plain": r3(fm.get("vs_plain")),
+                         "frac": r3(g(fm, "roofline", "frac")),
+                         "err": g(fm, "density_rel_l2_vs_f64"), "error": fm.get("error")}
+    pr = forms.get("precision")
+    if pr:
+        for k in ("f16", "bf16"):
+            if k in pr:
+                out[f"precision_{k}"] = {"value": r3(pr[k].get("value")),
+                                         "vs_plain": r3(pr[k].get("vs_plain"))}
+    df = forms.get("differentiation")
+    if df:
+        out["differentiation"] = {"value": r3(df.get("value")), "error": df.get("error")}
+    return out
+
+
 def config_dict():
     return {"workload": "plain frame step, N=1024 (size 1026), 20 GS sweeps, dt=0.05, "
                         "diff=visc=1e-5, 4 seeded rectangles, 8 seeded sources/frame",
@@ -1157,6 +1225,10 @@ def run_ours(args):
     except Exception as e:  # the oracle is only the reported baseline
         cpu = {"value": None, "unit": "cell-steps/s", "cores": 1, "kind": "port",
                "sample": f"failed: {e}"}
+    try:
+        parity = parity_check(local_rank)
+    except Exception as e:
+        parity = {"status": f"not checked: {type(e).__name__}: {e}"}
     forms = {}
     if args.forms:
         def form(name, fn):
@@ -1192,9 +1264,11 @@ def run_ours(args):
                     "d2h_bytes_per_step": 3 * SIZE * SIZE * 4,
                     "ms_per_step": e2e_s / args.steps * 1e3},
             "gpu_launches": int(count1.value - count0.value), "clocks": clk.summary(),
+            "parity": parity,
             "wall_s_timed_region": wall}
     if forms:
         line["forms"] = forms
+    line["summary"] = summarize(line)
     print(json.dumps(line), flush=True)
 
 

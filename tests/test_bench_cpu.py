@@ -27,3 +27,17 @@ def test_reference_arm_line():
     e2e = line["e2e"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
+
+
+def test_summary_digest_of_a_bench_line():
+    import bench
+    line = {"value": 3.2e8, "e2e": {"value": 3.0e8}, "roofline": {"frame_roofline_frac": 0.012},
+            "parity": {"status": "bit-exact"},
+            "forms": {"batched": {"value": 1.1e9, "vs_plain": 3.4, "roofline": {"frac": 0.03}},
+                      "precision": {"f16": {"value": 2e8, "vs_plain": 0.6}},
+                      "differentiation": {"error": "RuntimeError: x"}}}
+    s = bench.summarize(line)
+    assert s["plain"] == {"value": 3.2e8, "e2e": 3.0e8, "frame_frac": 0.012, "parity": "bit-exact"}
+    assert s["batched"]["vs_plain"] == 3.4 and s["batched"]["frac"] == 0.03
+    assert s["precision_f16"] == {"value": 2e8, "vs_plain": 0.6}
+    assert s["differentiation"]["error"] == "RuntimeError: x"
