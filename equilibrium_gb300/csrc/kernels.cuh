@@ -124,8 +124,11 @@ __device__ __forceinline__ Backtrace backtrace(int i, int j, float uij, float vi
                                                int S) {
   const float sf = (float)S;
   const float hi = fsub(sf, 1.0f);
-  float x = fsub((float)i, fmul(dt0, uij));
-  float y = fsub((float)j, fmul(dt0, vij));
+  // the backtrace position stays rounded twice in the FMA build too: a fused
+  // i - dt0*u moves the sample point by an ulp, which steep fields (the
+  // sources' edges) turn into relative errors above 1e-6
+  float x = __fsub_rn((float)i, __fmul_rn(dt0, uij));
+  float y = __fsub_rn((float)j, __fmul_rn(dt0, vij));
   x = rust_clamp(x, 0.5f, hi);
   y = rust_clamp(y, 0.5f, hi);
   const float fi0 = floorf(x), fj0 = floorf(y);

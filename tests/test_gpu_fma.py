@@ -97,9 +97,8 @@ def test_fma_small_workload_frames(fma):
         f.step()
         r.run(1, xs[fr:fr + 1], ys[fr:fr + 1], d[fr:fr + 1], u[fr:fr + 1], v[fr:fr + 1])
         if fr in (0, 2):
-            for k in range(6):
-                e = rel(f.read_field(k), r.fields[k])
-                assert e <= TOL, (fr + 1, oracle.FIELDS[k], e)
+            errs = {oracle.FIELDS[k]: rel(f.read_field(k), r.fields[k]) for k in range(6)}
+            assert max(errs.values()) <= TOL, (fr + 1, errs)
     f.close()
 
 
@@ -116,7 +115,6 @@ def test_fma_large_workload_frame(fma):
     f.add_sources(sx[0], sy[0], sd[0], su[0], sv[0])
     f.step()
     r.run(1, sx, sy, sd, su, sv)
-    for k in range(6):
-        e = rel(f.read_field(k), r.fields[k])
-        assert e <= TOL, (oracle.FIELDS[k], e)
+    errs = {oracle.FIELDS[k]: rel(f.read_field(k), r.fields[k]) for k in range(6)}
+    assert max(errs.values()) <= TOL, errs
     f.close()
