@@ -235,29 +235,31 @@ int h_project(eq_hfluid* h, int which, T* vx, T* vy, T* ps, T* divs) {
   return check_launch(pl);
 }
 
-template <class T>
-int h_advect(eq_hfluid* h, int mode, T* d, const T* d0, const T* u, const T* v) {
+template <class T, class TU>
+int h_advect(eq_hfluid* h, int mode, T* d, const T* d0, const TU* u, const TU* v) {
   eq_fluid* pl = h->plain;
   const int S = (int)pl->S, N = S - 2;
   const float dt0 = pl->dt * (float)(S - 2);
   const int threads = std::min(256, ((N + 31) / 32) * 32);
-  eqk::k_h_advect_rows<T><<<N, threads, 0, pl->stream>>>(d, d0, u, v, S, pl->P, dt0);
+  eqk::k_h_advect_rows<T, TU><<<N, threads, 0, pl->stream>>>(d, d0, u, v, S, pl->P, dt0);
   int rc = check_launch(pl);
   if (rc) return rc;
   return h_bnd<T>(h, mode, d);
 }
 
-template <class T>
+// One frame with density and scratch stored in TS, the four velocity arrays
+// (which project also uses for its pressure and divergence) in TV.
+template <class TS, class TV>
 int h_step(eq_hfluid* h) {
   eq_fluid* pl = h->plain;
   int rc = upload_mask(pl);
   if (rc) return rc;
-  T* sc = static_cast<T*>(h->f[EQ_FIELD_SCRATCH]);
-  T* de = static_cast<T*>(h->f[EQ_FIELD_DENSITY]);
-  T* vx = static_cast<T*>(h->f[EQ_FIELD_VX]);
-  T* vy = static_cast<T*>(h->f[EQ_FIELD_VY]);
-  T* vx0 = static_cast<T*>(h->f[EQ_FIELD_VX0]);
-  T* vy0 = static_cast<T*>(h->f[EQ_FIELD_VY0]);
+  TS* sc = static_cast<TS*>(h->f[EQ_FIELD_SCRATCH]);
+  TS* de = static_cast<TS*>(h->f[EQ_FIELD_DENSITY]);
+  TV* vx = static_cast<TV*>(h->f[EQ_FIELD_VX]);
+  TV* vy = static_cast<TV*>(h->f[EQ_FIELD_VY]);
+  TV* vx0 = static_cast<TV*>(h->f[EQ_FIELD_VX0]);
+  TV* vy0 = static_cast<TV*>(h->f[EQ_FIELD_VY0]);
   const int64_t ns = (int64_t)h->sx.size();
   if (ns > 0) {
     const size_t bytes = (size_t)ns * 20;
@@ -278,7 +280,7 @@ int h_step(eq_hfluid* h) {
     EQ_CUDA(cudaMemcpyAsync(h->d_src, buf.data(), bytes, cudaMemcpyHostToDevice, pl->stream));
     const uint32_t* dx = reinterpret_cast<const uint32_t*>(h->d_src);
     const float* dv = reinterpret_cast<const float*>(h->d_src + ns * 8);
-    eqk::k_h_sources<T><<<1, 1, 0, pl->stream>>>(de, sc, vx, vy, (int)pl->S, pl->P, ns, dx,
+    eqk::k_h_sources<TS, TV><<<1, 1, 0, pl->stream>>>(de, sc, vx, vy, (int)pl->S, pl->P, ns, dx,
                                                  dx + ns, dv, dv + ns, dv + 2 * ns);
     if ((rc = check_launch(pl))) return rc;
     EQ_CUDA(cudaStreamSynchronize(pl->stream));  // the staging vector goes out of scope
@@ -298,44 +300,44 @@ int h_step(eq_hfluid* h) {
     pl->cur = st;
     pl->cur_slot = slot;
   };
-  auto side = [&](int k, int mode, T* x, const T* x0, float dif) -> int {
+  auto side = [&](int k, int mode, auto* x, const auto* x0, float dif) -> int {
     EQ_CUDA(cudaStreamWaitEvent(pl->side[k], pl->fork_ev, 0));
     on(pl->side[k], k + 1);
-    int r = h_diffuse<T>(h, mode, x, x0, dif, k + 1);
+    int r = h_diffuse(h, mode, x, x0, dif, k + 1);
     if (!r && cudaEventRecord(pl->join_ev[k], pl->side[k]) != cudaSuccess)
       r = fail(EQ_ERR_CUDA, "side stream event");
     on(pl->stream, 0);
     return r;
   };
   if (sideVy || sideDe) EQ_CUDA(cudaEventRecord(pl->fork_ev, pl->stream));
-  if ((rc = h_diffuse<T>(h, eqk::kRow, vx0, vx, pl->visc))) return rc;
+  if ((rc = h_diffuse<TV>(h, eqk::kRow, vx0, vx, pl->visc))) return rc;
   if (sideVy && (rc = side(0, eqk::kCol, vy0, vy, pl->visc))) return rc;
   if (sideDe && (rc = side(1, eqk::kPassive, sc, de, pl->diff))) return rc;
   if (sideVy)
     EQ_CUDA(cudaStreamWaitEvent(pl->stream, pl->join_ev[0], 0));
-  else if ((rc = h_diffuse<T>(h, eqk::kCol, vy0, vy, pl->visc)))
+  else if ((rc = h_diffuse<TV>(h, eqk::kCol, vy0, vy, pl->visc)))
     return rc;
-  if ((rc = h_project<T>(h, 0, vx0, vy0, vx, vy))) return rc;
-  if ((rc = h_advect<T>(h, eqk::kRow, vx, vx0, vx0, vy0))) return rc;
-  if ((rc = h_advect<T>(h, eqk::kCol, vy, vy0, vx0, vy0))) return rc;
-  if ((rc = h_project<T>(h, 1, vx, vy, vx0, vy0))) return rc;
+  if ((rc = h_project<TV>(h, 0, vx0, vy0, vx, vy))) return rc;
+  if ((rc = h_advect<TV, TV>(h, eqk::kRow, vx, vx0, vx0, vy0))) return rc;
+  if ((rc = h_advect<TV, TV>(h, eqk::kCol, vy, vy0, vx0, vy0))) return rc;
+  if ((rc = h_project<TV>(h, 1, vx, vy, vx0, vy0))) return rc;
   if (sideDe)
     EQ_CUDA(cudaStreamWaitEvent(pl->stream, pl->join_ev[1], 0));
-  else if ((rc = h_diffuse<T>(h, eqk::kPassive, sc, de, pl->diff)))
+  else if ((rc = h_diffuse<TS>(h, eqk::kPassive, sc, de, pl->diff)))
     return rc;
-  if ((rc = h_advect<T>(h, eqk::kPassive, de, sc, vx, vy))) return rc;
+  if ((rc = h_advect<TS, TV>(h, eqk::kPassive, de, sc, vx, vy))) return rc;
   const size_t n = pl->grid_elems();
-  eqk::k_h_copy<T><<<h_blocks(n), 256, 0, pl->stream>>>(sc, de, n);
+  eqk::k_h_copy<TS><<<h_blocks(n), 256, 0, pl->stream>>>(sc, de, n);
   return check_launch(pl);
 }
 
-template <class T>
+template <class TS, class TV>
 int h_init(eq_hfluid* h) {
   eq_fluid* pl = h->plain;
   const int S = (int)pl->S;
-  eqk::k_h_init<T><<<h_grid(S, S), kHBlk, 0, pl->stream>>>(
-      static_cast<T*>(h->f[0]), static_cast<T*>(h->f[1]), static_cast<T*>(h->f[2]),
-      static_cast<T*>(h->f[3]), S, pl->P);
+  eqk::k_h_init<TS, TV><<<h_grid(S, S), kHBlk, 0, pl->stream>>>(
+      static_cast<TS*>(h->f[0]), static_cast<TS*>(h->f[1]), static_cast<TV*>(h->f[2]),
+      static_cast<TV*>(h->f[3]), S, pl->P);
   return check_launch(pl);
 }
 
@@ -347,8 +349,9 @@ int eq_hfluid_new(const eq_fluid_configs* fluid, const eq_simulation_configs* si
                   double pressure_rtol, int32_t max_refinements, int device, eq_hfluid** out) {
   if (!fluid || !sim || !out) return fail(EQ_ERR_ARG, "null argument");
   *out = nullptr;
-  if (storage != EQ_STORE_F16 && storage != EQ_STORE_BF16)
-    return fail(EQ_ERR_ARG, "storage must be EQ_STORE_F16 or EQ_STORE_BF16");
+  if (storage != EQ_STORE_F16 && storage != EQ_STORE_BF16 && storage != EQ_STORE_F16_SCALARS)
+    return fail(EQ_ERR_ARG,
+                "storage must be EQ_STORE_F16, EQ_STORE_BF16 or EQ_STORE_F16_SCALARS");
   if (sim->size < 20) return fail(EQ_ERR_ARG, "size must be >= 20 (fluid.rs:534 underflows)");
   if (sim->size > 32768) return fail(EQ_ERR_ARG, "size too large");
   if (sim->frames < 0) return fail(EQ_ERR_ARG, "frames must be >= 0");
@@ -380,15 +383,24 @@ int eq_hfluid_new(const eq_fluid_configs* fluid, const eq_simulation_configs* si
     hfree(h);
     return fail(code, what);
   };
-  if (cudaMalloc(&h->fblock, 6 * g * 2) != cudaSuccess ||
+  const bool mixed = storage == EQ_STORE_F16_SCALARS;
+  size_t fbytes = 0;  // scalars 2 bytes a cell; velocities 4 with FP32 velocity storage
+  for (int q = 0; q < 6; ++q) fbytes += g * ((mixed && q >= 2) ? 4 : 2);
+  if (cudaMalloc(&h->fblock, fbytes) != cudaSuccess ||
       cudaMalloc(&h->p32, g * 4) != cudaSuccess || cudaMalloc(&h->b32, g * 4) != cudaSuccess ||
       cudaMalloc(&h->r32, g * 4) != cudaSuccess ||
       cudaMalloc(&h->d_acc, 4 * sizeof(double)) != cudaSuccess)
     return bail(EQ_ERR_OOM, "cudaMalloc (half fields)");
   if (cudaMallocHost(&h->h_acc, 4 * sizeof(double)) != cudaSuccess)
     return bail(EQ_ERR_OOM, "cudaMallocHost");
-  for (int q = 0; q < 6; ++q) h->f[q] = static_cast<uint8_t*>(h->fblock) + (size_t)q * g * 2;
-  if (cudaMemsetAsync(h->fblock, 0, 6 * g * 2, pl->stream) != cudaSuccess ||
+  {
+    size_t off = 0;
+    for (int q = 0; q < 6; ++q) {
+      h->f[q] = static_cast<uint8_t*>(h->fblock) + off;
+      off += g * ((mixed && q >= 2) ? 4 : 2);
+    }
+  }
+  if (cudaMemsetAsync(h->fblock, 0, fbytes, pl->stream) != cudaSuccess ||
       cudaMemsetAsync(h->p32, 0, g * 4, pl->stream) != cudaSuccess ||
       cudaMemsetAsync(h->b32, 0, g * 4, pl->stream) != cudaSuccess ||
       cudaMemsetAsync(h->r32, 0, g * 4, pl->stream) != cudaSuccess)
@@ -401,7 +413,7 @@ int eq_hfluid_new(const eq_fluid_configs* fluid, const eq_simulation_configs* si
     L.pitch = ((n + 63) / 64) * 64;
     L.e = L.r = nullptr;
     h->lv.push_back(L);
-    bytes += (size_t)L.pitch * n * (4 + 2);
+    bytes += (size_t)L.pitch * n * (4 + (mixed ? 4 : 2));
     if (n <= 4) break;
   }
   if (cudaMalloc(&h->lvblock, bytes) != cudaSuccess) return bail(EQ_ERR_OOM, "cudaMalloc (levels)");
@@ -410,10 +422,12 @@ int eq_hfluid_new(const eq_fluid_configs* fluid, const eq_simulation_configs* si
   for (auto& L : h->lv) {
     L.e = base;  // FP32 correction
     base += (size_t)L.pitch * L.n * 4;
-    L.r = base;  // stored right-hand side
-    base += (size_t)L.pitch * L.n * 2;
+    L.r = base;  // right-hand side in the velocity storage format
+    base += (size_t)L.pitch * L.n * (mixed ? 4 : 2);
   }
-  rc = storage == EQ_STORE_F16 ? h_init<__half>(h) : h_init<__nv_bfloat16>(h);
+  rc = storage == EQ_STORE_F16    ? h_init<__half, __half>(h)
+       : storage == EQ_STORE_BF16 ? h_init<__nv_bfloat16, __nv_bfloat16>(h)
+                                  : h_init<__half, float>(h);
   if (rc) {
     hfree(h);
     return rc;
@@ -453,7 +467,9 @@ int eq_hfluid_add_sources(eq_hfluid* h, int64_t n, const uint32_t* x, const uint
 int eq_hfluid_step(eq_hfluid* h) {
   int rc = h_check(h);
   if (rc) return rc;
-  rc = h->storage == EQ_STORE_F16 ? h_step<__half>(h) : h_step<__nv_bfloat16>(h);
+  rc = h->storage == EQ_STORE_F16    ? h_step<__half, __half>(h)
+       : h->storage == EQ_STORE_BF16 ? h_step<__nv_bfloat16, __nv_bfloat16>(h)
+                                     : h_step<__half, float>(h);
   if (rc) return rc;
   return read_err_word(h->plain);
 }
@@ -475,8 +491,15 @@ static int hfield_copy(eq_hfluid* h, int field, float* host, uint64_t n, bool to
   const size_t g = pl->grid_elems();
   float* stage = pl->field[2];  // FP32 staging grid of the plain handle
   const size_t w = (size_t)pl->S * sizeof(float);
-  if (to_host) {
-    if (h->storage == EQ_STORE_F16)
+  const bool f32 = h->storage == EQ_STORE_F16_SCALARS && field >= 2;  // stored in FP32
+  if (f32) {
+    EQ_CUDA(cudaMemcpy2DAsync(to_host ? (void*)host : h->f[field], to_host ? w : (size_t)pl->P * 4,
+                              to_host ? h->f[field] : (void*)host,
+                              to_host ? (size_t)pl->P * 4 : w, w, pl->S,
+                              to_host ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice,
+                              pl->stream));
+  } else if (to_host) {
+    if (h->storage != EQ_STORE_BF16)
       eqk::k_h_widen<__half><<<h_blocks(g), 256, 0, pl->stream>>>(stage, static_cast<__half*>(h->f[field]), g);
     else
       eqk::k_h_widen<__nv_bfloat16><<<h_blocks(g), 256, 0, pl->stream>>>(stage, static_cast<__nv_bfloat16*>(h->f[field]), g);
@@ -486,7 +509,7 @@ static int hfield_copy(eq_hfluid* h, int field, float* host, uint64_t n, bool to
   } else {
     EQ_CUDA(cudaMemcpy2DAsync(stage, (size_t)pl->P * 4, host, w, w, pl->S, cudaMemcpyHostToDevice,
                               pl->stream));
-    if (h->storage == EQ_STORE_F16)
+    if (h->storage != EQ_STORE_BF16)
       eqk::k_h_narrow<__half><<<h_blocks(g), 256, 0, pl->stream>>>(static_cast<__half*>(h->f[field]), stage, g);
     else
       eqk::k_h_narrow<__nv_bfloat16><<<h_blocks(g), 256, 0, pl->stream>>>(static_cast<__nv_bfloat16*>(h->f[field]), stage, g);

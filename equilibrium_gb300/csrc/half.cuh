@@ -35,9 +35,10 @@ __global__ void k_h_copy(T* __restrict__ dst, const T* __restrict__ src, size_t 
     dst[q] = src[q];
 }
 
-// add_density / add_velocity (fluid.rs:120-131), serially in array order.
-template <class T>
-__global__ void k_h_sources(T* de, T* sc, T* vx, T* vy, int S, int P, int64_t n,
+// add_density / add_velocity (fluid.rs:120-131), serially in array order
+// (scalars in TS, velocities in TV).
+template <class TS, class TV>
+__global__ void k_h_sources(TS* de, TS* sc, TV* vx, TV* vy, int S, int P, int64_t n,
                             const uint32_t* xs, const uint32_t* ys, const float* dd,
                             const float* du, const float* dv) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
@@ -176,9 +177,9 @@ __device__ __forceinline__ float h_bilerp_f(const Backtrace& b, float A, float B
   return b.s0 * (b.t0 * A + b.t1 * B) + b.s1 * (b.t0 * C + b.t1 * D);
 }
 
-template <class T>
+template <class T, class TU = T>
 __global__ void k_h_advect_rows(T* __restrict__ d, const T* __restrict__ d0,
-                                const T* __restrict__ u, const T* __restrict__ v, int S, int P,
+                                const TU* __restrict__ u, const TU* __restrict__ v, int S, int P,
                                 float dt0) {
   const int j = blockIdx.x + 1;
   const int N = S - 2;
@@ -214,8 +215,8 @@ __global__ void k_h_advect_rows(T* __restrict__ d, const T* __restrict__ d0,
 
 // init() (fluid.rs:602-606) on zeroed stored fields: vx = vy = 1, +0.9
 // density and scratch on the block [S/2-10, S/2+10]^2 (idx!-clamped).
-template <class T>
-__global__ void k_h_init(T* sc, T* de, T* vx, T* vy, int S, int P) {
+template <class TS, class TV>
+__global__ void k_h_init(TS* sc, TS* de, TV* vx, TV* vy, int S, int P) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= S || j >= S) return;

@@ -17,7 +17,8 @@ class HalfFluid:
                  viscousity: float, storage: str = "f16", pressure_rtol: float = 1e-5,
                  max_refinements: int = 30, device: int = 0):
         L = _lib.load()
-        st = {"f16": _lib.STORE_F16, "bf16": _lib.STORE_BF16}[storage]
+        st = {"f16": _lib.STORE_F16, "bf16": _lib.STORE_BF16,
+              "f16_scalars": _lib.STORE_F16_SCALARS}[storage]
         fc = _lib.FluidConfigsC(diffusion, viscousity, 0)
         sc = _lib.SimulationConfigsC(delta_t, frames, size)
         h = ctypes.c_void_p()

@@ -352,9 +352,10 @@ int eq_batch_launch_count(const eq_batch* b, uint64_t* count);
  * refinement and the post-projection divergence of the last frame. */
 #define EQ_STORE_F16 1
 #define EQ_STORE_BF16 2
-/* Batches only: density and scratch stored in FP16, the four velocity fields
- * in FP32 (advect's backtraces multiply a velocity's rounding by dt*N cells,
- * so FP16 velocities dominate the density error; see eq_batch_new_storage). */
+/* Density and scratch stored in FP16, the four velocity fields (and the
+ * pressure / divergence project keeps in them) in FP32, for batches and for
+ * the precision form: advect's backtraces multiply a velocity's rounding by
+ * dt*N cells, so FP16 velocities dominate the density error. */
 #define EQ_STORE_F16_SCALARS 3
 
 typedef struct eq_hstats {

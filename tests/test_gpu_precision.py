@@ -20,30 +20,33 @@ S, DT, K, DIFF, VISC = 66, 0.1, 20, 1e-4, 1e-4
 RECT = (S // 3, S // 4, S // 3 + S // 8, S // 4 + S // 6)
 
 
-def rounded(a, storage):
+def rounded(a, storage, field=0):
     import torch
+    if storage == "f16_scalars" and field >= 2:  # velocities stored in FP32
+        return np.asarray(a, dtype=np.float32)
     t = torch.from_numpy(np.asarray(a, dtype=np.float32))
-    return t.to(torch.float16 if storage == "f16" else torch.bfloat16).float().numpy()
+    return t.to(torch.bfloat16 if storage == "bf16" else torch.float16).float().numpy()
 
 
-@pytest.mark.parametrize("storage", ["f16", "bf16"])
+@pytest.mark.parametrize("storage", ["f16", "bf16", "f16_scalars"])
 def test_init_and_field_roundtrip(eqlib, storage):
     g = HalfFluid(S, DT, K, DIFF, VISC, storage)
     r = oracle.OracleFluid(S, DT, K, DIFF, VISC)
     for f in range(6):
-        np.testing.assert_array_equal(g.read_field(f), rounded(r.fields[f], storage))
+        np.testing.assert_array_equal(g.read_field(f), rounded(r.fields[f], storage, f))
     vals = np.random.default_rng(0).uniform(-300, 300, S * S).astype(np.float32)
-    g.write_field(2, vals)
-    np.testing.assert_array_equal(g.read_field(2), rounded(vals, storage))
+    for f in (1, 2):
+        g.write_field(f, vals)
+        np.testing.assert_array_equal(g.read_field(f), rounded(vals, storage, f))
     g.close()
 
 
 # Frame-1 accuracy against the converged FP64 step (measured: FP16 3.2e-3
 # density, 5.5e-3 velocity; BF16 0.12 / 0.05) with margin.
-TOL = {"f16": (1e-2, 2e-2), "bf16": (0.3, 0.15)}
+TOL = {"f16": (1e-2, 2e-2), "bf16": (0.3, 0.15), "f16_scalars": (1e-2, 2e-2)}
 
 
-@pytest.mark.parametrize("storage", ["f16", "bf16"])
+@pytest.mark.parametrize("storage", ["f16", "bf16", "f16_scalars"])
 def test_first_frame_vs_converged_f64(eqlib, storage):
     rng = np.random.default_rng(1)
     g = HalfFluid(S, DT, K, DIFF, VISC, storage)
@@ -72,7 +75,7 @@ def test_first_frame_vs_converged_f64(eqlib, storage):
     g.close()
 
 
-@pytest.mark.parametrize("storage", ["f16", "bf16"])
+@pytest.mark.parametrize("storage", ["f16", "bf16", "f16_scalars"])
 def test_projection_lowers_divergence(eqlib, storage):
     g = HalfFluid(130, 0.05, 20, 1e-5, 1e-5, storage)
     g.fill_obstacle(40, 30, 60, 70)
@@ -102,7 +105,7 @@ def test_rejects_bad_arguments(eqlib):
         HalfFluid(S, DT, K, DIFF, VISC, pressure_rtol=0.0)
 
 
-@pytest.mark.parametrize("storage", ["f16", "bf16"])
+@pytest.mark.parametrize("storage", ["f16", "bf16", "f16_scalars"])
 def test_concurrent_diffusions_match_one_stream(eqlib, storage):
     """The step's vy and density diffusions on side streams (the default) give
     the one-stream step's fields; only the FP64 norms' summation order can
