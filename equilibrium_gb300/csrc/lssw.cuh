@@ -71,6 +71,11 @@ constexpr int kSwRD = 16;     // diagonals kept per sweep ring
 constexpr int kSwRW = 36;     // floats per ring row: positions -2 .. 33
 constexpr int kSwPC = 128;    // columns of the x0 / code rings
 constexpr int kSwPX = 32;     // columns of the initial-x ring
+// Row strides of those rings, padded so that the copy warp's per-row chunk
+// writes (one row per lane) fall in different banks; the sweep warps' reads
+// (row + lane, column - lane) stay conflict-free.
+constexpr int kSwPCS = kSwPC + 4;  // x0 ring row (floats) and code ring row (bytes)
+constexpr int kSwPXS = kSwPX + 4;  // initial-x ring row (floats)
 constexpr int kSwAH = 5;      // a chunk copy is issued kSwAH periods before its use
 constexpr int kSwAHI = 4;     // an import load is checked kSwAHI periods after its issue
 constexpr int kSwMaxK = 20;   // sweeps per launch
@@ -107,9 +112,9 @@ __host__ __device__ inline LsSwLayout ls_sw_layout(int KG, int S) {
   L.ui = L.vr + (size_t)KG * kSwRD * kSwRW * 4;     // KG RD floats
   L.vp = L.ui + (size_t)KG * kSwRD * 4;             // RD RW floats
   L.x0r = (L.vp + (size_t)kSwRD * kSwRW * 4 + 15) / 16 * 16;  // nrw PC floats
-  L.cr = L.x0r + nrw * kSwPC * 4;                  // nrw PC bytes
-  L.xr = L.cr + nrw * kSwPC;                       // 33 PX floats
-  L.xt = L.xr + 33 * kSwPX * 4;                    // S floats: frame row 0
+  L.cr = L.x0r + nrw * kSwPCS * 4;                 // nrw PCS bytes
+  L.xr = (L.cr + nrw * kSwPCS + 15) / 16 * 16;     // 33 PXS floats
+  L.xt = L.xr + 33 * kSwPXS * 4;                   // S floats: frame row 0
   L.xb = L.xt + (size_t)S * 4;                     // S floats: frame row S-1
   L.cf = L.xb + (size_t)S * 4;                     // S bytes: column has fluid
   L.total = (L.cf + (size_t)S + 15) / 16 * 16;
@@ -354,8 +359,8 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
         const int n = u + ((off + 3) >> 2);
         if (n < 0 || 4 * n >= P) continue;
         const int sc = (4 * n) & (kSwPC - 1);
-        cp_async16(&X0R[q * kSwPC + sc], A.x0 + (size_t)r * P + 4 * n, true);
-        cp_async4(&CR[q * kSwPC + sc], A.code + (size_t)r * P + 4 * n, true);
+        cp_async16(&X0R[q * kSwPCS + sc], A.x0 + (size_t)r * P + 4 * n, true);
+        cp_async4(&CR[q * kSwPCS + sc], A.code + (size_t)r * P + 4 * n, true);
       }
       if (g == 0) {
         for (int q = lane; q < 33; q += 32) {
@@ -363,7 +368,8 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
           if (r > S - 1) continue;
           const int n = u + 1 - ((q + 3) >> 2);
           if (n < 0 || 4 * n >= P) continue;
-          cp_async16(&XR[q * kSwPX + ((4 * n) & (kSwPX - 1))], A.x + (size_t)r * P + 4 * n, true);
+          cp_async16(&XR[q * kSwPXS + ((4 * n) & (kSwPX - 1))], A.x + (size_t)r * P + 4 * n,
+                     true);
         }
       }
       cp_async_commit();
@@ -490,10 +496,10 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
     W.prev = kk > 0 ? VR + (size_t)(kk - 1) * kSwRD * kSwRW : VP;
     W.ui = UI + (size_t)kr * kSwRD;
     const int rrow = 2 * (nk - 1 - kr) + lane;
-    W.x0row = X0R + (real ? rrow : 0) * kSwPC;
-    W.crow = CR + (real ? rrow : 0) * kSwPC;
-    W.xrl = XR + lane * kSwPX;
-    W.xrd = XR + (lane + 1) * kSwPX;
+    W.x0row = X0R + (real ? rrow : 0) * kSwPCS;
+    W.crow = CR + (real ? rrow : 0) * kSwPCS;
+    W.xrl = XR + lane * kSwPXS;
+    W.xrd = XR + (lane + 1) * kSwPXS;
     W.xt = XT;
     W.xb = XB;
     W.cf = CF;
