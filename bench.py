@@ -255,36 +255,57 @@ def batch_cpu_baseline(cfgs, rects, nsample: int = 24, seed: int = 7):
                       f"f32 step ({secs:.1f} s)"}
 
 
-def batch_half_errors(storage: str, nsample: int, local_rank: int, frames=(1, 3)):
+def _half_ref_task(task):
+    """The reference step of one batch scene on the host, in f32 and f64:
+    density at each checkpoint frame (a worker of batch_half_errors)."""
+    import oracle
+    (size, dt, K, dif, vis), rects, frames = task
+    out = {}
+    for dtype in (np.float32, np.float64):
+        r = oracle.OracleFluid(size, dt, K, dif, vis, dtype=dtype)
+        for rc in rects:
+            r.fill_obstacle(*rc)
+        done, dens = 0, []
+        for fr in frames:
+            for _ in range(fr - done):
+                r.step()
+            done = fr
+            dens.append(np.array(r.fields[1], dtype=np.float64))
+        out[np.dtype(dtype).name] = dens
+    return out
+
+
+def batch_half_errors(storage: str, nsample: int, local_rank: int, frames=(1, 50, 200)):
     """Relative L2 density error of half-storage batch scenes against the f64
     reference step (the oracle built with f64), for a seeded sample of the
-    workload's scenes: the median and maximum over the sample per frame."""
-    import oracle
+    workload's scenes, at frames 1, 50 and 200: the median and maximum over
+    the sample per frame, beside the reference's own f32 step's distance to
+    the f64 step on the same scenes (the flow's sensitivity, which any
+    rounding grows, separated from the storage error)."""
+    import multiprocessing as mp
     from equilibrium_gb300.batch import Batch, SceneConfig
     from equilibrium_gb300.precision import rel_l2
     cfgs, rects = batch_workload()
     rng = np.random.default_rng(11)
     pick = [int(q) for q in rng.choice(len(cfgs), size=nsample, replace=False)
             if cfgs[int(q)][0] <= 258][:nsample]
+    tasks = [(cfgs[q], rects[q], tuple(frames)) for q in pick]
+    with mp.get_context("spawn").Pool(min(len(tasks), os.cpu_count() or 1)) as pool:
+        refs = pool.map(_half_ref_task, tasks)
     b = Batch([SceneConfig(*cfgs[q]) for q in pick], device=local_rank, storage=storage)
-    refs = []
     for k, q in enumerate(pick):
-        size, dt, K, dif, vis = cfgs[q]
-        r = oracle.OracleFluid(size, dt, K, dif, vis, dtype=np.float64)
         for rc in rects[q]:
-            r.fill_obstacle(*rc)
             b.fill_obstacle(k, *rc)
-        refs.append(r)
     res, done = {}, 0
-    for fr in frames:
+    for n, fr in enumerate(frames):
         b.step(fr - done)
-        for r in refs:
-            for _ in range(fr - done):
-                r.step()
         done = fr
-        errs = [rel_l2(b.read_field(k, _lib_field_density()), r.fields[1])
-                for k, r in enumerate(refs)]
-        res[f"frame_{fr}"] = {"median": float(np.median(errs)), "max": float(np.max(errs))}
+        errs = [rel_l2(b.read_field(k, _lib_field_density()), refs[k]["float64"][n])
+                for k in range(len(pick))]
+        drift = [rel_l2(refs[k]["float32"][n], refs[k]["float64"][n]) for k in range(len(pick))]
+        res[f"frame_{fr}"] = {"median": float(np.median(errs)), "max": float(np.max(errs)),
+                              "f32_step_median": float(np.median(drift)),
+                              "f32_step_max": float(np.max(drift))}
     b.close()
     res["scenes"] = f"{len(pick)} seeded scenes of the workload with size <= 258"
     return res
@@ -350,7 +371,7 @@ def _precision_reference(task):
 
 
 def run_precision_form(local_rank: int, frames: int, size: int = PREC_SIZE,
-                       err_frames=(1,), storages=("f16", "bf16")):
+                       err_frames=(1,), storages=("f16", "bf16", "f16_scalars")):
     """The precision form on one scene: throughput of `frames` timed frames per
     storage format, its refinement statistics, and at `err_frames` the relative
     L2 density error, max-abs velocity error and post-projection divergence
@@ -1012,7 +1033,7 @@ def summarize(line):
                      "frame_frac": r3(g(line, "roofline", "frame_roofline_frac")),
                      "parity": g(line, "parity", "status")}}
     forms = line.get("forms", {})
-    for name in ("batched", "batched_f16", "batched_f16_scalars"):
+    for name in ("batched", "batched_f16", "batched_f16_scalars", "batched_bf16"):
         fm = forms.get(name)
         if fm:
             out[name] = {"value": r3(fm.get("value")), "vs_plain": r3(fm.get("vs_plain")),
@@ -1020,10 +1041,12 @@ def summarize(line):
                          "err": g(fm, "density_rel_l2_vs_f64"), "error": fm.get("error")}
     pr = forms.get("precision")
     if pr:
-        for k in ("f16", "bf16"):
+        for k in ("f16", "bf16", "f16_scalars"):
             if k in pr:
+                fe = g(pr[k], "errors", "frame_1", "f64_converged_pressure", "density_rel_l2")
                 out[f"precision_{k}"] = {"value": r3(pr[k].get("value")),
-                                         "vs_plain": r3(pr[k].get("vs_plain"))}
+                                         "vs_plain": r3(pr[k].get("vs_plain")),
+                                         "density_err_frame_1": r3(fe)}
     df = forms.get("differentiation")
     if df:
         out["differentiation"] = {"value": r3(df.get("value")), "error": df.get("error")}
@@ -1249,9 +1272,11 @@ def run_ours(args):
                                                      autotune=False, err_sample=24))
         form("batched_f16_scalars", lambda: run_batched_form(
             local_rank, args.batch_frames, 0, "f16_scalars", autotune=False, err_sample=24))
+        form("batched_bf16", lambda: run_batched_form(local_rank, args.batch_frames, 0, "bf16",
+                                                      autotune=False, err_sample=24))
         form("precision", lambda: run_precision_form(local_rank, args.precision_frames))
         form("differentiation", lambda: run_diff_form(local_rank, fd_dirs=args.fd_dirs))
-        for k in ("f16", "bf16"):
+        for k in ("f16", "bf16", "f16_scalars"):
             if "precision" in forms and k in forms["precision"]:
                 forms["precision"][k]["vs_plain"] = forms["precision"][k]["value"] / value
     line = {"metric": baseline_metric(), "value": value, "unit": "cell-steps/s", "n_gpus": world,

@@ -39,5 +39,5 @@ def test_summary_digest_of_a_bench_line():
     s = bench.summarize(line)
     assert s["plain"] == {"value": 3.2e8, "e2e": 3.0e8, "frame_frac": 0.012, "parity": "bit-exact"}
     assert s["batched"]["vs_plain"] == 3.4 and s["batched"]["frac"] == 0.03
-    assert s["precision_f16"] == {"value": 2e8, "vs_plain": 0.6}
+    assert s["precision_f16"] == {"value": 2e8, "vs_plain": 0.6, "density_err_frame_1": None}
     assert s["differentiation"]["error"] == "RuntimeError: x"
