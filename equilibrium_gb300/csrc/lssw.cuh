@@ -156,9 +156,10 @@ __device__ __forceinline__ float gs_update(float x0, float a, float sum, float c
 // One sweep warp's state and constants.
 struct SwWarp {
   // lane state: the value at the previous step (L), the one before, last
-  // step's U and the code of the previous cell
+  // step's U, the code of the previous cell and (frame rows) the column flag
+  // of the previous cell
   float vcur, vprev, uprev;
-  unsigned cprev;
+  unsigned cprev, cfprev;
   // lane constants
   int lane, j, S, N, k;
   bool interior, top, bot, idle, pasRow;
@@ -170,22 +171,30 @@ struct SwWarp {
   const uint8_t* crow;
   const float* xrl;    // first sweep of the first group: initial-x ring rows
   const float* xrd;
+  const float* xf;     // this lane's frame row (row 0 or S-1) in shared memory
   const float* xt;     // frame rows and column flags in shared memory
   const float* xb;
   const uint8_t* cf;
   unsigned long long* edgeOut;  // halo export (lanes 30, 31), null if none
   unsigned long long* gexpOut;  // group export, null if none
   float* xlast;                 // x + j P - lane for the last sweep, else null
-  bool hasFrame;
   unsigned tag;
 };
 
-template <int MODE, bool FAST, bool FIRSTX>
-__device__ __forceinline__ void sw_step(SwWarp& w, int d) {
+// Step d = dp + q of a sweep warp (dp a multiple of kSwQ, q < kSwQ). Ring
+// slot d % kSwRD holds diagonal d - 1, so a period's slots are consecutive
+// and their offsets constants of the unrolled period. FAST: every interior
+// lane at 2 <= i <= N (the rare boundary actions still vote into the general
+// rules); FRAME: the warp holds a frame row, whose lane takes the frame
+// cell's value without a branch.
+template <int MODE, bool FAST, bool FIRSTX, bool FRAME>
+__device__ __forceinline__ void sw_step(SwWarp& w, int dp, int q) {
   const unsigned FULL = 0xffffffffu;
   const int lane = w.lane;
+  const int d = dp + q;
   const int i = d - lane;
-  const int ro = ((d - 1) & (kSwRD - 1)) * kSwRW;
+  const int slot = (dp & (kSwRD - 1)) + q;
+  const int ro = slot * kSwRW;
   float R, D;
   if (FIRSTX) {
     R = w.xrl[(i + 1) & (kSwPX - 1)];
@@ -194,15 +203,24 @@ __device__ __forceinline__ void sw_step(SwWarp& w, int d) {
     R = w.prev[ro + lane];
     D = w.prev[ro + lane + 1];
   }
-  const float Ui = w.ui[(d - 1) & (kSwRD - 1)];
+  const float Ui = w.ui[slot];
   float U = __shfl_up_sync(FULL, w.vcur, 1);
   if (lane == 0) U = Ui;
   const int ci = i & (kSwPC - 1);
   const float X0 = w.x0row[ci];
   const unsigned cd = w.crow[ci];
+  const int S = w.S, N = w.N;
+  // the frame cell of this column (frame-row lanes), loaded by every lane
+  float xfc = 0.0f;
+  unsigned cfc = 0u;
+  if (FRAME) {
+    const int ic = min(max(i, 0), S - 1);
+    xfc = w.xf[ic];
+    if (MODE == kPassive) cfc = w.cf[ic];
+  }
   const float gs = gs_update(X0, w.a, fadd(fadd(fadd(R, w.vcur), D), U), w.cr);
   const bool fix = MODE == kCol && lane == 0 && (cd & kCodeAboveDown) != 0 &&
-                   (w.interior || w.bot) && (unsigned)(i - 1) < (unsigned)w.N;
+                   (w.interior || w.bot) && (unsigned)(i - 1) < (unsigned)N;
   bool general = !FAST;
   if (FAST && MODE != kPassive) {
     const unsigned actMask =
@@ -210,23 +228,17 @@ __device__ __forceinline__ void sw_step(SwWarp& w, int d) {
     general = __any_sync(FULL, w.interior && (((w.cprev & actMask) != 0u) || fix));
   }
   float vnew, post;
-  const int S = w.S, N = w.N;
   if (!general) {
     vnew = gs;
     post = w.vcur;
-    if (w.hasFrame) {  // frame-row lanes: the frame cell as the sweep sees it
+    if (FRAME) {  // frame-row lanes: the frame cell as the sweep sees it
       const bool fl = w.top || w.bot;
-      const int ic = min(max(i, 0), S - 1);
-      if (fl) {
-        const float xf = w.top ? w.xt[ic] : w.xb[ic];
-        vnew = (unsigned)i < (unsigned)S
-                   ? ((MODE == kPassive && w.top && w.k > 0 && w.cf[ic]) ? D : xf)
-                   : w.vcur;
-      }
+      const float vf = (MODE == kPassive && w.top && w.k > 0 && cfc) ? D : xfc;
+      vnew = fl ? vf : vnew;
       if (MODE == kPassive) {
         const float vdown = __shfl_down_sync(FULL, vnew, 1);
-        const int im1 = min(max(i - 1, 0), S - 1);
-        if (fl && (unsigned)(i - 2) < (unsigned)N && w.cf[im1]) post = w.top ? vdown : w.uprev;
+        const bool pc = fl && (unsigned)(i - 2) < (unsigned)N && w.cfprev != 0u;
+        post = pc ? (w.top ? vdown : w.uprev) : post;
       }
     }
   } else {
@@ -270,25 +282,22 @@ __device__ __forceinline__ void sw_step(SwWarp& w, int d) {
   }
   float* const wrow = w.own + ro;
   wrow[lane + 2] = post;
-  float pm1 = 0.0f;  // position -1 of this diagonal (lane 0): the fix, or the imported value
   if (MODE == kCol && fix) wrow[1] = -vnew;
-  if (w.edgeOut && d >= 1) {  // lanes 30, 31: record d-1 = [post30, -, uval31, post31]
-    if (lane >= 30)
-      sw_st2(w.edgeOut + (size_t)(d - 1) * 4, lane == 31 ? w.vcur : post, post, w.tag);
-  }
-  if (w.gexpOut) {  // record d: word p + 2 = position p of diagonal d-1
+  // lanes 30, 31: halo record d-1 = [post30, -, uval31, post31]
+  if (w.edgeOut && d >= 1)
+    sw_st2(w.edgeOut + (size_t)(d - 1) * 4, lane == 31 ? w.vcur : post, post, w.tag);
+  if (w.gexpOut) {  // group record d: word p + 2 = position p of diagonal d-1
     unsigned long long* const rec = w.gexpOut + (size_t)d * kSwGrpWords;
     sw_st1(rec + lane + 2, post, w.tag);
-    if (lane < 2) {
-      pm1 = (MODE == kCol && fix) ? -vnew : wrow[1 - lane];
-      sw_st1(rec + (1 - lane), pm1, w.tag);
-    }
+    if (lane < 2)
+      sw_st1(rec + (1 - lane), (MODE == kCol && fix) ? -vnew : wrow[1 - lane], w.tag);
   }
   if (w.xlast && w.interior && (unsigned)(i - 1) < (unsigned)N) w.xlast[d] = vnew;
   w.vprev = w.vcur;
   w.vcur = vnew;
   w.uprev = U;
   w.cprev = cd;
+  if (FRAME) w.cfprev = cfc;
 }
 
 template <int MODE>
@@ -433,8 +442,8 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
       for (int s = 0; s < 5; ++s) {
         if (put && ok_of(u, s)) {
           const int w = lane + 32 * s;
-          const int r = rec_of(u, s);  // diagonal r - 1
-          VP[((r - 1) & (kSwRD - 1)) * kSwRW + (w % 34)] =
+          const int r = rec_of(u, s);  // diagonal r - 1, in slot r
+          VP[(r & (kSwRD - 1)) * kSwRW + (w % 34)] =
               __uint_as_float((unsigned)(v[s] & 0xffffffffull));
         }
       }
@@ -485,7 +494,7 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
     W.top = W.j == 0;
     W.bot = W.j == S - 1;
     W.idle = !(W.interior || W.top || W.bot);
-    W.hasFrame = __any_sync(FULL, W.top || W.bot);
+    const bool hasFrame = __any_sync(FULL, W.top || W.bot);
     W.pasRow = MODE == kPassive && W.interior && A.rowfl[W.j] != 0;
     W.xL = W.interior ? A.x[(size_t)W.j * P] : 0.0f;
     W.xR = W.interior ? A.x[(size_t)W.j * P + (S - 1)] : 0.0f;
@@ -502,6 +511,7 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
     W.xrd = XR + (lane + 1) * kSwPXS;
     W.xt = XT;
     W.xb = XB;
+    W.xf = W.bot ? XB : XT;
     W.cf = CF;
     W.edgeOut = (real && b < B - 1 && lane >= 30)
                     ? A.edge + ((size_t)b * K + k) * A.RE * 4 + (lane == 30 ? 0 : 2)
@@ -511,7 +521,7 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
     W.xlast = (real && k == K - 1) ? A.x + (size_t)max(W.j, 0) * P - lane : nullptr;
     W.tag = tag;
     W.vcur = W.vprev = W.uprev = 0.0f;
-    W.cprev = 0u;
+    W.cprev = W.cfprev = 0u;
     const bool firstX = g == 0 && kk == 0;
     // fast range: every interior lane at 2 <= i <= N
     const int lA = max(0, 1 - j0), lB = min(31, N - j0);
@@ -555,7 +565,7 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
         }
       }
       if (put && need) {
-        const int s = imp_dd(u) & (kSwRD - 1);
+        const int s = (imp_dd(u) + 1) & (kSwRD - 1);  // diagonal dd lives in slot dd + 1
         const float v = __uint_as_float((unsigned)(w & 0xffffffffull));
         if (iw == 2)
           UIk[s] = v;
@@ -587,20 +597,28 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
           const int dp = cp * kSwQ - kSwLg * kk;
           if (dp >= dF0 && dp + kSwQ - 1 <= dF1) {
             if (firstX) {
+              if (hasFrame) {
 #pragma unroll
-              for (int q = 0; q < kSwQ; ++q) sw_step<MODE, true, true>(W, dp + q);
+                for (int q = 0; q < kSwQ; ++q) sw_step<MODE, true, true, true>(W, dp, q);
+              } else {
+#pragma unroll
+                for (int q = 0; q < kSwQ; ++q) sw_step<MODE, true, true, false>(W, dp, q);
+              }
+            } else if (hasFrame) {
+#pragma unroll
+              for (int q = 0; q < kSwQ; ++q) sw_step<MODE, true, false, true>(W, dp, q);
             } else {
 #pragma unroll
-              for (int q = 0; q < kSwQ; ++q) sw_step<MODE, true, false>(W, dp + q);
+              for (int q = 0; q < kSwQ; ++q) sw_step<MODE, true, false, false>(W, dp, q);
             }
           } else {
             for (int q = 0; q < kSwQ; ++q) {
               const int d = dp + q;
               if (d < 0 || d > S + 31) continue;
               if (firstX)
-                sw_step<MODE, false, true>(W, d);
+                sw_step<MODE, false, true, true>(W, dp, q);
               else
-                sw_step<MODE, false, false>(W, d);
+                sw_step<MODE, false, false, true>(W, dp, q);
             }
           }
         }

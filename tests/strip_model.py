@@ -169,7 +169,7 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                         continue
                     rec = dd + 32
                     assert (etag[b - 1, k, rec, [0, 2, 3]] == TAG).all(), ("halo", b, k, rec)
-                    s = dd % RD
+                    s = (dd + 1) % RD  # diagonal dd lives in slot dd + 1
                     VR.write((kk, s, 0), edge[b - 1, k, rec, 0], ("vr", k, dd, -2), cp + 1)
                     UI.write((kk, s), edge[b - 1, k, rec, 2], ("ui", k, dd), cp + 1)
                     VR.write((kk, s, 1), edge[b - 1, k, rec, 3], ("vr", k, dd, -1), cp + 1)
@@ -182,7 +182,7 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                         continue
                     assert (gtag[b, g - 1, d, :34] == TAG).all(), ("group", b, g, d)
                     for p in range(-2, 32):
-                        VP.write(((d - 1) % RD, p + 2), gexp[b, g - 1, d, p + 2],
+                        VP.write((d % RD, p + 2), gexp[b, g - 1, d, p + 2],
                                  ("vr", kF - 1, d - 1, p), cp + 1)
 
             for cp in range(-AH - 1, 0):
@@ -228,11 +228,11 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                         D = np.zeros(32, np.float32)
                         for l in range(32):
                             if kk > 0:
-                                sl = (kk - 1, (d - 1) % RD)
+                                sl = (kk - 1, d % RD)
                                 R[l] = VR.read(sl + (l,), ("vr", k - 1, d - 1, l - 2), cp, useR[l], "R")
                                 D[l] = VR.read(sl + (l + 1,), ("vr", k - 1, d - 1, l - 1), cp, useD[l], "D")
                             elif g > 0:
-                                sl = ((d - 1) % RD,)
+                                sl = (d % RD,)
                                 R[l] = VP.read(sl + (l,), ("vr", k - 1, d - 1, l - 2), cp, useR[l], "R")
                                 D[l] = VP.read(sl + (l + 1,), ("vr", k - 1, d - 1, l - 1), cp, useD[l], "D")
                             else:
@@ -240,7 +240,7 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                                 D[l] = XR.read((l + 1, i[l] % PX), ("x", j[l] + 1, i[l]), cp, useD[l], "XR")
                         U = np.empty(32, np.float32)
                         U[1:] = vcur[kk, :-1]
-                        U[0] = UI.read((kk, (d - 1) % RD), ("ui", k, d - 1), cp, bool(gsl[0]), "UI")
+                        U[0] = UI.read((kk, d % RD), ("ui", k, d - 1), cp, bool(gsl[0]), "UI")
                         X0 = np.zeros(32, np.float32)
                         cd = np.zeros(32, np.uint8)
                         useC = (interior | bot) & (i >= 1) & (i <= N)
@@ -291,7 +291,7 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                                                   gs[interior].view(np.uint32))
                             assert np.array_equal(post[interior].view(np.uint32),
                                                   vc[interior].view(np.uint32))
-                        s = (d - 1) % RD
+                        s = d % RD  # slot d holds diagonal d - 1
                         for l in range(32):
                             VR.write((kk, s, l + 2), post[l], ("vr", k, d - 1, l), cp + 1)
                         fixv = None
