@@ -451,6 +451,7 @@ int sw_groups_for(const eq_fluid* h, int K) {
     G = std::max(1, std::min(kSwMaxGroups, 152 / std::max(B, 1)));
   }
   G = std::min(G, std::min(K, kSwMaxGroups));
+  G = std::max(G, (K + eqk::kSwMaxKG - 1) / eqk::kSwMaxKG);  // at most kSwMaxKG sweeps a block
   const int KG = (K + G - 1) / G;
   return (K + KG - 1) / KG;  // groups that hold a sweep
 }

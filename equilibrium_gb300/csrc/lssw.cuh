@@ -79,7 +79,7 @@ constexpr int kSwPXS = kSwPX + 4;  // initial-x ring row (floats)
 constexpr int kSwAH = 5;      // a chunk copy is issued kSwAH periods before its use
 constexpr int kSwAHI = 4;     // an import load is checked kSwAHI periods after its issue
 constexpr int kSwMaxK = 20;   // sweeps per launch
-constexpr int kSwMaxKG = 20;  // sweeps per block
+constexpr int kSwMaxKG = 10;  // sweeps per block (its warps' registers hold a period's operands)
 constexpr int kSwGrpWords = 36;  // words per group-export record (34 used)
 static_assert(kSwLg >= kSwQ, "a ring value must be one barrier old when read");
 
@@ -181,44 +181,60 @@ struct SwWarp {
   unsigned tag;
 };
 
-// Step d = dp + q of a sweep warp (dp a multiple of kSwQ, q < kSwQ). Ring
-// slot d % kSwRD holds diagonal d - 1, so a period's slots are consecutive
-// and their offsets constants of the unrolled period. FAST: every interior
-// lane at 2 <= i <= N (the rare boundary actions still vote into the general
-// rules); FRAME: the warp holds a frame row, whose lane takes the frame
-// cell's value without a branch.
-template <int MODE, bool FAST, bool FIRSTX, bool FRAME>
-__device__ __forceinline__ void sw_step(SwWarp& w, int dp, int q) {
+// The shared-memory operands of step d = dp + q of a sweep warp (dp a
+// multiple of kSwQ, q < kSwQ): loaded for a whole period before its first
+// step, so that no load waits behind a previous step's ring store. Ring slot
+// d % kSwRD holds diagonal d - 1, so a period's slots are consecutive.
+struct SwOps {
+  float R, D, Ui, X0, xf;
+  unsigned cd, cf;
+};
+
+template <int MODE, bool FIRSTX, bool FRAME>
+__device__ __forceinline__ SwOps sw_load(const SwWarp& w, int dp, int q) {
+  const int lane = w.lane;
+  const int d = dp + q;
+  const int i = d - lane;
+  const int slot = (dp & (kSwRD - 1)) + q;
+  SwOps o;
+  if (FIRSTX) {
+    o.R = w.xrl[(i + 1) & (kSwPX - 1)];
+    o.D = w.xrd[i & (kSwPX - 1)];
+  } else {
+    o.R = w.prev[slot * kSwRW + lane];
+    o.D = w.prev[slot * kSwRW + lane + 1];
+  }
+  o.Ui = w.ui[slot];
+  const int ci = i & (kSwPC - 1);
+  o.X0 = w.x0row[ci];
+  o.cd = w.crow[ci];
+  o.xf = 0.0f;
+  o.cf = 0u;
+  if (FRAME) {  // the frame cell of this column (frame-row lanes), every lane
+    const int ic = min(max(i, 0), w.S - 1);
+    o.xf = w.xf[ic];
+    if (MODE == kPassive) o.cf = w.cf[ic];
+  }
+  return o;
+}
+
+// Step d = dp + q from its loaded operands. FAST: every interior lane at
+// 2 <= i <= N (the rare boundary actions still vote into the general rules);
+// FRAME: the warp holds a frame row, whose lane takes the frame cell's value
+// without a branch.
+template <int MODE, bool FAST, bool FRAME>
+__device__ __forceinline__ void sw_compute(SwWarp& w, int dp, int q, const SwOps& o) {
   const unsigned FULL = 0xffffffffu;
   const int lane = w.lane;
   const int d = dp + q;
   const int i = d - lane;
   const int slot = (dp & (kSwRD - 1)) + q;
-  const int ro = slot * kSwRW;
-  float R, D;
-  if (FIRSTX) {
-    R = w.xrl[(i + 1) & (kSwPX - 1)];
-    D = w.xrd[i & (kSwPX - 1)];
-  } else {
-    R = w.prev[ro + lane];
-    D = w.prev[ro + lane + 1];
-  }
-  const float Ui = w.ui[slot];
+  const float R = o.R, D = o.D;
+  const unsigned cd = o.cd;
   float U = __shfl_up_sync(FULL, w.vcur, 1);
-  if (lane == 0) U = Ui;
-  const int ci = i & (kSwPC - 1);
-  const float X0 = w.x0row[ci];
-  const unsigned cd = w.crow[ci];
+  if (lane == 0) U = o.Ui;
   const int S = w.S, N = w.N;
-  // the frame cell of this column (frame-row lanes), loaded by every lane
-  float xfc = 0.0f;
-  unsigned cfc = 0u;
-  if (FRAME) {
-    const int ic = min(max(i, 0), S - 1);
-    xfc = w.xf[ic];
-    if (MODE == kPassive) cfc = w.cf[ic];
-  }
-  const float gs = gs_update(X0, w.a, fadd(fadd(fadd(R, w.vcur), D), U), w.cr);
+  const float gs = gs_update(o.X0, w.a, fadd(fadd(fadd(R, w.vcur), D), U), w.cr);
   const bool fix = MODE == kCol && lane == 0 && (cd & kCodeAboveDown) != 0 &&
                    (w.interior || w.bot) && (unsigned)(i - 1) < (unsigned)N;
   bool general = !FAST;
@@ -233,7 +249,7 @@ __device__ __forceinline__ void sw_step(SwWarp& w, int dp, int q) {
     post = w.vcur;
     if (FRAME) {  // frame-row lanes: the frame cell as the sweep sees it
       const bool fl = w.top || w.bot;
-      const float vf = (MODE == kPassive && w.top && w.k > 0 && cfc) ? D : xfc;
+      const float vf = (MODE == kPassive && w.top && w.k > 0 && o.cf) ? D : o.xf;
       vnew = fl ? vf : vnew;
       if (MODE == kPassive) {
         const float vdown = __shfl_down_sync(FULL, vnew, 1);
@@ -280,7 +296,7 @@ __device__ __forceinline__ void sw_step(SwWarp& w, int dp, int q) {
       post = 0.0f;
     }
   }
-  float* const wrow = w.own + ro;
+  float* const wrow = w.own + slot * kSwRW;
   wrow[lane + 2] = post;
   if (MODE == kCol && fix) wrow[1] = -vnew;
   // lanes 30, 31: halo record d-1 = [post30, -, uval31, post31]
@@ -297,7 +313,17 @@ __device__ __forceinline__ void sw_step(SwWarp& w, int dp, int q) {
   w.vcur = vnew;
   w.uprev = U;
   w.cprev = cd;
-  if (FRAME) w.cfprev = cfc;
+  if (FRAME) w.cfprev = o.cf;
+}
+
+// A fast period: every operand loaded first, then the kSwQ steps.
+template <int MODE, bool FIRSTX, bool FRAME>
+__device__ __forceinline__ void sw_period_fast(SwWarp& w, int dp) {
+  SwOps o[kSwQ];
+#pragma unroll
+  for (int q = 0; q < kSwQ; ++q) o[q] = sw_load<MODE, FIRSTX, FRAME>(w, dp, q);
+#pragma unroll
+  for (int q = 0; q < kSwQ; ++q) sw_compute<MODE, true, FRAME>(w, dp, q, o[q]);
 }
 
 template <int MODE>
@@ -597,28 +623,23 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
           const int dp = cp * kSwQ - kSwLg * kk;
           if (dp >= dF0 && dp + kSwQ - 1 <= dF1) {
             if (firstX) {
-              if (hasFrame) {
-#pragma unroll
-                for (int q = 0; q < kSwQ; ++q) sw_step<MODE, true, true, true>(W, dp, q);
-              } else {
-#pragma unroll
-                for (int q = 0; q < kSwQ; ++q) sw_step<MODE, true, true, false>(W, dp, q);
-              }
+              if (hasFrame)
+                sw_period_fast<MODE, true, true>(W, dp);
+              else
+                sw_period_fast<MODE, true, false>(W, dp);
             } else if (hasFrame) {
-#pragma unroll
-              for (int q = 0; q < kSwQ; ++q) sw_step<MODE, true, false, true>(W, dp, q);
+              sw_period_fast<MODE, false, true>(W, dp);
             } else {
-#pragma unroll
-              for (int q = 0; q < kSwQ; ++q) sw_step<MODE, true, false, false>(W, dp, q);
+              sw_period_fast<MODE, false, false>(W, dp);
             }
           } else {
             for (int q = 0; q < kSwQ; ++q) {
               const int d = dp + q;
               if (d < 0 || d > S + 31) continue;
               if (firstX)
-                sw_step<MODE, false, true, true>(W, dp, q);
+                sw_compute<MODE, false, true>(W, dp, q, sw_load<MODE, true, true>(W, dp, q));
               else
-                sw_step<MODE, false, false, true>(W, dp, q);
+                sw_compute<MODE, false, true>(W, dp, q, sw_load<MODE, false, true>(W, dp, q));
             }
           }
         }
