@@ -834,14 +834,15 @@ def run_case(case: str):
         print(json.dumps({"case": case, "ms": (time.perf_counter() - t) * 1e3,
                           "cells": b.cell_count()}))
         b.close()
-    elif case == "lscs1024":
+    elif case in ("lscs1024", "lssw1024"):
         from equilibrium_gb300 import _lib
         from equilibrium_gb300.simulation import Fluid, FluidConfigs, SimulationConfigs
         L = _lib.load()
         f = Fluid(FluidConfigs(DIFF, VISC, False), SimulationConfigs(DT, ITERS, SIZE))
         _lib.check(L.eq_fluid_fill_obstacle(f.handle, SIZE // 4, SIZE // 4, SIZE // 3,
                                             SIZE // 3))
-        _lib.check(L.eq_fluid_set_solver(f.handle, 2))  # the cluster form for every solve
+        # every solve by the streamed cluster form (2) or the strip wavefront (3)
+        _lib.check(L.eq_fluid_set_solver(f.handle, 2 if case == "lscs1024" else 3))
         ms = []
         for _ in range(2):
             t = time.perf_counter()
@@ -1312,13 +1313,13 @@ def main():
                     help="only the differentiation form (N=256, 64 frames)")
     ap.add_argument("--case", default=None,
                     choices=["batch256", "batch256_f16", "precision1024", "diff256",
-                             "lscs1024"],
+                             "lscs1024", "lssw1024"],
                     help="one small run for profiling: 'batch256' = one frame of 256 scenes of "
                          "the batched workload (after one warm-up frame), 'precision1024' = two "
                          "frames of the precision form at N = 1024 (FP16), 'diff256' = one "
                          "gradient of the differentiation workload at N = 256 over 4 frames, "
                          "'lscs1024' = two Passive lin_solves at N = 1024 by the streamed "
-                         "cluster wavefront")
+                         "cluster wavefront, 'lssw1024' = the same by the strip wavefront")
     ap.add_argument("--study-size", type=int, default=514,
                     help="size (N + 2) of --precision-study")
     ap.add_argument("--precision-study", action="store_true",

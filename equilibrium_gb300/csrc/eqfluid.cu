@@ -135,7 +135,8 @@ struct eq_fluid {
   unsigned long long* sw_edge[3] = {};
   unsigned long long* sw_gexp[3] = {};  // group exports [strips][groups-1][records+1][36]
   unsigned* sw_ctr[3] = {};
-  int sw_groups = 0;  // sweep groups per strip (0: by size)
+  int sw_groups = 0;  // sweep groups per strip (0: by size, fewest beside other solves)
+  bool sw_shared = false;  // step(): this solve runs beside the side streams' solves
   int sw_slack = 0;   // periods a block's producers must be ahead before it starts
 
   size_t grid_elems() const { return (size_t)P * S; }
@@ -443,12 +444,17 @@ int launch_lin_solve_cluster(eq_fluid* h, int mode, float* x, const float* x0, f
 }
 
 // Sweep groups of the strip wavefront for K sweeps on this grid: blocks of
-// one strip share its sweeps so that about one block per SM works on a solve.
+// one strip share its sweeps so that about one block per SM works on a solve
+// that runs alone; a solve that shares the GPU with step()'s concurrent
+// diffusions (a side stream's, or the main stream's beside them) takes the
+// fewest groups, so that the three fit the SMs together.
 int sw_groups_for(const eq_fluid* h, int K) {
   int G = h->sw_groups;
   if (G <= 0) {
     const int B = eqk::ls_sw_strips((int)h->S, K);
-    G = std::max(1, std::min(kSwMaxGroups, 152 / std::max(B, 1)));
+    G = (h->sw_shared || h->cur_slot != 0)
+            ? 1
+            : std::max(1, std::min(kSwMaxGroups, 152 / std::max(B, 1)));
   }
   G = std::min(G, std::min(K, kSwMaxGroups));
   G = std::max(G, (K + eqk::kSwMaxKG - 1) / eqk::kSwMaxKG);  // at most kSwMaxKG sweeps a block
@@ -551,7 +557,11 @@ int launch_lin_solve(eq_fluid* h, int mode, float* x, const float* x0, float a, 
   const int64_t K = h->frames;
   if (K <= 0) return EQ_OK;
   const float c_recip = 1.0f / c;  // fluid.rs:311, IEEE f32 division
-  if (h->solver == 3 && sw_fits(h)) return launch_lin_solve_sw(h, mode, x, x0, a, c_recip);
+  // the strip wavefront's bulk copies read x, x0 and the codes from 16-byte
+  // aligned rows (a handle's fields and codes always are)
+  const bool aligned16 = (((uintptr_t)x | (uintptr_t)x0 | (uintptr_t)h->code) & 15u) == 0;
+  if (h->solver == 3 && aligned16 && sw_fits(h))
+    return launch_lin_solve_sw(h, mode, x, x0, a, c_recip);
   if (h->solver != 1) {
     // The staged cluster form is the fastest kernel where it applies. The
     // streamed one is slower alone than the multi-block wavefront but holds
@@ -733,7 +743,10 @@ int launch_step(eq_fluid* h, float* tape = nullptr) {
     h->cur_slot = slot;
   };
   // the critical path's solve first, then the side solves
-  if ((rc = launch_diffuse(h, eqk::kRow, vx0, vx, h->visc))) return rc;
+  h->sw_shared = sideVy || sideDe;
+  rc = launch_diffuse(h, eqk::kRow, vx0, vx, h->visc);
+  h->sw_shared = false;
+  if (rc) return rc;
   if (sideVy) {
     EQ_CUDA(cudaStreamWaitEvent(h->side[0], h->fork_ev, 0));
     on(h->side[0], 1);

@@ -32,19 +32,21 @@
 //
 // Steps. Inside a warp's fast range (every grid row of the warp an interior
 // row at 2 <= i <= N) a step is the update and one post store; the general
-// rules (frame columns, boundary codes, the lane-0 fix) run only on the steps
-// that need them, decided by one warp vote.
+// rules (frame columns, boundary codes, the lane-0 fix) run only in the
+// periods that need them, decided by one warp vote per period, so that a
+// fast period is straight-line code.
 //
 // Block-to-block values, as 64-bit words (value | tag << 32) polled with
-// relaxed loads issued two periods ahead and copied into shared memory:
+// relaxed loads issued kSwAHI periods ahead and copied into shared memory:
 // * halo: lanes 30 and 31 of sweep warp k export per diagonal
 //   [post30, -, uval31, post31] for strip b+1's sweep warp k (its ring
-//   positions -2, -1 and lane-0 U ring). Lane 31 cannot finish a post value
-//   that needs the next strip's row (AdjustColumn, wall below); strip b+1's
-//   lane 0 overwrites it in its ring.
+//   positions -2, -1 and lane-0 U ring), imported by that warp at the start
+//   of the period that reads them. Lane 31 cannot finish a post value that
+//   needs the next strip's row (AdjustColumn, wall below); strip b+1's lane 0
+//   overwrites it in its ring.
 // * group: the last sweep warp of group g exports its post ring row per
 //   diagonal (positions -2 .. 31) for group g+1's first sweep, read by an
-//   import warp.
+//   import warp one period ahead.
 // The tag is the launch's epoch (a device word the last block advances), so
 // a captured graph replays without clearing anything.
 //
@@ -74,7 +76,8 @@ constexpr int kSwPX = 32;     // columns of the initial-x ring
 // Row strides of those rings, padded so that the copy warp's per-row chunk
 // writes (one row per lane) fall in different banks; the sweep warps' reads
 // (row + lane, column - lane) stay conflict-free.
-constexpr int kSwPCS = kSwPC + 4;  // x0 ring row (floats) and code ring row (bytes)
+constexpr int kSwPCS = kSwPC + 4;  // x0 ring row (floats)
+constexpr int kSwCCS = kSwPC + 4;  // code ring row (bytes)
 constexpr int kSwPXS = kSwPX + 4;  // initial-x ring row (floats)
 constexpr int kSwAH = 5;      // a chunk copy is issued kSwAH periods before its use
 constexpr int kSwAHI = 4;     // an import load is checked kSwAHI periods after its issue
@@ -112,8 +115,8 @@ __host__ __device__ inline LsSwLayout ls_sw_layout(int KG, int S) {
   L.ui = L.vr + (size_t)KG * kSwRD * kSwRW * 4;     // KG RD floats
   L.vp = L.ui + (size_t)KG * kSwRD * 4;             // RD RW floats
   L.x0r = (L.vp + (size_t)kSwRD * kSwRW * 4 + 15) / 16 * 16;  // nrw PC floats
-  L.cr = L.x0r + nrw * kSwPCS * 4;                 // nrw PCS bytes
-  L.xr = (L.cr + nrw * kSwPCS + 15) / 16 * 16;     // 33 PXS floats
+  L.cr = L.x0r + nrw * kSwPCS * 4;                 // nrw CCS bytes
+  L.xr = (L.cr + nrw * kSwCCS + 15) / 16 * 16;     // 33 PXS floats
   L.xt = L.xr + 33 * kSwPXS * 4;                   // S floats: frame row 0
   L.xb = L.xt + (size_t)S * 4;                     // S floats: frame row S-1
   L.cf = L.xb + (size_t)S * 4;                     // S bytes: column has fluid
@@ -132,16 +135,17 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
   return v;
 }
 // Exports: each 64-bit element is one single-copy-atomic word (value | tag).
+// A word validates itself by its tag, so no export is ordered against any
+// other memory access: no memory clobber, and the compiler may schedule the
+// steps' shared-memory traffic across it.
 __device__ __forceinline__ void sw_st1(unsigned long long* p, float v, unsigned tag) {
   asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p),
-               "l"((unsigned long long)__float_as_uint(v) | ((unsigned long long)tag << 32))
-               : "memory");
+               "l"((unsigned long long)__float_as_uint(v) | ((unsigned long long)tag << 32)));
 }
 __device__ __forceinline__ void sw_st2(unsigned long long* p, float v0, float v1, unsigned tag) {
   asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p),
                "l"((unsigned long long)__float_as_uint(v0) | ((unsigned long long)tag << 32)),
-               "l"((unsigned long long)__float_as_uint(v1) | ((unsigned long long)tag << 32))
-               : "memory");
+               "l"((unsigned long long)__float_as_uint(v1) | ((unsigned long long)tag << 32)));
 }
 
 // The Gauss-Seidel update; the FMA build contracts x0 + a*sum.
@@ -187,10 +191,11 @@ struct SwWarp {
 // d % kSwRD holds diagonal d - 1, so a period's slots are consecutive.
 struct SwOps {
   float R, D, Ui, X0, xf;
+  float g01;  // group exporter, lanes 0 and 1: this ring's position -1 / -2
   unsigned cd, cf;
 };
 
-template <int MODE, bool FIRSTX, bool FRAME>
+template <int MODE, bool FIRSTX, bool FRAME, bool GEXP = false>
 __device__ __forceinline__ SwOps sw_load(const SwWarp& w, int dp, int q) {
   const int lane = w.lane;
   const int d = dp + q;
@@ -215,6 +220,10 @@ __device__ __forceinline__ SwOps sw_load(const SwWarp& w, int dp, int q) {
     o.xf = w.xf[ic];
     if (MODE == kPassive) o.cf = w.cf[ic];
   }
+  // ring positions -2 and -1 hold the imported halo values (written before
+  // the period's barrier); a lane-0 fix of this step overwrites position -1
+  // later, and the export takes that value from the step itself
+  o.g01 = GEXP ? w.own[slot * kSwRW + (1 - (lane & 1))] : 0.0f;
   return o;
 }
 
@@ -316,14 +325,85 @@ __device__ __forceinline__ void sw_compute(SwWarp& w, int dp, int q, const SwOps
   if (FRAME) w.cfprev = o.cf;
 }
 
-// A fast period: every operand loaded first, then the kSwQ steps.
-template <int MODE, bool FIRSTX, bool FRAME>
+// A step of a fast period: the update, the post store and the exports, with
+// no warp vote and no branch, so that the compiler schedules a period's kSwQ
+// steps as one straight-line block. Gives the bits of sw_compute<MODE, true,
+// FRAME> whose vote came out false. GEXP: the warp is its group's exporter.
+template <int MODE, bool FRAME, bool GEXP>
+__device__ __forceinline__ void sw_step_fast(SwWarp& w, int dp, int q, const SwOps& o) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = w.lane;
+  const int d = dp + q;
+  const int i = d - lane;
+  const int slot = (dp & (kSwRD - 1)) + q;
+  const int N = w.N;
+  float U = __shfl_up_sync(FULL, w.vcur, 1);
+  U = lane == 0 ? o.Ui : U;
+  const float gs = gs_update(o.X0, w.a, fadd(fadd(fadd(o.R, w.vcur), o.D), U), w.cr);
+  // a lane-0 fix outside the interior (a frame row's lane 0 does not vote)
+  const bool fix = MODE == kCol && lane == 0 && (o.cd & kCodeAboveDown) != 0 &&
+                   (w.interior || w.bot) && (unsigned)(i - 1) < (unsigned)N;
+  float vnew = gs, post = w.vcur;
+  if (FRAME) {  // frame-row lanes: the frame cell as the sweep sees it
+    const bool fl = w.top || w.bot;
+    const float vf = (MODE == kPassive && w.top && w.k > 0 && o.cf) ? o.D : o.xf;
+    vnew = fl ? vf : vnew;
+    if (MODE == kPassive) {
+      const float vdown = __shfl_down_sync(FULL, vnew, 1);
+      const bool pc = fl && (unsigned)(i - 2) < (unsigned)N && w.cfprev != 0u;
+      post = pc ? (w.top ? vdown : w.uprev) : post;
+    }
+  }
+  float* const wrow = w.own + slot * kSwRW;
+  wrow[lane + 2] = post;
+  if (MODE == kCol && fix) wrow[1] = -vnew;
+  // lanes 30, 31: halo record d-1 = [post30, -, uval31, post31] (d >= 2 here)
+  if (w.edgeOut) sw_st2(w.edgeOut + (size_t)(d - 1) * 4, lane == 31 ? w.vcur : post, post, w.tag);
+  if (GEXP) {  // group record d: word p + 2 = position p of diagonal d-1
+    unsigned long long* const rec = w.gexpOut + (size_t)d * kSwGrpWords;
+    sw_st1(rec + lane + 2, post, w.tag);
+    if (lane < 2) sw_st1(rec + (1 - lane), (MODE == kCol && fix) ? -vnew : o.g01, w.tag);
+  }
+  if (w.xlast && w.interior) w.xlast[d] = vnew;  // 1 <= i - 1 < N in the fast range
+  w.vprev = w.vcur;
+  w.vcur = vnew;
+  w.uprev = U;
+  w.cprev = o.cd;
+  if (FRAME) w.cfprev = o.cf;
+}
+
+// A period of a warp's fast range: every operand loaded first; one warp vote
+// on the codes of all kSwQ steps (a boundary action of the previous cell, a
+// lane-0 fix) sends the whole period through the general rules, which give
+// the fast steps' bits wherever those apply.
+template <int MODE, bool FIRSTX, bool FRAME, bool GEXP>
 __device__ __forceinline__ void sw_period_fast(SwWarp& w, int dp) {
+  const unsigned FULL = 0xffffffffu;
   SwOps o[kSwQ];
 #pragma unroll
-  for (int q = 0; q < kSwQ; ++q) o[q] = sw_load<MODE, FIRSTX, FRAME>(w, dp, q);
+  for (int q = 0; q < kSwQ; ++q) o[q] = sw_load<MODE, FIRSTX, FRAME, GEXP>(w, dp, q);
+  bool general = false;
+  if (MODE != kPassive) {
+    const unsigned actMask =
+        MODE == kRow ? (unsigned)(kCodeRowLeft | kCodeRowRight) : (unsigned)(kCodeColUp | kCodeColDown);
+    unsigned prevCodes = w.cprev;  // the previous cell's code of every step
 #pragma unroll
-  for (int q = 0; q < kSwQ; ++q) sw_compute<MODE, true, FRAME>(w, dp, q, o[q]);
+    for (int q = 0; q + 1 < kSwQ; ++q) prevCodes |= o[q].cd;
+    bool need = (prevCodes & actMask) != 0u;
+    if (MODE == kCol && w.lane == 0) {
+#pragma unroll
+      for (int q = 0; q < kSwQ; ++q)
+        need |= (o[q].cd & kCodeAboveDown) != 0 && (unsigned)(dp + q - 1) < (unsigned)w.N;
+    }
+    general = __any_sync(FULL, w.interior && need);
+  }
+  if (general) {
+#pragma unroll
+    for (int q = 0; q < kSwQ; ++q) sw_compute<MODE, false, FRAME>(w, dp, q, o[q]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < kSwQ; ++q) sw_step_fast<MODE, FRAME, GEXP>(w, dp, q, o[q]);
+  }
 }
 
 template <int MODE>
@@ -395,7 +475,7 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
         if (n < 0 || 4 * n >= P) continue;
         const int sc = (4 * n) & (kSwPC - 1);
         cp_async16(&X0R[q * kSwPCS + sc], A.x0 + (size_t)r * P + 4 * n, true);
-        cp_async4(&CR[q * kSwPCS + sc], A.code + (size_t)r * P + 4 * n, true);
+        cp_async4(&CR[q * kSwCCS + sc], A.code + (size_t)r * P + 4 * n, true);
       }
       if (g == 0) {
         for (int q = lane; q < 33; q += 32) {
@@ -532,7 +612,7 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
     W.ui = UI + (size_t)kr * kSwRD;
     const int rrow = 2 * (nk - 1 - kr) + lane;
     W.x0row = X0R + (real ? rrow : 0) * kSwPCS;
-    W.crow = CR + (real ? rrow : 0) * kSwPCS;
+    W.crow = CR + (real ? rrow : 0) * kSwCCS;
     W.xrl = XR + lane * kSwPXS;
     W.xrd = XR + (lane + 1) * kSwPXS;
     W.xt = XT;
@@ -576,15 +656,15 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
       const bool need = imp_ok(u);
       bool bad = need && (unsigned)(w >> 32) != tag;
       long long tries = 0;
-      unsigned ns = 32;
+      unsigned ns = 0;  // re-poll at once (the warp waits on the load), then back off
       while (__any_sync(FULL, bad)) {
         if (++tries > A.spin_limit) {
           if (lane == 0) atomicExch(A.err, 3 /* EQ_ERR_TIMEOUT */);
           return false;
         }
         if ((tries & 63) == 0 && __any_sync(FULL, ld_relaxed_i32(A.err) != 0)) return false;
-        __nanosleep(ns);
-        ns = ns < 256 ? ns * 2 : 256;
+        if (ns) __nanosleep(ns);
+        ns = tries < 4 ? 0u : (ns < 32 ? 32u : (ns < 256 ? ns * 2 : 256u));
         if (bad) {
           w = ld_relaxed_u64(edgeIn + (size_t)(imp_dd(u) + 32) * 4 + iw);
           bad = (unsigned)(w >> 32) != tag;
@@ -600,37 +680,48 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
       }
       return true;
     };
-    unsigned long long hv[kSwAHI];  // hv[q]: the words of use period cp + 1 + q
-    bool ok0 = imp_store(0, imp_load(0));  // the prologue: imports of period 0
+    // The halo words of period cp are imported at its start: lane 0's U ring
+    // is read by this warp only (after a __syncwarp), ring positions -2 and -1
+    // by the next sweep's warp one barrier later.
+    bool ok0 = true;
     // start only once strip b-1 is A.slack periods ahead, so that the loads
     // issued kSwAHI periods early find their words written
-    if (ok0 && impOn) {
-      const int us = min(1 + A.slack, (S - 1 + kSwLg * kk) / kSwQ);
-      if (us >= 1) ok0 = imp_store(us, imp_load(us), false);
+    if (impOn && A.slack > 0) {
+      const int us = min(A.slack, (S - 1 + kSwLg * kk) / kSwQ);
+      ok0 = imp_store(us, imp_load(us), false);
     }
+    unsigned long long hv[kSwAHI];  // hv[q]: the words of use period cp + q
 #pragma unroll
-    for (int q = 0; q < kSwAHI; ++q) hv[q] = imp_load(1 + q);
+    for (int q = 0; q < kSwAHI; ++q) hv[q] = imp_load(q);
     if (!ok0) s_abort[1] = 1;  // the prologue counts as period -1
     __syncthreads();
     if (!s_abort[1]) {
       for (int cp = 0; cp < NP; ++cp) {
-        const bool fine = imp_store(cp + 1, hv[0]);
+        const bool fine = imp_store(cp, hv[0]);
         if (!fine) s_abort[cp & 1] = 1;
 #pragma unroll
         for (int q = 0; q + 1 < kSwAHI; ++q) hv[q] = hv[q + 1];
-        hv[kSwAHI - 1] = imp_load(cp + 1 + kSwAHI);
+        hv[kSwAHI - 1] = imp_load(cp + kSwAHI);
+        __syncwarp();
         if (runs && fine) {
           const int dp = cp * kSwQ - kSwLg * kk;
           if (dp >= dF0 && dp + kSwQ - 1 <= dF1) {
-            if (firstX) {
-              if (hasFrame)
-                sw_period_fast<MODE, true, true>(W, dp);
+            if (exportGroup) {
+              if (firstX)
+                sw_period_fast<MODE, true, true, true>(W, dp);
+              else if (hasFrame)
+                sw_period_fast<MODE, false, true, true>(W, dp);
               else
-                sw_period_fast<MODE, true, false>(W, dp);
+                sw_period_fast<MODE, false, false, true>(W, dp);
+            } else if (firstX) {
+              if (hasFrame)
+                sw_period_fast<MODE, true, true, false>(W, dp);
+              else
+                sw_period_fast<MODE, true, false, false>(W, dp);
             } else if (hasFrame) {
-              sw_period_fast<MODE, false, true>(W, dp);
+              sw_period_fast<MODE, false, true, false>(W, dp);
             } else {
-              sw_period_fast<MODE, false, false>(W, dp);
+              sw_period_fast<MODE, false, false, false>(W, dp);
             }
           } else {
             for (int q = 0; q < kSwQ; ++q) {

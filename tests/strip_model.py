@@ -23,7 +23,8 @@ class Cfg:
     RW = 36   # floats per ring row (positions -2 .. 33)
     PC = 128  # columns of the x0 / code rings
     PX = 32   # columns of the initial-x ring
-    AH = 5    # a chunk copy is issued AH periods before its use period
+    CH = 4    # columns per chunk copy
+    AH = 5    # a row's chunk is issued AH periods before its first use period
 
 
 def derive_codes(cells, S):
@@ -90,7 +91,7 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
     """One launch over K sweeps in G sweep groups: x with the last sweep's raw
     interior values (the caller then applies set_boundaries), and the number
     of (warp, step)s and of those on the fast path."""
-    Q, LG, RD, PC, PX, AH = cfg.Q, cfg.LG, cfg.RD, cfg.PC, cfg.PX, cfg.AH
+    Q, LG, RD, PC, PX, AH, CH = cfg.Q, cfg.LG, cfg.RD, cfg.PC, cfg.PX, cfg.AH, cfg.CH
     N = S - 2
     a = F(a)
     cr = F(F(1.0) / F(c))
@@ -129,19 +130,28 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
             CR = Tracked((nrw, PC), np.uint8)
             XR = Tracked((33, PX), np.float32)
 
+            def chunk_of(n, first):
+                # row's 4-column chunk n is first read in the use period; a
+                # CH-column copy goes out when n is a multiple of CH / 4 (and
+                # in the first period, the copy under way)
+                if n < 0 or 4 * n >= P:
+                    return -1
+                return n // (CH // 4) if n % (CH // 4) == 0 or first else -1
+
             def load_chunks(cp):
                 u = cp + AH
+                first = cp == -AH - 1
                 for q in range(nrw):
                     r = rA + q
                     if r < 0 or r > S - 1:
                         continue
                     dr = jb - r
                     kmin = (dr + 1) >> 1 if dr > 0 else 0
-                    n = u + ((dr - (LG + 2) * kmin + 3) >> 2)
-                    if n < 0 or 4 * n >= P:
+                    m = chunk_of(u + ((dr - (LG + 2) * kmin + 3) >> 2), first)
+                    if m < 0:
                         continue
-                    for e in range(4):
-                        col = 4 * n + e
+                    for e in range(CH):
+                        col = CH * m + e
                         X0R.write((q, col % PC), x0g[r, col] if col < S else F(0),
                                   ("x0", r, col), u)
                         CR.write((q, col % PC), code[r, col] if col < S else 0,
@@ -151,19 +161,22 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                         r = jb + q
                         if r > S - 1:
                             continue
-                        n = u + 1 - ((q + 3) >> 2)
-                        if n < 0 or 4 * n >= P:
+                        m = chunk_of(u + 1 - ((q + 3) >> 2), first)
+                        if m < 0:
                             continue
-                        for e in range(4):
-                            col = 4 * n + e
+                        for e in range(CH):
+                            col = CH * m + e
                             XR.write((q, col % PX), xin[r, col] if col < S else F(0),
                                      ("x", r, col), u)
 
             def halo_import(kk, cp):
+                # the halo words of period cp, at its start: the U ring is read
+                # by the same warp in this period (after a __syncwarp), ring
+                # positions -2 / -1 by the next sweep's warp after the barrier
                 k = kF + kk
                 if b == 0 or not act(b - 1, k):
                     return
-                lo = (cp + 1) * Q - LG * kk - 1
+                lo = cp * Q - LG * kk - 1
                 for dd in range(lo, lo + Q):
                     if dd < -1 or dd > S - 2:
                         continue
@@ -171,7 +184,7 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                     assert (etag[b - 1, k, rec, [0, 2, 3]] == TAG).all(), ("halo", b, k, rec)
                     s = (dd + 1) % RD  # diagonal dd lives in slot dd + 1
                     VR.write((kk, s, 0), edge[b - 1, k, rec, 0], ("vr", k, dd, -2), cp + 1)
-                    UI.write((kk, s), edge[b - 1, k, rec, 2], ("ui", k, dd), cp + 1)
+                    UI.write((kk, s), edge[b - 1, k, rec, 2], ("ui", k, dd), cp)
                     VR.write((kk, s, 1), edge[b - 1, k, rec, 3], ("vr", k, dd, -1), cp + 1)
 
             def group_import(cp):
@@ -187,8 +200,6 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
 
             for cp in range(-AH - 1, 0):
                 load_chunks(cp)
-            for kk in range(nk):
-                halo_import(kk, -1)
             group_import(-1)
             vcur = np.zeros((nk, 32), np.float32)
             vprev = np.zeros((nk, 32), np.float32)

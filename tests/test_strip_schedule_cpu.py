@@ -33,11 +33,28 @@ def _case(S, K, mode, seed, G):
 
 
 # sizes from the smallest grid to several strips, sweep counts that leave the
-# last group short, groups from one to five sweeps each
+# last group short, groups from one to ten sweeps each (ten: the widest spread
+# of a row's readers over the x0 / code rings)
 @pytest.mark.parametrize("S,K,G", [(20, 1, 1), (20, 3, 2), (37, 5, 3), (40, 4, 4),
-                                   (66, 6, 2), (45, 9, 3), (70, 20, 5)])
+                                   (66, 6, 2), (45, 9, 3), (70, 20, 5), (70, 20, 2),
+                                   (150, 10, 1)])
 @pytest.mark.parametrize("mode", [M.ROW, M.COL, M.PAS])
 def test_strip_model_matches_oracle(S, K, G, mode):
     diff, steps, fast = _case(S, K, mode, S + K + mode, G)
     assert diff == 0
     assert steps > 0
+
+
+def test_strip_model_catches_a_small_ring():
+    """The model's slot keys catch a ring too narrow for the chunk schedule:
+    a 16-column initial-x ring is overwritten by the chunks issued kSwAH
+    periods ahead before its last read."""
+    class Narrow(M.Cfg):
+        PX = 16
+    rng = np.random.default_rng(0)
+    S, K = 70, 6
+    cells = np.zeros((S, S), np.uint8)
+    cells[0, :] = cells[-1, :] = cells[:, 0] = cells[:, -1] = 1
+    x = rng.uniform(-1, 1, S * S).astype(np.float32)
+    with pytest.raises(AssertionError, match="XR"):
+        M.run(M.ROW, x, x.copy(), cells.reshape(-1), S, 96, K, 0.5, 3.0, G=1, cfg=Narrow)
