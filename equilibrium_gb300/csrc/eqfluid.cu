@@ -523,7 +523,7 @@ int launch_lin_solve_sw(eq_fluid* h, int mode, float* x, const float* x0, float 
     A.a = a;
     A.cr = c_recip;
     const size_t smem = eqk::ls_sw_layout(KG, S).total;
-    const dim3 grid((unsigned)(A.B * G)), block(32u * (unsigned)(KG + 2));
+    const dim3 grid((unsigned)(A.B * G)), block(32u * (unsigned)(KG + 3));
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     if (h->profiling) {
       EQ_CUDA(cudaEventCreate(&ev0));
@@ -560,14 +560,16 @@ int launch_lin_solve(eq_fluid* h, int mode, float* x, const float* x0, float a, 
   // the strip wavefront's bulk copies read x, x0 and the codes from 16-byte
   // aligned rows (a handle's fields and codes always are)
   const bool aligned16 = (((uintptr_t)x | (uintptr_t)x0 | (uintptr_t)h->code) & 15u) == 0;
-  if (h->solver == 3 && aligned16 && sw_fits(h))
+  // The strip wavefront is the fastest kernel at every measured size (N = 128
+  // to 1024, alone and in step()); it runs wherever its shared memory fits.
+  if ((h->solver == 0 || h->solver == 3) && aligned16 && sw_fits(h))
     return launch_lin_solve_sw(h, mode, x, x0, a, c_recip);
   if (h->solver != 1) {
-    // The staged cluster form is the fastest kernel where it applies. The
-    // streamed one is slower alone than the multi-block wavefront but holds
-    // only C SMs, so by default it takes the side-stream solves of step()
-    // (beside the multi-block solve of the critical path); solver 2 uses it
-    // for every solve.
+    // Otherwise (and with solver 4): the staged cluster form where it
+    // applies. The streamed one is slower alone than the multi-block
+    // wavefront but holds only C SMs, so it takes the side-stream solves of
+    // step() (beside the multi-block solve of the critical path); solver 2
+    // uses it for every solve.
     const int C = cluster_blocks(h, K);
     if (C > 0 && (h->cl_kind == 1 || h->cur_slot != 0 || h->solver == 2))
       return launch_lin_solve_cluster(h, mode, x, x0, a, c_recip, C);
@@ -1412,7 +1414,7 @@ int eq_fluid_set_concurrency(eq_fluid* h, int mask) {
 
 int eq_fluid_set_solver(eq_fluid* h, int solver) {
   if (!h) return fail(EQ_ERR_ARG, "null handle");
-  if (solver < 0 || solver > 3) return fail(EQ_ERR_ARG, "solver must be 0, 1, 2 or 3");
+  if (solver < 0 || solver > 4) return fail(EQ_ERR_ARG, "solver must be 0..4");
   h->solver = solver;
   return EQ_OK;
 }

@@ -406,13 +406,34 @@ __device__ __forceinline__ void sw_period_fast(SwWarp& w, int dp) {
   }
 }
 
+// Warps of a block: kSwMaxKG sweep warps at most, the copy warp, the group
+// import warp and the halo import warp.
+constexpr int kSwThreads = 32 * (kSwMaxKG + 3);
+static_assert(12 * kSwMaxKG <= 128, "the halo import warp holds 4 words a lane per period");
+
+// The role of warp w of a block with KG sweep warps (nk of them real): sweep
+// kk < KG, or KG (copy), KG + 1 (group import), KG + 2 (halo import). Warp w
+// issues from SM sub-partition w % 4, so the helpers take warps h, h+1, h+2
+// (h = min(4, KG)) and the two heaviest sweeps, the first (it reads the
+// initial x or the group import ring) and the last (group export or x), take
+// warps 0 and 1: each shares its sub-partition with a helper.
+__device__ __forceinline__ int sw_role(int w, int KG, int nk) {
+  const int h = KG < 4 ? KG : 4;
+  if (w >= h && w < h + 3) return KG + (w - h);
+  const int slot = w < h ? w : w - 3;  // sweep slots in warp order
+  if (slot == 0 || nk < 2) return slot;
+  if (slot == 1) return nk - 1;
+  return slot <= nk - 1 ? slot - 1 : slot;
+}
+
 template <int MODE>
-__global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
+__global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
   extern __shared__ __align__(16) unsigned char ls_sw_smem[];
-  // abort flags by period parity: set during period cp in s_abort[cp & 1] and
-  // read by every thread after that period's barrier (nobody writes that slot
-  // again before the next barrier), so all warps leave at the same barrier
-  __shared__ int s_t, s_abort[2];
+  // A warp that gives up a wait (timeout) raises its vote at the period's
+  // barrier (__syncthreads_or), and every warp leaves at that barrier. The
+  // vote needs no shared-memory flag: a warp with global loads in flight
+  // would wait for them before any shared-memory load returns.
+  __shared__ int s_t;
   __shared__ unsigned s_tag;
   const unsigned FULL = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -420,7 +441,6 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
   if (threadIdx.x == 0) {
     s_t = (int)atomicAdd(&A.ctr[0], 1u);
     s_tag = ld_relaxed_u32(&A.ctr[2]) + 1u;
-    s_abort[0] = s_abort[1] = 0;
   }
   __syncthreads();
   const int t = s_t;
@@ -440,6 +460,7 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
     const int j0 = 32 * b - 2 * k;
     return j0 <= S - 1 && j0 + 31 >= 0;
   };
+  const int role = sw_role(warp, KG, nk);
   const LsSwLayout lay = ls_sw_layout(KG, S);
   float* const VR = reinterpret_cast<float*>(ls_sw_smem + lay.vr);
   float* const UI = reinterpret_cast<float*>(ls_sw_smem + lay.ui);
@@ -461,7 +482,7 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
   const unsigned long long* const gexpIn =
       g > 0 ? A.gexp + ((size_t)b * (G - 1) + (g - 1)) * (A.RE + 1) * kSwGrpWords : nullptr;
 
-  if (warp == KG) {
+  if (role == KG) {
     // ---- the copy warp: x0 / code rows and the first group's initial-x rows
     auto issue = [&](int cp) {
       const int u = cp + kSwAH;  // use period
@@ -491,17 +512,15 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
     };
     for (int cp = -kSwAH - 1; cp < 0; ++cp) issue(cp);
     cp_async_wait<kSwAH - 1>();  // use periods -1 and 0 have landed
-    __syncthreads();
-    if (!s_abort[1]) {
+    if (!__syncthreads_or(0)) {
       for (int cp = 0; cp < NP; ++cp) {
         issue(cp);
         cp_async_wait<kSwAH - 1>();  // use period cp + 1 has landed
-        __syncthreads();
-        if (s_abort[cp & 1]) break;
+        if (__syncthreads_or(0)) break;
       }
     }
     cp_async_wait<0>();
-  } else if (warp == KG + 1) {
+  } else if (role == KG + 1) {
     // ---- the group import warp: the previous group's last sweep, per period
     // 4 records x 34 words (positions -2 .. 31) of the diagonals d - 1 the
     // first sweep reads in that period; slot s of lane l is word l + 32 s
@@ -569,23 +588,109 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
     }
 #pragma unroll
     for (int q = 0; q < kSwAHI; ++q) load(1 + q, wv[q]);
-    if (!ok0) s_abort[1] = 1;
-    __syncthreads();
-    if (!s_abort[1]) {
+    if (!__syncthreads_or(!ok0)) {  // the prologue counts as period -1
       for (int cp = 0; cp < NP; ++cp) {
-        if (!settle(cp + 1, wv[0], true)) s_abort[cp & 1] = 1;
+        const bool bad = !settle(cp + 1, wv[0], true);
 #pragma unroll
         for (int q = 0; q + 1 < kSwAHI; ++q)
 #pragma unroll
           for (int s = 0; s < 5; ++s) wv[q][s] = wv[q + 1][s];
         load(cp + 1 + kSwAHI, wv[kSwAHI - 1]);
-        __syncthreads();
-        if (s_abort[cp & 1]) break;
+        if (__syncthreads_or(bad)) break;
+      }
+    }
+  } else if (role == KG + 2) {
+    // ---- the halo import warp: strip b-1's exports for every sweep warp of
+    // the block, copied into its rings one period before their use (lane 0's
+    // U ring, ring positions -2 and -1). Word w = lane + 32 s of a period is
+    // word {0, 2, 3}[t % 3] of record t / 3 (t = w % 12) for sweep w / 12.
+    bool hon[4];
+    int hdd0[4], hslot0[4], hstr[4];
+    const unsigned long long* hin[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const int w = lane + 32 * s, kk = w / 12, tt = w - 12 * (w / 12);
+      const int k = kF + kk;
+      const int jp = 32 * (b - 1) - 2 * k;  // strip b-1's rows of sweep k (the producer)
+      hon[s] = w < 12 * nk && b > 0 && jp <= S - 1 && jp + 31 >= 0;
+      const int iwi = tt - 3 * (tt / 3), iw = iwi == 0 ? 0 : iwi + 1;
+      hdd0[s] = -kSwLg * kk - 1 + tt / 3;  // diagonal of period u: u kSwQ + hdd0
+      // U ring slot base (word 2) or ring position -2 / -1 (words 0 / 3)
+      hslot0[s] = iw == 2 ? (int)(lay.ui / 4) + kk * kSwRD
+                          : (int)(lay.vr / 4) + kk * kSwRD * kSwRW + (iw == 0 ? 0 : 1);
+      hstr[s] = iw == 2 ? 1 : kSwRW;
+      hin[s] = hon[s] ? A.edge + ((size_t)(b - 1) * K + k) * A.RE * 4 + iw : nullptr;
+    }
+    auto ok_of = [&](int u, int s) {
+      const int dd = u * kSwQ + hdd0[s];
+      return hon[s] && dd >= -1 && dd <= S - 2;
+    };
+    auto addr_of = [&](int u, int s) { return hin[s] + (size_t)(u * kSwQ + hdd0[s] + 32) * 4; };
+    auto load = [&](int u, unsigned long long* v) {
+#pragma unroll
+      for (int s = 0; s < 4; ++s) v[s] = ok_of(u, s) ? ld_relaxed_u64(addr_of(u, s)) : 0ull;
+    };
+    float* const smf = reinterpret_cast<float*>(ls_sw_smem);
+    // spin until the words of use period u carry the launch's tag (bounded);
+    // with put, copy them into the rings (diagonal dd lives in slot dd + 1)
+    auto settle = [&](int u, unsigned long long* v, bool put) -> bool {
+      bool bad = false;
+#pragma unroll
+      for (int s = 0; s < 4; ++s) bad |= ok_of(u, s) && (unsigned)(v[s] >> 32) != tag;
+      long long tries = 0;
+      unsigned ns = 0;  // re-poll at once, then back off
+      while (__any_sync(FULL, bad)) {
+        if (++tries > A.spin_limit) {
+          if (lane == 0) atomicExch(A.err, 3 /* EQ_ERR_TIMEOUT */);
+          return false;
+        }
+        if ((tries & 63) == 0 && __any_sync(FULL, ld_relaxed_i32(A.err) != 0)) return false;
+        if (ns) __nanosleep(ns);
+        ns = tries < 4 ? 0u : (ns < 32 ? 32u : (ns < 256 ? ns * 2 : 256u));
+        bad = false;
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+          if (ok_of(u, s) && (unsigned)(v[s] >> 32) != tag) {
+            v[s] = ld_relaxed_u64(addr_of(u, s));
+            bad |= (unsigned)(v[s] >> 32) != tag;
+          }
+        }
+      }
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        if (put && ok_of(u, s)) {
+          const int slot = (u * kSwQ + hdd0[s] + 1) & (kSwRD - 1);
+          smf[hslot0[s] + slot * hstr[s]] = __uint_as_float((unsigned)(v[s] & 0xffffffffull));
+        }
+      }
+      return true;
+    };
+    unsigned long long hv[kSwAHI][4];  // hv[q]: the words of use period cp + 1 + q
+    load(0, hv[0]);
+    bool ok0 = settle(0, hv[0], true);  // the prologue: imports of period 0
+    // start only once strip b-1 is A.slack periods ahead, so that the loads
+    // issued kSwAHI periods early find their words written
+    if (ok0 && A.slack > 0) {
+      unsigned long long ws[4];
+      load(1 + A.slack, ws);
+      ok0 = settle(1 + A.slack, ws, false);
+    }
+#pragma unroll
+    for (int q = 0; q < kSwAHI; ++q) load(1 + q, hv[q]);
+    if (!__syncthreads_or(!ok0)) {  // the prologue counts as period -1
+      for (int cp = 0; cp < NP; ++cp) {
+        const bool bad = !settle(cp + 1, hv[0], true);
+#pragma unroll
+        for (int q = 0; q + 1 < kSwAHI; ++q)
+#pragma unroll
+          for (int s = 0; s < 4; ++s) hv[q][s] = hv[q + 1][s];
+        load(cp + 1 + kSwAHI, hv[kSwAHI - 1]);
+        if (__syncthreads_or(bad)) break;
       }
     }
   } else {
     // ---- sweep warp kk (k = kF + kk); warps past nk only meet the barriers
-    const int kk = warp, k = kF + kk;
+    const int kk = role, k = kF + kk;
     const bool real = kk < nk;
     const bool exportGroup = real && g < G - 1 && kk == nk - 1;
     const bool runs = real && (rows_active(k) || (exportGroup && rows_active(k + 1)));
@@ -632,78 +737,9 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
     // fast range: every interior lane at 2 <= i <= N
     const int lA = max(0, 1 - j0), lB = min(31, N - j0);
     const int dF0 = lA <= lB ? lB + 2 : 1 << 30, dF1 = lA <= lB ? lA + N : -(1 << 30);
-    // halo imports from strip b-1's sweep warp k: lane t < 12 holds word
-    // {0, 2, 3}[t % 3] of record t / 3 of each period
-    const int jp = 32 * (b - 1) - 2 * k;  // strip b-1's rows of sweep k (the producer)
-    const bool impOn = real && b > 0 && jp <= S - 1 && jp + 31 >= 0;
-    const int iq = lane / 3, iwi = lane - 3 * (lane / 3);
-    const int iw = iwi == 0 ? 0 : iwi + 1;
-    const unsigned long long* const edgeIn =
-        impOn ? A.edge + ((size_t)(b - 1) * K + k) * A.RE * 4 : nullptr;
-    auto imp_dd = [&](int u) { return u * kSwQ - kSwLg * kk - 1 + iq; };
-    auto imp_ok = [&](int u) {
-      const int dd = imp_dd(u);
-      return impOn && lane < 12 && dd >= -1 && dd <= S - 2;
-    };
-    auto imp_load = [&](int u) -> unsigned long long {
-      return imp_ok(u) ? ld_relaxed_u64(edgeIn + (size_t)(imp_dd(u) + 32) * 4 + iw) : 0ull;
-    };
-    float* const VRk = W.own;
-    float* const UIk = UI + (size_t)kr * kSwRD;
-    // spin until the words of use period u carry the launch's tag (bounded);
-    // with put, copy them into the rings
-    auto imp_store = [&](int u, unsigned long long w, bool put = true) -> bool {
-      const bool need = imp_ok(u);
-      bool bad = need && (unsigned)(w >> 32) != tag;
-      long long tries = 0;
-      unsigned ns = 0;  // re-poll at once (the warp waits on the load), then back off
-      while (__any_sync(FULL, bad)) {
-        if (++tries > A.spin_limit) {
-          if (lane == 0) atomicExch(A.err, 3 /* EQ_ERR_TIMEOUT */);
-          return false;
-        }
-        if ((tries & 63) == 0 && __any_sync(FULL, ld_relaxed_i32(A.err) != 0)) return false;
-        if (ns) __nanosleep(ns);
-        ns = tries < 4 ? 0u : (ns < 32 ? 32u : (ns < 256 ? ns * 2 : 256u));
-        if (bad) {
-          w = ld_relaxed_u64(edgeIn + (size_t)(imp_dd(u) + 32) * 4 + iw);
-          bad = (unsigned)(w >> 32) != tag;
-        }
-      }
-      if (put && need) {
-        const int s = (imp_dd(u) + 1) & (kSwRD - 1);  // diagonal dd lives in slot dd + 1
-        const float v = __uint_as_float((unsigned)(w & 0xffffffffull));
-        if (iw == 2)
-          UIk[s] = v;
-        else
-          VRk[s * kSwRW + (iw == 0 ? 0 : 1)] = v;
-      }
-      return true;
-    };
-    // The halo words of period cp are imported at its start: lane 0's U ring
-    // is read by this warp only (after a __syncwarp), ring positions -2 and -1
-    // by the next sweep's warp one barrier later.
-    bool ok0 = true;
-    // start only once strip b-1 is A.slack periods ahead, so that the loads
-    // issued kSwAHI periods early find their words written
-    if (impOn && A.slack > 0) {
-      const int us = min(A.slack, (S - 1 + kSwLg * kk) / kSwQ);
-      ok0 = imp_store(us, imp_load(us), false);
-    }
-    unsigned long long hv[kSwAHI];  // hv[q]: the words of use period cp + q
-#pragma unroll
-    for (int q = 0; q < kSwAHI; ++q) hv[q] = imp_load(q);
-    if (!ok0) s_abort[1] = 1;  // the prologue counts as period -1
-    __syncthreads();
-    if (!s_abort[1]) {
+    if (!__syncthreads_or(0)) {  // the prologue counts as period -1
       for (int cp = 0; cp < NP; ++cp) {
-        const bool fine = imp_store(cp, hv[0]);
-        if (!fine) s_abort[cp & 1] = 1;
-#pragma unroll
-        for (int q = 0; q + 1 < kSwAHI; ++q) hv[q] = hv[q + 1];
-        hv[kSwAHI - 1] = imp_load(cp + kSwAHI);
-        __syncwarp();
-        if (runs && fine) {
+        if (runs) {
           const int dp = cp * kSwQ - kSwLg * kk;
           if (dp >= dF0 && dp + kSwQ - 1 <= dF1) {
             if (exportGroup) {
@@ -734,8 +770,7 @@ __global__ void __launch_bounds__(32 * (kSwMaxKG + 2), 1) k_ls_sw(LsSwArgs A) {
             }
           }
         }
-        __syncthreads();
-        if (s_abort[cp & 1]) break;
+        if (__syncthreads_or(0)) break;
       }
     }
   }

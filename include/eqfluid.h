@@ -507,17 +507,20 @@ int eq_fluid_set_spin_limit(eq_fluid* h, int64_t iterations);
 #define EQ_CONC_DENSITY 2
 int eq_fluid_set_concurrency(eq_fluid* h, int mask);
 
-/* Which kernel runs lin_solve (all are bit-exact). The thread-block-cluster
- * wavefront applies for 32 < N <= 1024 (strips of up to 64 positions on at
- * most 16 blocks): with its strips staged in shared memory whole where they
- * fit (<= 32 sweeps, N up to ~320), else streamed through shared-memory
- * rings (<= 31 sweeps). 0 (default) = the staged cluster form where it
- * applies; the streamed form only for the solves step() runs on its side
- * streams (it holds few SMs, so it runs beside the critical path's solve);
- * else the multi-block wavefront. 1 = the multi-block wavefront always.
- * 2 = the cluster form (staged or streamed) wherever it applies.
- * 3 = the strip wavefront (one launch per 20 sweeps over 32-row strips and
- * groups of sweeps, blocks chained through tagged exports; any size).
+/* Which kernel runs lin_solve (all are bit-exact).
+ * 0 (default) = the strip wavefront (one launch per 20 sweeps over 32-row
+ *   strips and groups of sweeps, blocks chained through tagged exports)
+ *   wherever its shared memory fits (frame rows of S floats: N up to about
+ *   17000), else as 4.
+ * 1 = the multi-block wavefront always.
+ * 2 = the thread-block-cluster wavefront wherever it applies: 32 < N <= 1024
+ *   (strips of up to 64 positions on at most 16 blocks), with its strips
+ *   staged in shared memory whole where they fit (<= 32 sweeps, N up to
+ *   ~320), else streamed through shared-memory rings (<= 31 sweeps).
+ * 3 = the strip wavefront wherever it fits, else as 4.
+ * 4 = the staged cluster form where it applies; the streamed form only for
+ *   the solves step() runs on its side streams (it holds few SMs, so it
+ *   runs beside the critical path's solve); else the multi-block wavefront.
  * get_solver reports the blocks per cluster of the cluster form (0 = it
  * does not apply); get_cluster_form its form: 0 = none, 1 = strips staged
  * whole, 2 = strips streamed. */
@@ -528,10 +531,11 @@ int eq_fluid_get_cluster_form(eq_fluid* h, int* form);
  * by default 3 steps for N >= 192 and 2 below, the fastest measured; the
  * longest interval up to the cap that fits in shared memory is used). */
 int eq_fluid_set_cluster_interval(eq_fluid* h, int max_m);
-/* Sweep groups per strip of the strip wavefront (solver 3): each strip's
- * sweeps of one launch are split over `groups` blocks (1..5; 0 = by grid
- * size, about one block per SM; a block holds at most 10 sweeps, so 20
- * sweeps take at least 2 groups). */
+/* Sweep groups per strip of the strip wavefront: each strip's sweeps of one
+ * launch are split over `groups` blocks (1..5; a block holds at most 10
+ * sweeps, so 20 sweeps take at least 2 groups). 0 (default) = by grid size,
+ * about one block per SM, for a solve that runs alone; the fewest for the
+ * solves that step() runs side by side. */
 int eq_fluid_set_strip_groups(eq_fluid* h, int groups);
 /* Periods (of 4 wavefront steps) a strip-wavefront block waits, before its
  * first step, for the blocks it reads from to be ahead of it (0..64; 0 by

@@ -170,13 +170,12 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                                      ("x", r, col), u)
 
             def halo_import(kk, cp):
-                # the halo words of period cp, at its start: the U ring is read
-                # by the same warp in this period (after a __syncwarp), ring
-                # positions -2 / -1 by the next sweep's warp after the barrier
+                # the halo import warp: the words of use period cp + 1 (lane 0's
+                # U ring, ring positions -2 / -1), one barrier before their use
                 k = kF + kk
                 if b == 0 or not act(b - 1, k):
                     return
-                lo = cp * Q - LG * kk - 1
+                lo = (cp + 1) * Q - LG * kk - 1
                 for dd in range(lo, lo + Q):
                     if dd < -1 or dd > S - 2:
                         continue
@@ -184,7 +183,7 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                     assert (etag[b - 1, k, rec, [0, 2, 3]] == TAG).all(), ("halo", b, k, rec)
                     s = (dd + 1) % RD  # diagonal dd lives in slot dd + 1
                     VR.write((kk, s, 0), edge[b - 1, k, rec, 0], ("vr", k, dd, -2), cp + 1)
-                    UI.write((kk, s), edge[b - 1, k, rec, 2], ("ui", k, dd), cp)
+                    UI.write((kk, s), edge[b - 1, k, rec, 2], ("ui", k, dd), cp + 1)
                     VR.write((kk, s, 1), edge[b - 1, k, rec, 3], ("vr", k, dd, -1), cp + 1)
 
             def group_import(cp):
@@ -200,6 +199,8 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
 
             for cp in range(-AH - 1, 0):
                 load_chunks(cp)
+            for kk in range(nk):
+                halo_import(kk, -1)
             group_import(-1)
             vcur = np.zeros((nk, 32), np.float32)
             vprev = np.zeros((nk, 32), np.float32)

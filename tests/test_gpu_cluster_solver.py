@@ -45,6 +45,7 @@ def test_cluster_lin_solve_bitexact(eqlib, size, K, mode):
         _lib.check(L.eq_fluid_fill_obstacle(f.handle, *rc))
         r.fill_obstacle(*rc)
     assert blocks(f) >= 2, "the cluster form should apply at this size"
+    _lib.check(L.eq_fluid_set_solver(f.handle, 2))  # the cluster form (0 = the strip wavefront)
     rng = np.random.default_rng(size * 3 + K + mode)
     n = size * size
     x = rng.normal(size=n).astype(np.float32)
@@ -119,7 +120,7 @@ def test_streamed_cluster_lin_solve_bitexact(eqlib, size, K, nblocks, mode):
 def test_streamed_cluster_frames_match_oracle(eqlib):
     """Three frames with sources at N = 1024: the streamed form in every solve
     (three of them side by side in each step), then three more with the
-    default split (multi-block on the critical path, streamed on the side
+    split of solver 4 (multi-block on the critical path, streamed on the side
     streams)."""
     size, K = 1026, 20
     L = _lib.load()
@@ -134,7 +135,7 @@ def test_streamed_cluster_frames_match_oracle(eqlib):
     d = np.array([40.0, 10.0, 25.0], dtype=np.float32)
     u = np.array([3.0, -2.0, 0.5], dtype=np.float32)
     v = np.array([-1.0, 4.0, 2.5], dtype=np.float32)
-    for solver in (2, 0):
+    for solver in (2, 4):
         _lib.check(L.eq_fluid_set_solver(f.handle, solver))
         for _ in range(3):
             f.add_sources(xs, ys, d, u, v)

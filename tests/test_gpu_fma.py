@@ -51,7 +51,7 @@ def pair(fma, size, K, seed, dt=0.1, dv=1e-4, nrect=5, randomize=True):
     return f, r
 
 
-@pytest.mark.parametrize("solver", [0, 3])
+@pytest.mark.parametrize("solver", [0, 4])  # the strip wavefront, the cluster form
 @pytest.mark.parametrize("mode", [ROW, COL, PAS])
 def test_fma_lin_solve(fma, mode, solver):
     size, K = 130, 20

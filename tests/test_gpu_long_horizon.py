@@ -47,13 +47,15 @@ def _run(case, sources, solver, conc, label):
     f.close()
 
 
-@pytest.mark.parametrize("solver,conc", [(0, 3), (1, 0), (3, 3)])
+# solver 0: the strip wavefront; 4: the cluster / multi-block split; 1: the
+# multi-block wavefront
+@pytest.mark.parametrize("solver,conc", [(0, 3), (1, 0), (4, 3)])
 def test_n64_workload_100_frames(eqlib, solver, conc):
     size, iters, dt, dv, rect, xs, ys, d, u, v = small_workload(100)
     _run("n64", (xs, ys, d, u, v), solver, conc, f"N=64 solver {solver} conc {conc}")
 
 
-@pytest.mark.parametrize("solver,conc", [(0, 3), (3, 3), (3, 0)])
+@pytest.mark.parametrize("solver,conc", [(0, 3), (0, 0), (4, 3)])
 def test_n1024_workload_1000_frames(eqlib, solver, conc):
     import bench
     c = json.load(open(HASHES))["n1024"]

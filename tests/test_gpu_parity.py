@@ -133,7 +133,7 @@ def test_full_step_random_state(eqlib, layout, size, iters, frames):
 
 
 @pytest.mark.parametrize("mask", [0, 1, 2, 3])
-@pytest.mark.parametrize("solver", [0, 1])
+@pytest.mark.parametrize("solver", [0, 1, 4])
 @pytest.mark.parametrize("size", [66, 258])
 def test_full_step_concurrency_masks(eqlib, mask, solver, size):
     """step() with the vy and / or the density diffusion on side streams
