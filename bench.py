@@ -352,9 +352,10 @@ def _precision_reference(task):
     = the same step with both pressure solves converged; returns the density
     and velocities after each frame in err_frames."""
     import oracle
-    kind, size, err_frames = task
+    kind, size, err_frames, ndraw = task
     nmax = max(err_frames)
-    rects, sx, sy, sd, su, sv = precision_scene(size, nframes=nmax)
+    # the same draw as the GPU run's (the per-frame sources depend on its length)
+    rects, sx, sy, sd, su, sv = precision_scene(size, nframes=ndraw)
     r = oracle.OracleFluid(size, PREC_DT, ITERS, PREC_DIFF, PREC_VISC, dtype=np.float64)
     for rc in rects:
         r.fill_obstacle(*rc)
@@ -440,7 +441,7 @@ def run_precision_form(local_rank: int, frames: int, size: int = PREC_SIZE,
     if err_frames:
         t0 = time.perf_counter()
         pool = cf.ProcessPoolExecutor(2, mp_context=mp.get_context("spawn"))
-        futs = [pool.submit(_precision_reference, (kind, size, tuple(err_frames)))
+        futs = [pool.submit(_precision_reference, (kind, size, tuple(err_frames), total))
                 for kind in ("f64_reference", "f64_converged_pressure")]
         for f in futs:
             kind, snaps = f.result()
@@ -813,6 +814,104 @@ def run_diff_form(local_rank: int, reps: int = 2, fd_dirs: int = 32, size: int =
     return out
 
 
+def run_fma_form(local_rank: int, steps: int = 20, warmup: int = 5):
+    """The plain step of the headline workload built with FMA contraction
+    (libeqfluid_fma.so): device time per step as in the timed region (L2
+    flushed between steps), and its distance after one frame to the
+    bit-exact library's state from the same start (rel. L2 per field)."""
+    import torch
+    from equilibrium_gb300 import _lib
+    from equilibrium_gb300.simulation import Fluid, FluidConfigs, SimulationConfigs
+    F = _lib.load_fma()
+    L = _lib.load()
+    rects, sx, sy, sd, su, sv = scene(SEED, warmup + steps)
+    dev = torch.device("cuda", local_rank)
+
+    def make(lib):
+        f = Fluid(FluidConfigs(DIFF, VISC, False), SimulationConfigs(DT, ITERS, SIZE),
+                  device=local_rank, lib=lib)
+        for r in rects:
+            _lib.check(lib.eq_fluid_fill_obstacle(f.handle, *r), lib)
+        return f
+
+    f = make(F)
+    sp = ctypes.c_void_p()
+    _lib.check(F.eq_fluid_get_stream(f.handle, ctypes.byref(sp)), F)
+    stream = torch.cuda.ExternalStream(sp.value)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for q in range(warmup):
+        f.add_sources(sx[q], sy[q], sd[q], su[q], sv[q])
+        f.step()
+    f.synchronize()
+    ms = []
+    for q in range(warmup, warmup + steps):
+        f.add_sources(sx[q], sy[q], sd[q], su[q], sv[q])  # host sources staged before timing
+        with torch.cuda.stream(stream):
+            flush.fill_(float(q))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+        f.step()
+        b.record(stream)
+        f.synchronize()
+        ms.append(a.elapsed_time(b))
+    f.close()
+    # one frame from the same start in both builds
+    f, g = make(F), make(L)
+    for h in (f, g):
+        h.add_sources(sx[0], sy[0], sd[0], su[0], sv[0])
+        h.step()
+        h.synchronize()
+    errs = {}
+    for k, name in ((1, "density"), (2, "vx"), (3, "vy")):
+        x, y = f.read_field(k).astype(np.float64), g.read_field(k).astype(np.float64)
+        errs[name] = float(np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300))
+    f.close()
+    g.close()
+    step_ms = float(np.mean(ms))
+    return {"value": N * N / (step_ms / 1e3), "unit": "cell-steps/s", "ms_per_step": step_ms,
+            "build": "libeqfluid_fma.so: --fmad=true, x0 + a*sum and the advect / project "
+                     "arithmetic contracted (backtrace position unfused)",
+            "rel_l2_vs_bit_exact_frame_1": errs,
+            "tolerance": "1e-6 per phase (tests/test_gpu_fma.py)"}
+
+
+def solve_alone_ms(L, fl, reps: int = 10):
+    """One Passive lin_solve of the headline grid with nothing beside it (the
+    pressure solves' situation): the library's per-launch CUDA-event time."""
+    a = np.float32(1.0)
+    c = np.float32(4.0)
+    for _ in range(3):
+        _lib_check(L, L.eq_fluid_lin_solve(fl.handle, 2, 4, 5, a, c))
+    fl.synchronize()
+    _lib_check(L, L.eq_fluid_set_profiling(fl.handle, 1))
+    for _ in range(reps):
+        _lib_check(L, L.eq_fluid_lin_solve(fl.handle, 2, 4, 5, a, c))
+    fl.synchronize()
+    ms, n = ctypes.c_double(), ctypes.c_uint64()
+    _lib_check(L, L.eq_fluid_kernel_stats(fl.handle, 0, ctypes.byref(ms), ctypes.byref(n)))
+    _lib_check(L, L.eq_fluid_set_profiling(fl.handle, 0))
+    return ms.value / max(n.value, 1)
+
+
+def _lib_check(L, rc):
+    from equilibrium_gb300 import _lib
+    _lib.check(rc, L)
+
+
+def latency_bound_ms(sm_mhz: float, strips: int, groups: int, handoff_us: float = 1.5,
+                     op_cycles: int = 4):
+    """The lin_solve dependency-chain bound: 2 S + 3 K cell updates in sequence
+    (lexicographic Gauss-Seidel on the critical path), 6 dependent f32
+    operations each at op_cycles per operation, plus one L2 hand-off for each
+    block-to-block boundary on that path (strips - 1 strip edges, groups - 1
+    sweep-group edges; hand-offs inside a block go through shared memory)."""
+    chain_ms = (2 * SIZE + 3 * ITERS) * 6 * op_cycles / (sm_mhz * 1e3)
+    hand_ms = (strips - 1 + groups - 1) * handoff_us / 1e3
+    return {"latency_bound_ms": chain_ms + hand_ms, "chain_ms": chain_ms,
+            "handoff_ms": hand_ms, "sm_mhz": sm_mhz, "dependent_op_cycles": op_cycles,
+            "handoff_us": handoff_us, "strips": strips, "sweep_groups": groups}
+
+
 def run_case(case: str):
     """Small, self-contained runs of one form, for kernel profiles."""
     import torch
@@ -1051,6 +1150,13 @@ def summarize(line):
     df = forms.get("differentiation")
     if df:
         out["differentiation"] = {"value": r3(df.get("value")), "error": df.get("error")}
+    fm = forms.get("fma")
+    if fm:
+        errs = fm.get("rel_l2_vs_bit_exact_frame_1") or {}
+        out["fma"] = {"value": r3(fm.get("value")), "vs_plain": r3(fm.get("vs_plain")),
+                      "err": r3(max(errs.values())) if errs else None, "error": fm.get("error")}
+    out["plain"]["solve_alone_ms"] = r3(g(line, "roofline", "alone_ms"))
+    out["plain"]["latency_bound_ms"] = r3(g(line, "roofline", "latency_bound_ms"))
     return out
 
 
@@ -1203,6 +1309,7 @@ def run_ours(args):
         e2e_times.append(time.perf_counter() - t0)
     e2e_value, e2e_s = replicas_value(sum(e2e_times), args.steps, world, reduce_max)
     assert np.isfinite(outs[0].numpy()).all()
+    alone_ms = solve_alone_ms(L, fl)  # after the timed regions (it changes vx0 / vy0)
 
     # the batched form shards by scene: every rank steps its own part
     sharded = None
@@ -1224,12 +1331,18 @@ def run_ours(args):
     avg_ls = ls_ms.value / max(ls_n.value, 1) / 1e3
     achieved = BYTES_PER_CELL_LINSOLVE * SIZE * SIZE / avg_ls / 1e9 if avg_ls > 0 else None
     traffic, traffic_src = profile_traffic()
+    clocks = clk.summary()
+    sm_mhz = float(clocks.get("sm_mhz") or 2070.0)
+    strips = (SIZE + 2 * (ITERS - 1) + 31) // 32
+    groups_alone = max(2, min(5, 152 // strips))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
-                "kernel": ("lin_solve: k_lin_solve (multi-block temporal wavefront, the "
-                           "three solves on the critical path) and k_ls_cs (cluster "
-                           "wavefront, strips streamed; the two side-stream diffusions)"),
+                "kernel": ("lin_solve: k_ls_sw (strip wavefront), every solve of step(): "
+                           "the three diffusions side by side, then the two pressure solves"),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "alone_ms": alone_ms,
+                "alone_achieved": BYTES_PER_CELL_LINSOLVE * SIZE * SIZE / (alone_ms / 1e3) / 1e9,
+                **latency_bound_ms(sm_mhz, strips, groups_alone),
                 "algorithmic_bytes_per_launch": BYTES_PER_CELL_LINSOLVE * SIZE * SIZE,
                 "launches_timed": int(ls_n.value), "avg_launch_ms": avg_ls * 1e3,
                 "share_of_step": (ls_ms.value / (dev_s / world * 1e3)) if dev_s else None,
@@ -1277,6 +1390,7 @@ def run_ours(args):
                                                       autotune=False, err_sample=24))
         form("precision", lambda: run_precision_form(local_rank, args.precision_frames))
         form("differentiation", lambda: run_diff_form(local_rank, fd_dirs=args.fd_dirs))
+        form("fma", lambda: run_fma_form(local_rank))
         for k in ("f16", "bf16", "f16_scalars"):
             if "precision" in forms and k in forms["precision"]:
                 forms["precision"][k]["vs_plain"] = forms["precision"][k]["value"] / value
@@ -1289,7 +1403,7 @@ def run_ours(args):
                     "h2d_bytes_per_step": NSRC * 20,
                     "d2h_bytes_per_step": 3 * SIZE * SIZE * 4,
                     "ms_per_step": e2e_s / args.steps * 1e3},
-            "gpu_launches": int(count1.value - count0.value), "clocks": clk.summary(),
+            "gpu_launches": int(count1.value - count0.value), "clocks": clocks,
             "parity": parity,
             "wall_s_timed_region": wall}
     if forms:

@@ -173,6 +173,7 @@ def load(path: str = LIB_PATH):
         "eq_hfluid_get_stream": (i32, [H, PP]),
         "eq_hfluid_launch_count": (i32, [H, ctypes.POINTER(ctypes.c_uint64)]),
         "eq_hfluid_set_concurrency": (i32, [H, i32]),
+        "eq_hfluid_set_solver": (i32, [H, i32]),
         "eq_batch_launch_count": (i32, [H, ctypes.POINTER(ctypes.c_uint64)]),
         "eq_grad_new": (i32, [H, i64, i64, PP]),
         "eq_grad_free": (i32, [H]),

@@ -523,7 +523,7 @@ int launch_lin_solve_sw(eq_fluid* h, int mode, float* x, const float* x0, float 
     A.a = a;
     A.cr = c_recip;
     const size_t smem = eqk::ls_sw_layout(KG, S).total;
-    const dim3 grid((unsigned)(A.B * G)), block(32u * (unsigned)(KG + 3));
+    const dim3 grid((unsigned)(A.B * G)), block(32u * (unsigned)(KG + eqk::kSwHelpers));
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     if (h->profiling) {
       EQ_CUDA(cudaEventCreate(&ev0));

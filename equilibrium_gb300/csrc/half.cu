@@ -550,4 +550,9 @@ int eq_hfluid_set_concurrency(eq_hfluid* h, int mask) {
   return eq_fluid_set_concurrency(h->plain, mask);
 }
 
+int eq_hfluid_set_solver(eq_hfluid* h, int solver) {
+  if (!h) return fail(EQ_ERR_ARG, "null handle");
+  return eq_fluid_set_solver(h->plain, solver);
+}
+
 }  // extern "C"

@@ -50,10 +50,12 @@
 // The tag is the launch's epoch (a device word the last block advances), so
 // a captured graph replays without clearing anything.
 //
-// Staging. A copy warp streams x0 and the codes of the block's rows, and the
-// initial x rows the first group's first sweep reads, into shared-memory
-// rings: per row one aligned 16-byte chunk (4 columns) per period, issued
-// kSwAH periods before its first use. All warps meet at one block barrier per
+// Staging. A copy warp streams x0 and the codes of the block's rows into
+// shared-memory rings (and in the first group, which imports nothing from a
+// previous group, the group import warp streams the initial x rows its first
+// sweep reads): per row one aligned 16-byte chunk (4 columns) per period,
+// issued kSwAH periods before its first use. No sweep warp issues a global
+// load: a warp's shared-memory loads return in order behind its global loads. All warps meet at one block barrier per
 // period of kSwQ steps; every cross-warp value is written at least one
 // barrier before it is read and its slot is reused only after its last read
 // (the schedule is checked on the CPU with these formulas).
@@ -180,7 +182,6 @@ struct SwWarp {
   const float* xb;
   const uint8_t* cf;
   unsigned long long* edgeOut;  // halo export (lanes 30, 31), null if none
-  unsigned long long* gexpOut;  // group export, null if none
   float* xlast;                 // x + j P - lane for the last sweep, else null
   unsigned tag;
 };
@@ -191,11 +192,10 @@ struct SwWarp {
 // d % kSwRD holds diagonal d - 1, so a period's slots are consecutive.
 struct SwOps {
   float R, D, Ui, X0, xf;
-  float g01;  // group exporter, lanes 0 and 1: this ring's position -1 / -2
   unsigned cd, cf;
 };
 
-template <int MODE, bool FIRSTX, bool FRAME, bool GEXP = false>
+template <int MODE, bool FIRSTX, bool FRAME>
 __device__ __forceinline__ SwOps sw_load(const SwWarp& w, int dp, int q) {
   const int lane = w.lane;
   const int d = dp + q;
@@ -220,10 +220,6 @@ __device__ __forceinline__ SwOps sw_load(const SwWarp& w, int dp, int q) {
     o.xf = w.xf[ic];
     if (MODE == kPassive) o.cf = w.cf[ic];
   }
-  // ring positions -2 and -1 hold the imported halo values (written before
-  // the period's barrier); a lane-0 fix of this step overwrites position -1
-  // later, and the export takes that value from the step itself
-  o.g01 = GEXP ? w.own[slot * kSwRW + (1 - (lane & 1))] : 0.0f;
   return o;
 }
 
@@ -311,12 +307,6 @@ __device__ __forceinline__ void sw_compute(SwWarp& w, int dp, int q, const SwOps
   // lanes 30, 31: halo record d-1 = [post30, -, uval31, post31]
   if (w.edgeOut && d >= 1)
     sw_st2(w.edgeOut + (size_t)(d - 1) * 4, lane == 31 ? w.vcur : post, post, w.tag);
-  if (w.gexpOut) {  // group record d: word p + 2 = position p of diagonal d-1
-    unsigned long long* const rec = w.gexpOut + (size_t)d * kSwGrpWords;
-    sw_st1(rec + lane + 2, post, w.tag);
-    if (lane < 2)
-      sw_st1(rec + (1 - lane), (MODE == kCol && fix) ? -vnew : wrow[1 - lane], w.tag);
-  }
   if (w.xlast && w.interior && (unsigned)(i - 1) < (unsigned)N) w.xlast[d] = vnew;
   w.vprev = w.vcur;
   w.vcur = vnew;
@@ -328,8 +318,8 @@ __device__ __forceinline__ void sw_compute(SwWarp& w, int dp, int q, const SwOps
 // A step of a fast period: the update, the post store and the exports, with
 // no warp vote and no branch, so that the compiler schedules a period's kSwQ
 // steps as one straight-line block. Gives the bits of sw_compute<MODE, true,
-// FRAME> whose vote came out false. GEXP: the warp is its group's exporter.
-template <int MODE, bool FRAME, bool GEXP>
+// FRAME> whose vote came out false.
+template <int MODE, bool FRAME>
 __device__ __forceinline__ void sw_step_fast(SwWarp& w, int dp, int q, const SwOps& o) {
   const unsigned FULL = 0xffffffffu;
   const int lane = w.lane;
@@ -359,11 +349,6 @@ __device__ __forceinline__ void sw_step_fast(SwWarp& w, int dp, int q, const SwO
   if (MODE == kCol && fix) wrow[1] = -vnew;
   // lanes 30, 31: halo record d-1 = [post30, -, uval31, post31] (d >= 2 here)
   if (w.edgeOut) sw_st2(w.edgeOut + (size_t)(d - 1) * 4, lane == 31 ? w.vcur : post, post, w.tag);
-  if (GEXP) {  // group record d: word p + 2 = position p of diagonal d-1
-    unsigned long long* const rec = w.gexpOut + (size_t)d * kSwGrpWords;
-    sw_st1(rec + lane + 2, post, w.tag);
-    if (lane < 2) sw_st1(rec + (1 - lane), (MODE == kCol && fix) ? -vnew : o.g01, w.tag);
-  }
   if (w.xlast && w.interior) w.xlast[d] = vnew;  // 1 <= i - 1 < N in the fast range
   w.vprev = w.vcur;
   w.vcur = vnew;
@@ -376,12 +361,12 @@ __device__ __forceinline__ void sw_step_fast(SwWarp& w, int dp, int q, const SwO
 // on the codes of all kSwQ steps (a boundary action of the previous cell, a
 // lane-0 fix) sends the whole period through the general rules, which give
 // the fast steps' bits wherever those apply.
-template <int MODE, bool FIRSTX, bool FRAME, bool GEXP>
+template <int MODE, bool FIRSTX, bool FRAME>
 __device__ __forceinline__ void sw_period_fast(SwWarp& w, int dp) {
   const unsigned FULL = 0xffffffffu;
   SwOps o[kSwQ];
 #pragma unroll
-  for (int q = 0; q < kSwQ; ++q) o[q] = sw_load<MODE, FIRSTX, FRAME, GEXP>(w, dp, q);
+  for (int q = 0; q < kSwQ; ++q) o[q] = sw_load<MODE, FIRSTX, FRAME>(w, dp, q);
   bool general = false;
   if (MODE != kPassive) {
     const unsigned actMask =
@@ -402,25 +387,28 @@ __device__ __forceinline__ void sw_period_fast(SwWarp& w, int dp) {
     for (int q = 0; q < kSwQ; ++q) sw_compute<MODE, false, FRAME>(w, dp, q, o[q]);
   } else {
 #pragma unroll
-    for (int q = 0; q < kSwQ; ++q) sw_step_fast<MODE, FRAME, GEXP>(w, dp, q, o[q]);
+    for (int q = 0; q < kSwQ; ++q) sw_step_fast<MODE, FRAME>(w, dp, q, o[q]);
   }
 }
 
 // Warps of a block: kSwMaxKG sweep warps at most, the copy warp, the group
-// import warp and the halo import warp.
-constexpr int kSwThreads = 32 * (kSwMaxKG + 3);
+// import warp, the halo import warp and the group export warp.
+constexpr int kSwHelpers = 4;
+constexpr int kSwThreads = 32 * (kSwMaxKG + kSwHelpers);
 static_assert(12 * kSwMaxKG <= 128, "the halo import warp holds 4 words a lane per period");
 
 // The role of warp w of a block with KG sweep warps (nk of them real): sweep
-// kk < KG, or KG (copy), KG + 1 (group import), KG + 2 (halo import). Warp w
-// issues from SM sub-partition w % 4, so the helpers take warps h, h+1, h+2
-// (h = min(4, KG)) and the two heaviest sweeps, the first (it reads the
-// initial x or the group import ring) and the last (group export or x), take
-// warps 0 and 1: each shares its sub-partition with a helper.
+// kk < KG, or KG (copy), KG + 1 (group import), KG + 2 (halo import), KG + 3
+// (group export). Warp w issues from SM sub-partition w % 4, so the helpers
+// take warps h .. h+3 (h = min(4, KG)) and the two heaviest sweeps, the first
+// (it reads the initial x or the group import ring) and the last (it writes
+// x in the last group), take warps 0 and 1.
 __device__ __forceinline__ int sw_role(int w, int KG, int nk) {
   const int h = KG < 4 ? KG : 4;
-  if (w >= h && w < h + 3) return KG + (w - h);
-  const int slot = w < h ? w : w - 3;  // sweep slots in warp order
+  // helpers in warp order: group export (light, beside the first sweep and
+  // the sweep of slot 4), group import, halo import, copy
+  if (w >= h && w < h + kSwHelpers) return KG + ((0x0213 >> (4 * (w - h))) & 0xF);
+  const int slot = w < h ? w : w - kSwHelpers;  // sweep slots in warp order
   if (slot == 0 || nk < 2) return slot;
   if (slot == 1) return nk - 1;
   return slot <= nk - 1 ? slot - 1 : slot;
@@ -482,34 +470,9 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
   const unsigned long long* const gexpIn =
       g > 0 ? A.gexp + ((size_t)b * (G - 1) + (g - 1)) * (A.RE + 1) * kSwGrpWords : nullptr;
 
-  if (role == KG) {
-    // ---- the copy warp: x0 / code rows and the first group's initial-x rows
-    auto issue = [&](int cp) {
-      const int u = cp + kSwAH;  // use period
-      for (int q = lane; q < nrw; q += 32) {
-        const int r = rA + q;
-        if (r < 0 || r > S - 1) continue;
-        const int dr = jb - r;
-        const int kmin = dr > 0 ? (dr + 1) >> 1 : 0;
-        const int off = dr - (kSwLg + 2) * kmin;
-        const int n = u + ((off + 3) >> 2);
-        if (n < 0 || 4 * n >= P) continue;
-        const int sc = (4 * n) & (kSwPC - 1);
-        cp_async16(&X0R[q * kSwPCS + sc], A.x0 + (size_t)r * P + 4 * n, true);
-        cp_async4(&CR[q * kSwCCS + sc], A.code + (size_t)r * P + 4 * n, true);
-      }
-      if (g == 0) {
-        for (int q = lane; q < 33; q += 32) {
-          const int r = jb + q;
-          if (r > S - 1) continue;
-          const int n = u + 1 - ((q + 3) >> 2);
-          if (n < 0 || 4 * n >= P) continue;
-          cp_async16(&XR[q * kSwPXS + ((4 * n) & (kSwPX - 1))], A.x + (size_t)r * P + 4 * n,
-                     true);
-        }
-      }
-      cp_async_commit();
-    };
+  // A copy loop: chunk copies issued kSwAH periods before their use period,
+  // the use period cp + 1 landed before the barrier that ends period cp.
+  auto copy_loop = [&](auto issue) {
     for (int cp = -kSwAH - 1; cp < 0; ++cp) issue(cp);
     cp_async_wait<kSwAH - 1>();  // use periods -1 and 0 have landed
     if (!__syncthreads_or(0)) {
@@ -520,6 +483,60 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
       }
     }
     cp_async_wait<0>();
+  };
+  if (role == KG) {
+    // ---- the copy warp: x0 / code rows. Lane l copies rows l and l + 32 of
+    // the rings; row q's 4-column chunk n = u + c(q) is first read in use
+    // period u (c(q) from the first sweep that reads the row).
+    const float* gx[2];
+    const uint8_t* gc[2];
+    int cq[2], qs[2];
+#pragma unroll
+    for (int s2 = 0; s2 < 2; ++s2) {
+      const int q = lane + 32 * s2, r = rA + q;
+      const bool ok = q < nrw && r >= 0 && r <= S - 1;
+      const int dr = jb - r;
+      const int kmin = dr > 0 ? (dr + 1) >> 1 : 0;
+      cq[s2] = ok ? (dr - (kSwLg + 2) * kmin + 3) >> 2 : -(1 << 28);
+      gx[s2] = A.x0 + (size_t)(ok ? r : 0) * P;
+      gc[s2] = A.code + (size_t)(ok ? r : 0) * P;
+      qs[s2] = q;
+    }
+    copy_loop([&](int cp) {
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2) {
+        const int n = cp + kSwAH + cq[s2];
+        if (n >= 0 && 4 * n < P) {
+          const int sc = (4 * n) & (kSwPC - 1);
+          cp_async16(&X0R[qs[s2] * kSwPCS + sc], gx[s2] + 4 * n, true);
+          cp_async4(&CR[qs[s2] * kSwCCS + sc], gc[s2] + 4 * n, true);
+        }
+      }
+      cp_async_commit();
+    });
+  } else if (role == KG + 1 && g == 0) {
+    // ---- the first group has no group import: this warp copies the initial
+    // x rows its first sweep reads (row q's chunk u + 1 - ceil(q / 4) is first
+    // read in use period u)
+    const float* gx[2];
+    int cq[2], qs[2];
+#pragma unroll
+    for (int s2 = 0; s2 < 2; ++s2) {
+      const int q = lane + 32 * s2, r = jb + q;
+      const bool ok = q < 33 && r <= S - 1;
+      cq[s2] = ok ? 1 - ((q + 3) >> 2) : -(1 << 28);
+      gx[s2] = A.x + (size_t)(ok ? r : 0) * P;
+      qs[s2] = q;
+    }
+    copy_loop([&](int cp) {
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2) {
+        const int n = cp + kSwAH + cq[s2];
+        if (n >= 0 && 4 * n < P)
+          cp_async16(&XR[qs[s2] * kSwPXS + ((4 * n) & (kSwPX - 1))], gx[s2] + 4 * n, true);
+      }
+      cp_async_commit();
+    });
   } else if (role == KG + 1) {
     // ---- the group import warp: the previous group's last sweep, per period
     // 4 records x 34 words (positions -2 .. 31) of the diagonals d - 1 the
@@ -688,6 +705,37 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
         if (__syncthreads_or(bad)) break;
       }
     }
+  } else if (role == KG + 3) {
+    // ---- the group export warp: the group's last sweep (kk = nk - 1) leaves
+    // its ring row of diagonal d - 1 complete (positions -2 .. 31, with the
+    // imported halo and any lane-0 fix) at the end of the period that holds
+    // step d; this warp stores it as record d (word p + 2 = position p) for
+    // group g+1's import warp during the next period (the ring keeps it for
+    // kSwRD steps).
+    const int kx = nk - 1, k = kF + kx;
+    const bool on = g < G - 1 && (rows_active(k) || rows_active(k + 1));
+    unsigned long long* const out =
+        on ? A.gexp + ((size_t)b * (G - 1) + g) * (A.RE + 1) * kSwGrpWords : nullptr;
+    const float* const ring = VR + (size_t)kx * kSwRD * kSwRW;
+    auto export_period = [&](int p) {  // the records of period p
+#pragma unroll
+      for (int s = 0; s < 5; ++s) {
+        const int w = lane + 32 * s;  // word w % 34 of record q = w / 34
+        const int q = w / 34, word = w - 34 * (w / 34);
+        const int d = p * kSwQ - kSwLg * kx + q;
+        if (w < 4 * 34 && d >= 0 && d <= S + 31)
+          sw_st1(out + (size_t)d * kSwGrpWords + word, ring[(d & (kSwRD - 1)) * kSwRW + word], tag);
+      }
+    };
+    int done = -1;  // the last period whose records are out
+    if (!__syncthreads_or(0)) {  // the prologue counts as period -1
+      for (int cp = 0; cp < NP; ++cp) {
+        if (on && cp > 0) export_period(cp - 1);
+        done = cp - 1;
+        if (__syncthreads_or(0)) break;
+      }
+      if (on && done == NP - 2) export_period(NP - 1);  // after the last barrier
+    }
   } else {
     // ---- sweep warp kk (k = kF + kk); warps past nk only meet the barriers
     const int kk = role, k = kF + kk;
@@ -727,8 +775,6 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
     W.edgeOut = (real && b < B - 1 && lane >= 30)
                     ? A.edge + ((size_t)b * K + k) * A.RE * 4 + (lane == 30 ? 0 : 2)
                     : nullptr;
-    W.gexpOut = exportGroup ? A.gexp + ((size_t)b * (G - 1) + g) * (A.RE + 1) * kSwGrpWords
-                            : nullptr;
     W.xlast = (real && k == K - 1) ? A.x + (size_t)max(W.j, 0) * P - lane : nullptr;
     W.tag = tag;
     W.vcur = W.vprev = W.uprev = 0.0f;
@@ -742,22 +788,15 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
         if (runs) {
           const int dp = cp * kSwQ - kSwLg * kk;
           if (dp >= dF0 && dp + kSwQ - 1 <= dF1) {
-            if (exportGroup) {
-              if (firstX)
-                sw_period_fast<MODE, true, true, true>(W, dp);
-              else if (hasFrame)
-                sw_period_fast<MODE, false, true, true>(W, dp);
-              else
-                sw_period_fast<MODE, false, false, true>(W, dp);
-            } else if (firstX) {
+            if (firstX) {
               if (hasFrame)
-                sw_period_fast<MODE, true, true, false>(W, dp);
+                sw_period_fast<MODE, true, true>(W, dp);
               else
-                sw_period_fast<MODE, true, false, false>(W, dp);
+                sw_period_fast<MODE, true, false>(W, dp);
             } else if (hasFrame) {
-              sw_period_fast<MODE, false, true, false>(W, dp);
+              sw_period_fast<MODE, false, true>(W, dp);
             } else {
-              sw_period_fast<MODE, false, false, false>(W, dp);
+              sw_period_fast<MODE, false, false>(W, dp);
             }
           } else {
             for (int q = 0; q < kSwQ; ++q) {

@@ -76,6 +76,10 @@ class HalfFluid:
         """Which diffusions run on side streams (bit 1: vy, bit 2: density)."""
         check(_lib.load().eq_hfluid_set_concurrency(self.handle, mask))
 
+    def set_solver(self, solver: int):
+        """The kernel of the diffusion solves (as Fluid's eq_fluid_set_solver)."""
+        check(_lib.load().eq_hfluid_set_solver(self.handle, solver))
+
 
 def rel_l2(a: np.ndarray, ref: np.ndarray) -> float:
     """||a - ref||_2 / ||ref||_2 over the interior cells."""

@@ -389,6 +389,8 @@ int eq_hfluid_launch_count(const eq_hfluid* h, uint64_t* count);
 /* Which diffusions of a step run on side streams (EQ_CONC_* bits, as
  * eq_fluid_set_concurrency; default both). */
 int eq_hfluid_set_concurrency(eq_hfluid* h, int mask);
+/* The kernel of the diffusion solves (eq_fluid_set_solver's values). */
+int eq_hfluid_set_solver(eq_hfluid* h, int solver);
 
 /* ---- the differentiation form: adjoint of the frame step --------------- */
 
