@@ -135,8 +135,7 @@ struct eq_fluid {
   unsigned long long* sw_edge[3] = {};
   unsigned long long* sw_gexp[3] = {};  // group exports [strips][groups-1][records+1][36]
   unsigned* sw_ctr[3] = {};
-  int sw_groups = 0;  // sweep groups per strip (0: by size, fewest beside other solves)
-  bool sw_shared = false;  // step(): this solve runs beside the side streams' solves
+  int sw_groups = 0;  // sweep groups per strip (0: by size)
   int sw_slack = 0;   // periods a block's producers must be ahead before it starts
 
   size_t grid_elems() const { return (size_t)P * S; }
@@ -444,17 +443,15 @@ int launch_lin_solve_cluster(eq_fluid* h, int mode, float* x, const float* x0, f
 }
 
 // Sweep groups of the strip wavefront for K sweeps on this grid: blocks of
-// one strip share its sweeps so that about one block per SM works on a solve
-// that runs alone; a solve that shares the GPU with step()'s concurrent
-// diffusions (a side stream's, or the main stream's beside them) takes the
-// fewest groups, so that the three fit the SMs together.
+// one strip share its sweeps so that about one block per SM works on a solve.
+// The same for the diffusions step() runs side by side: their blocks queue
+// for SMs, which measured faster than fewer groups each (N = 1024, 20
+// sweeps: 2.02 against 2.06 ms a step).
 int sw_groups_for(const eq_fluid* h, int K) {
   int G = h->sw_groups;
   if (G <= 0) {
     const int B = eqk::ls_sw_strips((int)h->S, K);
-    G = (h->sw_shared || h->cur_slot != 0)
-            ? 1
-            : std::max(1, std::min(kSwMaxGroups, 152 / std::max(B, 1)));
+    G = std::max(1, std::min(kSwMaxGroups, 152 / std::max(B, 1)));
   }
   G = std::min(G, std::min(K, kSwMaxGroups));
   G = std::max(G, (K + eqk::kSwMaxKG - 1) / eqk::kSwMaxKG);  // at most kSwMaxKG sweeps a block
@@ -745,10 +742,7 @@ int launch_step(eq_fluid* h, float* tape = nullptr) {
     h->cur_slot = slot;
   };
   // the critical path's solve first, then the side solves
-  h->sw_shared = sideVy || sideDe;
-  rc = launch_diffuse(h, eqk::kRow, vx0, vx, h->visc);
-  h->sw_shared = false;
-  if (rc) return rc;
+  if ((rc = launch_diffuse(h, eqk::kRow, vx0, vx, h->visc))) return rc;
   if (sideVy) {
     EQ_CUDA(cudaStreamWaitEvent(h->side[0], h->fork_ev, 0));
     on(h->side[0], 1);

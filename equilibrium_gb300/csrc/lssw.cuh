@@ -31,10 +31,10 @@
 // array.
 //
 // Steps. Inside a warp's fast range (every grid row of the warp an interior
-// row at 2 <= i <= N) a step is the update and one post store; the general
-// rules (frame columns, boundary codes, the lane-0 fix) run only in the
-// periods that need them, decided by one warp vote per period, so that a
-// fast period is straight-line code.
+// row at 2 <= i <= N) a period is straight-line code: the update, the
+// interior boundary rule by the cell's code (branch-free selects; AdjustColumn
+// takes the lane below by a shuffle), the post store and the lane-0 fix. The
+// general rules (frame columns, idle lanes) run only outside that range.
 //
 // Block-to-block values, as 64-bit words (value | tag << 32) polled with
 // relaxed loads issued kSwAHI periods ahead and copied into shared memory:
@@ -82,7 +82,7 @@ constexpr int kSwPCS = kSwPC + 4;  // x0 ring row (floats)
 constexpr int kSwCCS = kSwPC + 4;  // code ring row (bytes)
 constexpr int kSwPXS = kSwPX + 4;  // initial-x ring row (floats)
 constexpr int kSwAH = 5;      // a chunk copy is issued kSwAH periods before its use
-constexpr int kSwAHI = 4;     // an import load is checked kSwAHI periods after its issue
+constexpr int kSwAHI = 2;     // an import load is checked kSwAHI periods after its issue
 constexpr int kSwMaxK = 20;   // sweeps per launch
 constexpr int kSwMaxKG = 10;  // sweeps per block (its warps' registers hold a period's operands)
 constexpr int kSwGrpWords = 36;  // words per group-export record (34 used)
@@ -223,11 +223,10 @@ __device__ __forceinline__ SwOps sw_load(const SwWarp& w, int dp, int q) {
   return o;
 }
 
-// Step d = dp + q from its loaded operands. FAST: every interior lane at
-// 2 <= i <= N (the rare boundary actions still vote into the general rules);
-// FRAME: the warp holds a frame row, whose lane takes the frame cell's value
-// without a branch.
-template <int MODE, bool FAST, bool FRAME>
+// Step d = dp + q from its loaded operands by the general rules (frame
+// columns, frame rows, idle lanes, every boundary code): the steps outside a
+// warp's fast range.
+template <int MODE, bool FRAME>
 __device__ __forceinline__ void sw_compute(SwWarp& w, int dp, int q, const SwOps& o) {
   const unsigned FULL = 0xffffffffu;
   const int lane = w.lane;
@@ -242,64 +241,43 @@ __device__ __forceinline__ void sw_compute(SwWarp& w, int dp, int q, const SwOps
   const float gs = gs_update(o.X0, w.a, fadd(fadd(fadd(R, w.vcur), D), U), w.cr);
   const bool fix = MODE == kCol && lane == 0 && (cd & kCodeAboveDown) != 0 &&
                    (w.interior || w.bot) && (unsigned)(i - 1) < (unsigned)N;
-  bool general = !FAST;
-  if (FAST && MODE != kPassive) {
-    const unsigned actMask =
-        MODE == kRow ? (unsigned)(kCodeRowLeft | kCodeRowRight) : (unsigned)(kCodeColUp | kCodeColDown);
-    general = __any_sync(FULL, w.interior && (((w.cprev & actMask) != 0u) || fix));
-  }
   float vnew, post;
-  if (!general) {
-    vnew = gs;
-    post = w.vcur;
-    if (FRAME) {  // frame-row lanes: the frame cell as the sweep sees it
-      const bool fl = w.top || w.bot;
-      const float vf = (MODE == kPassive && w.top && w.k > 0 && o.cf) ? D : o.xf;
-      vnew = fl ? vf : vnew;
-      if (MODE == kPassive) {
-        const float vdown = __shfl_down_sync(FULL, vnew, 1);
-        const bool pc = fl && (unsigned)(i - 2) < (unsigned)N && w.cfprev != 0u;
-        post = pc ? (w.top ? vdown : w.uprev) : post;
-      }
+  // ---- the general rules, every lane
+  vnew = w.vcur;
+  if (w.interior) {
+    if ((unsigned)(i - 1) < (unsigned)N)
+      vnew = gs;
+    else if (i == 0)
+      vnew = (MODE == kPassive && w.k > 0 && w.pasRow) ? R : w.xL;
+    else if (i == S - 1)
+      vnew = w.xR;
+  } else if (w.top || w.bot) {
+    if ((unsigned)i < (unsigned)S) {
+      const float xf = w.top ? w.xt[i] : w.xb[i];
+      vnew = (MODE == kPassive && w.top && w.k > 0 && w.cf[i]) ? D : xf;
     }
   } else {
-    // ---- the general rules, every lane
-    vnew = w.vcur;
-    if (w.interior) {
-      if ((unsigned)(i - 1) < (unsigned)N)
-        vnew = gs;
-      else if (i == 0)
-        vnew = (MODE == kPassive && w.k > 0 && w.pasRow) ? R : w.xL;
-      else if (i == S - 1)
-        vnew = w.xR;
-    } else if (w.top || w.bot) {
-      if ((unsigned)i < (unsigned)S) {
-        const float xf = w.top ? w.xt[i] : w.xb[i];
-        vnew = (MODE == kPassive && w.top && w.k > 0 && w.cf[i]) ? D : xf;
-      }
-    } else {
-      vnew = 0.0f;
+    vnew = 0.0f;
+  }
+  const float vdown = __shfl_down_sync(FULL, vnew, 1);
+  const int im1 = i - 1;
+  post = w.vcur;
+  if (w.interior) {
+    if ((unsigned)(im1 - 1) < (unsigned)N) {
+      if (MODE == kRow)
+        post = (w.cprev & kCodeRowRight) ? -vnew : ((w.cprev & kCodeRowLeft) ? -w.vprev : w.vcur);
+      else if (MODE == kCol)
+        post = (w.cprev & kCodeColUp) ? -w.uprev : ((w.cprev & kCodeColDown) ? -vdown : w.vcur);
+    } else if (im1 == 0) {
+      post = w.pasRow ? vnew : w.vcur;
+    } else if (im1 == S - 1) {
+      post = w.pasRow ? w.vprev : w.vcur;
     }
-    const float vdown = __shfl_down_sync(FULL, vnew, 1);
-    const int im1 = i - 1;
-    post = w.vcur;
-    if (w.interior) {
-      if ((unsigned)(im1 - 1) < (unsigned)N) {
-        if (MODE == kRow)
-          post = (w.cprev & kCodeRowRight) ? -vnew : ((w.cprev & kCodeRowLeft) ? -w.vprev : w.vcur);
-        else if (MODE == kCol)
-          post = (w.cprev & kCodeColUp) ? -w.uprev : ((w.cprev & kCodeColDown) ? -vdown : w.vcur);
-      } else if (im1 == 0) {
-        post = w.pasRow ? vnew : w.vcur;
-      } else if (im1 == S - 1) {
-        post = w.pasRow ? w.vprev : w.vcur;
-      }
-    } else if (w.top || w.bot) {
-      if (MODE == kPassive && (unsigned)(im1 - 1) < (unsigned)N && w.cf[im1])
-        post = w.top ? vdown : w.uprev;
-    } else {
-      post = 0.0f;
-    }
+  } else if (w.top || w.bot) {
+    if (MODE == kPassive && (unsigned)(im1 - 1) < (unsigned)N && w.cf[im1])
+      post = w.top ? vdown : w.uprev;
+  } else {
+    post = 0.0f;
   }
   float* const wrow = w.own + slot * kSwRW;
   wrow[lane + 2] = post;
@@ -315,10 +293,11 @@ __device__ __forceinline__ void sw_compute(SwWarp& w, int dp, int q, const SwOps
   if (FRAME) w.cfprev = o.cf;
 }
 
-// A step of a fast period: the update, the post store and the exports, with
-// no warp vote and no branch, so that the compiler schedules a period's kSwQ
-// steps as one straight-line block. Gives the bits of sw_compute<MODE, true,
-// FRAME> whose vote came out false.
+// A step of a fast period: the update, the boundary rule of the interior
+// lanes, the post store and the halo export, with no warp vote and no branch,
+// so that the compiler schedules a period's kSwQ steps as one straight-line
+// block. Gives the bits of the general rules wherever every interior lane of
+// the warp is at 2 <= i <= N.
 template <int MODE, bool FRAME>
 __device__ __forceinline__ void sw_step_fast(SwWarp& w, int dp, int q, const SwOps& o) {
   const unsigned FULL = 0xffffffffu;
@@ -344,6 +323,19 @@ __device__ __forceinline__ void sw_step_fast(SwWarp& w, int dp, int q, const SwO
       post = pc ? (w.top ? vdown : w.uprev) : post;
     }
   }
+  // set_boundaries' rule for the interior cell (i-1, j) by its code, branch
+  // free: AdjustRow takes -raw(i, j) (right wall) or -raw(i-2, j) (left),
+  // AdjustColumn -raw(i-1, j-1) (up) or -raw(i-1, j+1) (down, lane l+1)
+  if (MODE == kRow) {
+    const float pr =
+        (w.cprev & kCodeRowRight) ? -vnew : ((w.cprev & kCodeRowLeft) ? -w.vprev : w.vcur);
+    post = w.interior ? pr : post;
+  } else if (MODE == kCol) {
+    const float vdown = __shfl_down_sync(FULL, vnew, 1);
+    const float pc =
+        (w.cprev & kCodeColUp) ? -w.uprev : ((w.cprev & kCodeColDown) ? -vdown : w.vcur);
+    post = w.interior ? pc : post;
+  }
   float* const wrow = w.own + slot * kSwRW;
   wrow[lane + 2] = post;
   if (MODE == kCol && fix) wrow[1] = -vnew;
@@ -357,38 +349,15 @@ __device__ __forceinline__ void sw_step_fast(SwWarp& w, int dp, int q, const SwO
   if (FRAME) w.cfprev = o.cf;
 }
 
-// A period of a warp's fast range: every operand loaded first; one warp vote
-// on the codes of all kSwQ steps (a boundary action of the previous cell, a
-// lane-0 fix) sends the whole period through the general rules, which give
-// the fast steps' bits wherever those apply.
+// A period of a warp's fast range: every operand loaded first, then the
+// kSwQ steps.
 template <int MODE, bool FIRSTX, bool FRAME>
 __device__ __forceinline__ void sw_period_fast(SwWarp& w, int dp) {
-  const unsigned FULL = 0xffffffffu;
   SwOps o[kSwQ];
 #pragma unroll
   for (int q = 0; q < kSwQ; ++q) o[q] = sw_load<MODE, FIRSTX, FRAME>(w, dp, q);
-  bool general = false;
-  if (MODE != kPassive) {
-    const unsigned actMask =
-        MODE == kRow ? (unsigned)(kCodeRowLeft | kCodeRowRight) : (unsigned)(kCodeColUp | kCodeColDown);
-    unsigned prevCodes = w.cprev;  // the previous cell's code of every step
 #pragma unroll
-    for (int q = 0; q + 1 < kSwQ; ++q) prevCodes |= o[q].cd;
-    bool need = (prevCodes & actMask) != 0u;
-    if (MODE == kCol && w.lane == 0) {
-#pragma unroll
-      for (int q = 0; q < kSwQ; ++q)
-        need |= (o[q].cd & kCodeAboveDown) != 0 && (unsigned)(dp + q - 1) < (unsigned)w.N;
-    }
-    general = __any_sync(FULL, w.interior && need);
-  }
-  if (general) {
-#pragma unroll
-    for (int q = 0; q < kSwQ; ++q) sw_compute<MODE, false, FRAME>(w, dp, q, o[q]);
-  } else {
-#pragma unroll
-    for (int q = 0; q < kSwQ; ++q) sw_step_fast<MODE, FRAME>(w, dp, q, o[q]);
-  }
+  for (int q = 0; q < kSwQ; ++q) sw_step_fast<MODE, FRAME>(w, dp, q, o[q]);
 }
 
 // Warps of a block: kSwMaxKG sweep warps at most, the copy warp, the group
@@ -803,9 +772,9 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
               const int d = dp + q;
               if (d < 0 || d > S + 31) continue;
               if (firstX)
-                sw_compute<MODE, false, true>(W, dp, q, sw_load<MODE, true, true>(W, dp, q));
+                sw_compute<MODE, true>(W, dp, q, sw_load<MODE, true, true>(W, dp, q));
               else
-                sw_compute<MODE, false, true>(W, dp, q, sw_load<MODE, false, true>(W, dp, q));
+                sw_compute<MODE, true>(W, dp, q, sw_load<MODE, false, true>(W, dp, q));
             }
           }
         }

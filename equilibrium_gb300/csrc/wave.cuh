@@ -201,8 +201,10 @@ __device__ __forceinline__ void wave_chunk(const WTask<ST>& T, WLaneState& st, i
       Xv[r] = xa[r];
       Cv[r] = ca[r];
     }
-    // prefetch the next group
-    if (q0 + kWG < kWQ) wave_prefetch<EDGE>(T, ib + q0 + kWG, S, P, xa, ca);
+    // This group's shared-memory operands first, then the next group's x0 /
+    // codes: a warp's shared loads return in order behind its global loads,
+    // so a shared load issued after the prefetch would wait for it; issued
+    // before, the prefetch overlaps this group's arithmetic instead.
     float Rv[kWG], Dv[kWG], Ev[kWG];
 #pragma unroll
     for (int r = 0; r < kWG; ++r) {
@@ -221,6 +223,7 @@ __device__ __forceinline__ void wave_chunk(const WTask<ST>& T, WLaneState& st, i
         Ev[r] = lds_f32(T.sedge + 4u * (uint32_t)i);
       }
     }
+    if (q0 + kWG < kWQ) wave_prefetch<EDGE>(T, ib + q0 + kWG, S, P, xa, ca);
 #pragma unroll
     for (int r = 0; r < kWG; ++r) {
       const int q = q0 + r;

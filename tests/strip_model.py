@@ -292,17 +292,26 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                         post = np.where(top & cfp, vdown, post)
                         post = np.where(bot & cfp, uprev[kk], post)
                         post = np.where(idle, F(0), post).astype(np.float32)
-                        # the fast path: every interior lane at 2 <= i <= N and no
-                        # boundary action or lane-0 fix; it must give the same bits
-                        actm = {ROW: C_RR | C_RL, COL: C_CU | C_CD, PAS: 0}[mode]
-                        fix0 = mode == COL and bool(cd[0] & C_AD) and bool(interior[0])
-                        if dF0 <= d <= dF1 and not (interior & ((cprev[kk] & actm) != 0)).any() \
-                                and not fix0:
+                        # the fast path (every interior lane at 2 <= i <= N): the
+                        # update and the interior boundary rule on the frame-selected
+                        # values, with no vote; it must give the general rules' bits
+                        if dF0 <= d <= dF1:
                             fast += 1
+                            vf = np.where(interior, gs, vnew).astype(np.float32)
+                            vdf = np.append(vf[1:], vf[31]).astype(np.float32)
+                            if mode == ROW:
+                                pf = np.where(cprev[kk] & C_RR, -vf,
+                                              np.where(cprev[kk] & C_RL, -vprev[kk], vc))
+                            elif mode == COL:
+                                pf = np.where(cprev[kk] & C_CU, -uprev[kk],
+                                              np.where(cprev[kk] & C_CD, -vdf, vc))
+                            else:
+                                pf = vc
+                            pf = pf.astype(np.float32)
                             assert np.array_equal(vnew[interior].view(np.uint32),
                                                   gs[interior].view(np.uint32))
                             assert np.array_equal(post[interior].view(np.uint32),
-                                                  vc[interior].view(np.uint32))
+                                                  pf[interior].view(np.uint32))
                         s = d % RD  # slot d holds diagonal d - 1
                         for l in range(32):
                             VR.write((kk, s, l + 2), post[l], ("vr", k, d - 1, l), cp + 1)
