@@ -76,8 +76,10 @@ constexpr int kSwRW = 36;     // floats per ring row: positions -2 .. 33
 constexpr int kSwPC = 128;    // columns of the x0 / code rings
 constexpr int kSwPX = 32;     // columns of the initial-x ring
 // Row strides of those rings, padded so that the copy warp's per-row chunk
-// writes (one row per lane) fall in different banks; the sweep warps' reads
-// (row + lane, column - lane) stay conflict-free.
+// writes (one row per lane) fall in different banks and the sweep warps'
+// reads (row + lane, column - lane) stay conflict-free; the 4 padding columns
+// repeat the ring's columns 0 .. 3, so a period's 4 columns are read from one
+// base without wrapping.
 constexpr int kSwPCS = kSwPC + 4;  // x0 ring row (floats)
 constexpr int kSwCCS = kSwPC + 4;  // code ring row (bytes)
 constexpr int kSwPXS = kSwPX + 4;  // initial-x ring row (floats)
@@ -203,14 +205,16 @@ __device__ __forceinline__ SwOps sw_load(const SwWarp& w, int dp, int q) {
   const int slot = (dp & (kSwRD - 1)) + q;
   SwOps o;
   if (FIRSTX) {
-    o.R = w.xrl[(i + 1) & (kSwPX - 1)];
-    o.D = w.xrd[i & (kSwPX - 1)];
+    // a period's 4 columns from one base: the ring's column 0 chunk is also
+    // stored past its end (columns kSwPX .. kSwPX + 3)
+    o.R = w.xrl[((dp - lane + 1) & (kSwPX - 1)) + q];
+    o.D = w.xrd[((dp - lane) & (kSwPX - 1)) + q];
   } else {
     o.R = w.prev[slot * kSwRW + lane];
     o.D = w.prev[slot * kSwRW + lane + 1];
   }
   o.Ui = w.ui[slot];
-  const int ci = i & (kSwPC - 1);
+  const int ci = ((dp - lane) & (kSwPC - 1)) + q;  // column i, the same way
   o.X0 = w.x0row[ci];
   o.cd = w.crow[ci];
   o.xf = 0.0f;
@@ -479,6 +483,10 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
           const int sc = (4 * n) & (kSwPC - 1);
           cp_async16(&X0R[qs[s2] * kSwPCS + sc], gx[s2] + 4 * n, true);
           cp_async4(&CR[qs[s2] * kSwCCS + sc], gc[s2] + 4 * n, true);
+          if (sc == 0) {  // the copy past the ring's end (the readers' period base)
+            cp_async16(&X0R[qs[s2] * kSwPCS + kSwPC], gx[s2] + 4 * n, true);
+            cp_async4(&CR[qs[s2] * kSwCCS + kSwPC], gc[s2] + 4 * n, true);
+          }
         }
       }
       cp_async_commit();
@@ -501,8 +509,11 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
 #pragma unroll
       for (int s2 = 0; s2 < 2; ++s2) {
         const int n = cp + kSwAH + cq[s2];
-        if (n >= 0 && 4 * n < P)
-          cp_async16(&XR[qs[s2] * kSwPXS + ((4 * n) & (kSwPX - 1))], gx[s2] + 4 * n, true);
+        if (n >= 0 && 4 * n < P) {
+          const int sc = (4 * n) & (kSwPX - 1);
+          cp_async16(&XR[qs[s2] * kSwPXS + sc], gx[s2] + 4 * n, true);
+          if (sc == 0) cp_async16(&XR[qs[s2] * kSwPXS + kSwPX], gx[s2] + 4 * n, true);
+        }
       }
       cp_async_commit();
     });

@@ -126,9 +126,10 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
             VR = Tracked((nk, RD, cfg.RW), np.float32)
             UI = Tracked((nk, RD), np.float32)
             VP = Tracked((RD, cfg.RW), np.float32)
-            X0R = Tracked((nrw, PC), np.float32)
-            CR = Tracked((nrw, PC), np.uint8)
-            XR = Tracked((33, PX), np.float32)
+            # rings with 4 padding columns that repeat columns 0 .. 3
+            X0R = Tracked((nrw, PC + 4), np.float32)
+            CR = Tracked((nrw, PC + 4), np.uint8)
+            XR = Tracked((33, PX + 4), np.float32)
 
             def chunk_of(n, first):
                 # row's 4-column chunk n is first read in the use period; a
@@ -152,10 +153,11 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                         continue
                     for e in range(CH):
                         col = CH * m + e
-                        X0R.write((q, col % PC), x0g[r, col] if col < S else F(0),
-                                  ("x0", r, col), u)
-                        CR.write((q, col % PC), code[r, col] if col < S else 0,
-                                 ("cd", r, col), u)
+                        for sc in ((col % PC,) if (CH * m) % PC else (col % PC, PC + e)):
+                            X0R.write((q, sc), x0g[r, col] if col < S else F(0),
+                                      ("x0", r, col), u)
+                            CR.write((q, sc), code[r, col] if col < S else 0,
+                                     ("cd", r, col), u)
                 if g == 0:
                     for q in range(33):
                         r = jb + q
@@ -166,8 +168,9 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                             continue
                         for e in range(CH):
                             col = CH * m + e
-                            XR.write((q, col % PX), xin[r, col] if col < S else F(0),
-                                     ("x", r, col), u)
+                            for sc in ((col % PX,) if (CH * m) % PX else (col % PX, PX + e)):
+                                XR.write((q, sc), xin[r, col] if col < S else F(0),
+                                         ("x", r, col), u)
 
             def halo_import(kk, cp):
                 # the halo import warp: the words of use period cp + 1 (lane 0's
@@ -247,9 +250,12 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                                 sl = (d % RD,)
                                 R[l] = VP.read(sl + (l,), ("vr", k - 1, d - 1, l - 2), cp, useR[l], "R")
                                 D[l] = VP.read(sl + (l + 1,), ("vr", k - 1, d - 1, l - 1), cp, useD[l], "D")
-                            else:
-                                R[l] = XR.read((l, (i[l] + 1) % PX), ("x", j[l], i[l] + 1), cp, useR[l], "XR")
-                                D[l] = XR.read((l + 1, i[l] % PX), ("x", j[l] + 1, i[l]), cp, useD[l], "XR")
+                            else:  # a period's columns from one base (no wrap)
+                                dp = cp * Q - LG * kk
+                                R[l] = XR.read((l, ((dp - l + 1) % PX) + t), ("x", j[l], i[l] + 1), cp,
+                                               useR[l], "XR")
+                                D[l] = XR.read((l + 1, ((dp - l) % PX) + t), ("x", j[l] + 1, i[l]), cp,
+                                               useD[l], "XR")
                         U = np.empty(32, np.float32)
                         U[1:] = vcur[kk, :-1]
                         U[0] = UI.read((kk, d % RD), ("ui", k, d - 1), cp, bool(gsl[0]), "UI")
@@ -258,8 +264,9 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                         useC = (interior | bot) & (i >= 1) & (i <= N)
                         for l in range(32):
                             rr = 2 * (nk - 1 - kk) + l
-                            X0[l] = X0R.read((rr, i[l] % PC), ("x0", j[l], i[l]), cp, bool(gsl[l]), "X0")
-                            cd[l] = CR.read((rr, i[l] % PC), ("cd", j[l], i[l]), cp, bool(useC[l]), "CD")
+                            ci = ((cp * Q - LG * kk - l) % PC) + t  # a period's columns, one base
+                            X0[l] = X0R.read((rr, ci), ("x0", j[l], i[l]), cp, bool(gsl[l]), "X0")
+                            cd[l] = CR.read((rr, ci), ("cd", j[l], i[l]), cp, bool(useC[l]), "CD")
                         with np.errstate(all="ignore"):
                             gs = ((X0 + a * (((R + vcur[kk]) + D) + U)) * cr).astype(np.float32)
                         vc = vcur[kk]
