@@ -11,6 +11,7 @@ struct eq_hfluid {
   void* f[6] = {};            // stored fields (2 bytes per cell), pitched like the plain grids
   void* fblock = nullptr;
   float* p32 = nullptr;       // pressure (FP32, pitched, with ghosts)
+  float* plo = nullptr;       // its low-order part during refinement (p = p32 + plo)
   float* b32 = nullptr;       // right-hand side: project's div (FP32)
   float* r32 = nullptr;       // fine residual (FP32)
   double* d_acc = nullptr;    // FP64 reduction slots
@@ -50,6 +51,7 @@ void hfree(eq_hfluid* h) {
   }
   cudaFree(h->fblock);
   cudaFree(h->p32);
+  cudaFree(h->plo);
   cudaFree(h->b32);
   cudaFree(h->r32);
   cudaFree(h->d_acc);
@@ -160,15 +162,15 @@ int h_project(eq_hfluid* h, int which, T* vx, T* vy, T* ps, T* divs) {
   // p: the stored array's values (its frame is the Dirichlet value where a
   // row / column has no fluid cell), interior zeroed
   eqk::k_h_widen<T><<<h_blocks(n), 256, 0, st>>>(h->p32, ps, n);
-  eqk::k_ir_zero<<<h_grid(N, N), kHBlk, 0, st>>>(h->p32, S, P);
+  eqk::k_ir_zero<<<h_grid(N, N), kHBlk, 0, st>>>(h->p32, h->plo, S, P);
   if ((rc = check_launch(pl))) return rc;
   const auto& L0 = h->lv[0];
   double bnorm = 0.0, rel = 0.0, prev = 0.0;
   int it = 0, slow = 0;
   for (;; ++it) {
     EQ_CUDA(cudaMemsetAsync(h->d_acc, 0, 2 * sizeof(double), st));
-    eqk::k_ir_residual<<<h_blocks((size_t)N * N), 256, 0, st>>>(h->p32, h->b32, S, P, pl->rowfl,
-                                                               pl->colfl, h->r32, h->d_acc);
+    eqk::k_ir_residual<<<h_blocks((size_t)N * N), 256, 0, st>>>(
+        h->p32, h->plo, h->b32, S, P, pl->rowfl, pl->colfl, h->r32, h->d_acc);
     if ((rc = check_launch(pl))) return rc;
     EQ_CUDA(cudaMemcpyAsync(h->h_acc, h->d_acc, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
     EQ_CUDA(cudaStreamSynchronize(st));
@@ -181,9 +183,9 @@ int h_project(eq_hfluid* h, int which, T* vx, T* vy, T* ps, T* divs) {
     }
     rel = bnorm > 0.0 ? rn / bnorm : 0.0;
     if (rel <= h->rtol || it >= h->max_ir || rn == 0.0) break;
-    // FP32 floor: the residual of the FP32-rounded pressure (about
-    // eps32 * ||A|| * ||p||) can exceed rtol * ||div|| on large grids; stop
-    // once two rounds in a row gain less than a factor 2.
+    // The pressure is held as p32 + plo (FP32 pairs) and the residual and
+    // the update are computed in FP64, so the residual floor is far below
+    // rtol; still stop once two rounds in a row gain less than a factor 2.
     if (it > 0) slow = (rel > 0.5 * prev) ? slow + 1 : 0;
     if (slow >= 2) break;
     prev = rel;
@@ -193,9 +195,9 @@ int h_project(eq_hfluid* h, int which, T* vx, T* vy, T* ps, T* divs) {
                                                        static_cast<T*>(L0.r), L0.pitch);
     EQ_CUDA(cudaMemsetAsync(L0.e, 0, (size_t)L0.pitch * L0.n * sizeof(float), st));
     h_vcycle<T>(h, 0);
-    eqk::k_ir_update<<<h_grid(N, N), kHBlk, 0, st>>>(h->p32, S, P,
+    eqk::k_ir_update<<<h_grid(N, N), kHBlk, 0, st>>>(h->p32, h->plo, S, P,
                                                      static_cast<const float*>(L0.e), L0.pitch,
-                                                     (float)scale);
+                                                     scale);
     if ((rc = check_launch(pl))) return rc;
   }
   h->stats.ir_iterations[which] = it;
@@ -215,8 +217,8 @@ int h_project(eq_hfluid* h, int which, T* vx, T* vy, T* ps, T* divs) {
     }
     if (neumann) {
       EQ_CUDA(cudaMemsetAsync(h->d_acc, 0, 2 * sizeof(double), st));
-      eqk::k_ir_sum<<<h_blocks((size_t)N * N), 256, 0, st>>>(h->p32, S, P, h->d_acc);
-      eqk::k_ir_center<<<h_grid(N, N), kHBlk, 0, st>>>(h->p32, S, P, h->d_acc);
+      eqk::k_ir_sum<<<h_blocks((size_t)N * N), 256, 0, st>>>(h->p32, h->plo, S, P, h->d_acc);
+      eqk::k_ir_center<<<h_grid(N, N), kHBlk, 0, st>>>(h->p32, h->plo, S, P, h->d_acc);
       if ((rc = check_launch(pl))) return rc;
     }
   }
@@ -387,7 +389,8 @@ int eq_hfluid_new(const eq_fluid_configs* fluid, const eq_simulation_configs* si
   size_t fbytes = 0;  // scalars 2 bytes a cell; velocities 4 with FP32 velocity storage
   for (int q = 0; q < 6; ++q) fbytes += g * ((mixed && q >= 2) ? 4 : 2);
   if (cudaMalloc(&h->fblock, fbytes) != cudaSuccess ||
-      cudaMalloc(&h->p32, g * 4) != cudaSuccess || cudaMalloc(&h->b32, g * 4) != cudaSuccess ||
+      cudaMalloc(&h->p32, g * 4) != cudaSuccess || cudaMalloc(&h->plo, g * 4) != cudaSuccess ||
+      cudaMalloc(&h->b32, g * 4) != cudaSuccess ||
       cudaMalloc(&h->r32, g * 4) != cudaSuccess ||
       cudaMalloc(&h->d_acc, 4 * sizeof(double)) != cudaSuccess)
     return bail(EQ_ERR_OOM, "cudaMalloc (half fields)");
@@ -402,6 +405,7 @@ int eq_hfluid_new(const eq_fluid_configs* fluid, const eq_simulation_configs* si
   }
   if (cudaMemsetAsync(h->fblock, 0, fbytes, pl->stream) != cudaSuccess ||
       cudaMemsetAsync(h->p32, 0, g * 4, pl->stream) != cudaSuccess ||
+      cudaMemsetAsync(h->plo, 0, g * 4, pl->stream) != cudaSuccess ||
       cudaMemsetAsync(h->b32, 0, g * 4, pl->stream) != cudaSuccess ||
       cudaMemsetAsync(h->r32, 0, g * 4, pl->stream) != cudaSuccess)
     return bail(EQ_ERR_CUDA, "cudaMemsetAsync");

@@ -243,9 +243,24 @@ __device__ __forceinline__ void block_add_f64x2(double a, double b, double* out)
   }
 }
 
-// r = b - A p on the interior (FP32), with FP64 sums of r and r^2.
-__global__ void k_ir_residual(const float* __restrict__ p, const float* __restrict__ b, int S,
-                              int P, const uint8_t* __restrict__ rowfl,
+// The refinement's pressure is a pair of FP32 grids, p = ph + pl (pl the
+// low-order part), read and updated in FP64: the residual of an FP32 pressure
+// has a floor near eps32 ||A|| ||p||, above a 1e-5 relative target on large
+// grids; the pair's floor is near eps64's.
+__device__ __forceinline__ double ir_p(const float* ph, const float* pl, size_t q) {
+  return (double)ph[q] + (double)pl[q];
+}
+__device__ __forceinline__ void ir_set(float* ph, float* pl, size_t q, double v) {
+  const float hi = (float)v;
+  ph[q] = hi;
+  pl[q] = (float)(v - (double)hi);
+}
+
+// r = b - A p on the interior (FP64 arithmetic, stored FP32), with FP64 sums
+// of r and r^2.
+__global__ void k_ir_residual(const float* __restrict__ ph, const float* __restrict__ pl,
+                              const float* __restrict__ b, int S, int P,
+                              const uint8_t* __restrict__ rowfl,
                               const uint8_t* __restrict__ colfl, float* __restrict__ r,
                               double* __restrict__ acc) {
   const int N = S - 2;
@@ -255,15 +270,15 @@ __global__ void k_ir_residual(const float* __restrict__ p, const float* __restri
        k += (size_t)gridDim.x * blockDim.x) {
     const int j = (int)(k / N) + 1, i = (int)(k % N) + 1;
     const size_t q = (size_t)j * P + i;
-    const float c = p[q];
-    const float L = (i == 1) ? (rowfl[j] ? c : p[q - 1]) : p[q - 1];
-    const float R = (i == N) ? (rowfl[j] ? c : p[q + 1]) : p[q + 1];
-    const float U = (j == 1) ? (colfl[i] ? c : p[q - P]) : p[q - P];
-    const float D = (j == N) ? (colfl[i] ? c : p[q + P]) : p[q + P];
-    const float res = b[q] - (4.0f * c - (((L + R) + U) + D));
-    r[q] = res;
+    const double c = ir_p(ph, pl, q);
+    const double L = (i == 1) ? (rowfl[j] ? c : ir_p(ph, pl, q - 1)) : ir_p(ph, pl, q - 1);
+    const double R = (i == N) ? (rowfl[j] ? c : ir_p(ph, pl, q + 1)) : ir_p(ph, pl, q + 1);
+    const double U = (j == 1) ? (colfl[i] ? c : ir_p(ph, pl, q - P)) : ir_p(ph, pl, q - P);
+    const double D = (j == N) ? (colfl[i] ? c : ir_p(ph, pl, q + P)) : ir_p(ph, pl, q + P);
+    const double res = (double)b[q] - (4.0 * c - (((L + R) + U) + D));
+    r[q] = (float)res;
     s1 += res;
-    s2 += (double)res * res;
+    s2 += res * res;
   }
   block_add_f64x2(s1, s2, acc);
 }
@@ -279,46 +294,50 @@ __global__ void k_ir_scale(const float* __restrict__ r, int S, int P, float mean
   hs(r0, (size_t)J * pitch0 + I, (r[(size_t)(J + 1) * P + I + 1] - mean) * inv_scale);
 }
 
-// p += scale * e0 on the interior.
-__global__ void k_ir_update(float* __restrict__ p, int S, int P, const float* __restrict__ e0,
-                            int pitch0, float scale) {
+// p += scale * e0 on the interior (FP64, split back into the pair).
+__global__ void k_ir_update(float* __restrict__ ph, float* __restrict__ pl, int S, int P,
+                            const float* __restrict__ e0, int pitch0, double scale) {
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
   const int N = S - 2;
   if (I >= N || J >= N) return;
   const size_t q = (size_t)(J + 1) * P + I + 1;
-  p[q] += scale * e0[(size_t)J * pitch0 + I];
+  ir_set(ph, pl, q, ir_p(ph, pl, q) + scale * (double)e0[(size_t)J * pitch0 + I]);
 }
 
 // Sum of p over the interior (FP64) into acc[0].
-__global__ void k_ir_sum(const float* __restrict__ p, int S, int P, double* __restrict__ acc) {
+__global__ void k_ir_sum(const float* __restrict__ ph, const float* __restrict__ pl, int S, int P,
+                         double* __restrict__ acc) {
   const int N = S - 2;
   double s1 = 0.0;
   const size_t n = (size_t)N * N;
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
        k += (size_t)gridDim.x * blockDim.x) {
     const int j = (int)(k / N) + 1, i = (int)(k % N) + 1;
-    s1 += p[(size_t)j * P + i];
+    s1 += ir_p(ph, pl, (size_t)j * P + i);
   }
   block_add_f64x2(s1, 0.0, acc);
 }
 
 // p -= mean(p) on the interior: the pure-Neumann solution's free constant is
 // fixed at zero mean.
-__global__ void k_ir_center(float* __restrict__ p, int S, int P, const double* __restrict__ acc) {
+__global__ void k_ir_center(float* __restrict__ ph, float* __restrict__ pl, int S, int P,
+                            const double* __restrict__ acc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int N = S - 2;
   if (i > N || j > N) return;
-  p[(size_t)j * P + i] -= (float)(acc[0] / ((double)N * N));
+  const size_t q = (size_t)j * P + i;
+  ir_set(ph, pl, q, ir_p(ph, pl, q) - acc[0] / ((double)N * N));
 }
 
 // p = 0 on the interior (project's `p[idx] = 0.0`, fluid.rs:349).
-__global__ void k_ir_zero(float* __restrict__ p, int S, int P) {
+__global__ void k_ir_zero(float* __restrict__ ph, float* __restrict__ pl, int S, int P) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (i > S - 2 || j > S - 2) return;
-  p[(size_t)j * P + i] = 0.0f;
+  ph[(size_t)j * P + i] = 0.0f;
+  pl[(size_t)j * P + i] = 0.0f;
 }
 
 }  // namespace eqk

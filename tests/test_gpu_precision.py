@@ -68,8 +68,9 @@ def test_first_frame_vs_converged_f64(eqlib, storage):
                max_abs(g.read_field(3), conv.fields[3])) < vel_tol
     st = g.stats()
     for w in range(2):
-        # refinement reached its FP32 floor or the tolerance, well below the start
-        assert st["rel_residual"][w] < 1e-4
+        # refinement reached the tolerance (the pressure pair's FP64 residual
+        # has no floor near it)
+        assert st["rel_residual"][w] <= 1e-5
         assert 1 <= st["ir_iterations"][w] <= 30
         assert np.isfinite(st["div_norm"][w])
     g.close()
@@ -92,7 +93,7 @@ def test_projection_lowers_divergence(eqlib, storage):
         # wall reflections add some back); it only lowers it.
         assert np.isfinite(st["div_norm"][1])
         assert st["div_norm"][1] < st["div_norm_before"][1]
-        assert st["rel_residual"][1] < 1e-4
+        assert st["rel_residual"][1] <= 1e-5
     g.close()
 
 
@@ -108,8 +109,12 @@ def test_rejects_bad_arguments(eqlib):
 @pytest.mark.parametrize("storage", ["f16", "bf16", "f16_scalars"])
 def test_concurrent_diffusions_match_one_stream(eqlib, storage):
     """The step's vy and density diffusions on side streams (the default) give
-    the one-stream step's fields; only the FP64 norms' summation order can
-    differ, so the fields agree to far below the storage rounding."""
+    the one-stream step's fields; only the FP64 norms' summation order (float
+    atomics) can differ, so the fields agree to far below the storage
+    rounding: 1e-6 relative for half fields; 1e-5 for the FP32 velocity
+    fields of f16_scalars, whose rounding (6e-8) the order-dependent last bit
+    of the refinement's FP32 scale factor, amplified by three frames of flow,
+    can exceed (1.03e-6 measured)."""
     out = []
     for mask in (0, 3):
         g = HalfFluid(S, DT, K, DIFF, VISC, storage)
@@ -120,4 +125,25 @@ def test_concurrent_diffusions_match_one_stream(eqlib, storage):
         out.append([g.read_field(f) for f in range(6)])
         g.close()
     for f in range(6):
-        assert rel_l2(out[1][f], out[0][f]) < 1e-6, f
+        tol = 1e-5 if storage == "f16_scalars" and f >= 2 else 1e-6
+        assert rel_l2(out[1][f], out[0][f]) < tol, f
+
+
+@pytest.mark.parametrize("storage", ["f16", "f16_scalars"])
+def test_refinement_reaches_target_at_n2048(eqlib, storage):
+    """The configured precision workload (N = 2048): both pressure solves of a
+    frame reach the relative residual 1e-5 (the FP32 pressure alone stalls
+    near 3e-5; the refinement keeps a pair of FP32 grids read in FP64)."""
+    import bench
+    size = 2050
+    rects, xs, ys, d, u, v = bench.precision_scene(size, nframes=1)
+    g = HalfFluid(size, bench.PREC_DT, K, bench.PREC_DIFF, bench.PREC_VISC, storage, 1e-5, 30)
+    for rc in rects:
+        g.fill_obstacle(*rc)
+    g.add_sources(xs, ys, d[0], u[0], v[0])
+    g.step()
+    st = g.stats()
+    for w in range(2):
+        assert st["rel_residual"][w] <= 1e-5, st
+        assert st["div_norm"][w] < st["div_norm_before"][w], st
+    g.close()
