@@ -1304,8 +1304,7 @@ def run_ours(args):
             fl.handle, NSRC, h_sx.data_ptr() + 4 * o, h_sy.data_ptr() + 4 * o,
             h_sd.data_ptr() + 4 * o, h_su.data_ptr() + 4 * o, h_sv.data_ptr() + 4 * o))
         _lib.check(L.eq_fluid_step(fl.handle))
-        for f_idx, buf in zip((_lib.FIELD_DENSITY, _lib.FIELD_VX, _lib.FIELD_VY), outs):
-            _lib.check(L.eq_fluid_read_field(fl.handle, f_idx, buf.data_ptr(), SIZE * SIZE))
+        fl.read_fields((_lib.FIELD_DENSITY, _lib.FIELD_VX, _lib.FIELD_VY), outs)
         e2e_times.append(time.perf_counter() - t0)
     e2e_value, e2e_s = replicas_value(sum(e2e_times), args.steps, world, reduce_max)
     assert np.isfinite(outs[0].numpy()).all()

@@ -92,6 +92,10 @@ struct eq_fluid {
   uint32_t xtag[2] = {1, 1};
   long long spin_limit = kDefaultSpinLimit;
 
+  // dense staging of eq_fluid_read_fields (grown on demand)
+  float* d_pack = nullptr;
+  size_t d_pack_cap = 0;  // floats
+
   // source staging
   uint8_t* d_src = nullptr;
   size_t d_src_cap = 0;
@@ -831,6 +835,7 @@ void free_handle(eq_fluid* h) {
     cudaFree(h->sw_ctr[k]);
   }
   cudaFree(h->err);
+  cudaFree(h->d_pack);
   cudaFree(h->d_src);
   if (h->h_src) cudaFreeHost(h->h_src);
   if (h->src_ev) cudaEventDestroy(h->src_ev);
@@ -1268,6 +1273,39 @@ int eq_fluid_write_field(eq_fluid* h, int field, const float* host, uint64_t n) 
 }
 int eq_fluid_read_field_async(eq_fluid* h, int field, float* host, uint64_t n) {
   return field_copy(h, field, host, n, true, false);
+}
+
+int eq_fluid_read_fields(eq_fluid* h, int count, const int* fields, float* const* host,
+                         uint64_t n) {
+  if (!h || !fields || !host) return fail(EQ_ERR_ARG, "null argument");
+  if (count < 1 || count > 6) return fail(EQ_ERR_ARG, "count must be 1..6");
+  const size_t g = (size_t)h->S * h->S;
+  if (n != g) return fail(EQ_ERR_ARG, "element count must be size*size");
+  int rc;
+  for (int k = 0; k < count; ++k) {
+    if ((rc = check_field(fields[k]))) return rc;
+    if (!host[k]) return fail(EQ_ERR_ARG, "null host buffer");
+  }
+  if ((rc = select_device(h))) return rc;
+  if (h->d_pack_cap < (size_t)count * g) {
+    EQ_CUDA(cudaStreamSynchronize(h->stream));
+    cudaFree(h->d_pack);
+    h->d_pack = nullptr;
+    h->d_pack_cap = 0;
+    if (cudaMalloc(&h->d_pack, (size_t)count * g * sizeof(float)) != cudaSuccess)
+      return fail(EQ_ERR_OOM, "cudaMalloc (read staging)");
+    h->d_pack_cap = (size_t)count * g;
+  }
+  eqk::PackFields pf;
+  pf.count = count;
+  for (int k = 0; k < count; ++k) pf.src[k] = h->field[fields[k]];
+  const int blocks = (int)std::min<size_t>((g * count + 255) / 256, 152 * 8);
+  eqk::k_pack_fields<<<blocks, 256, 0, h->stream>>>(pf, h->d_pack, (int)h->S, h->P);
+  if ((rc = check_launch(h))) return rc;
+  for (int k = 0; k < count; ++k)
+    EQ_CUDA(cudaMemcpyAsync(host[k], h->d_pack + (size_t)k * g, g * sizeof(float),
+                            cudaMemcpyDeviceToHost, h->stream));
+  return read_err_word(h);  // synchronises the stream
 }
 int eq_fluid_write_field_async(eq_fluid* h, int field, const float* host, uint64_t n) {
   return field_copy(h, field, const_cast<float*>(host), n, false, false);

@@ -225,4 +225,21 @@ static __global__ void k_copy(float* __restrict__ dst, const float* __restrict__
   for (size_t q = t; q < n4; q += stride) d[q] = s[q];
 }
 
+// Dense copies of up to six pitched fields, one after another (the staging of
+// eq_fluid_read_fields: one contiguous device-to-host copy per field).
+struct PackFields {
+  const float* src[6];
+  int count;
+};
+static __global__ void k_pack_fields(PackFields f, float* __restrict__ dst, int S, int P) {
+  const size_t g = (size_t)S * S, total = g * (size_t)f.count;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+       q += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(q / g);
+    const size_t c = q - (size_t)k * g;
+    const size_t j = c / S, i = c - j * S;
+    dst[q] = f.src[k][j * P + i];
+  }
+}
+
 }  // namespace eqk

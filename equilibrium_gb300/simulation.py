@@ -236,6 +236,21 @@ class Fluid:
         check(self._L.eq_fluid_read_field(self._h, field_index, out.ctypes.data, out.size))
         return out
 
+    def read_fields(self, field_indices, outs=None) -> list:
+        """Several fields at once (one device-side packing, one copy each, one
+        synchronisation); `outs` may give the host arrays (pinned memory for
+        the fastest copies)."""
+        import ctypes
+        k = len(field_indices)
+        if outs is None:
+            outs = [np.empty(self._n(), dtype=np.float32) for _ in range(k)]
+        fi = (ctypes.c_int * k)(*field_indices)
+        ptrs = (ctypes.c_void_p * k)(*[o.ctypes.data if isinstance(o, np.ndarray)
+                                       else o.data_ptr() for o in outs])
+        check(self._L.eq_fluid_read_fields(self._h, k, ctypes.cast(fi, ctypes.c_void_p),
+                                           ctypes.cast(ptrs, ctypes.c_void_p), self._n()))
+        return outs
+
     def write_field(self, field_index: int, values):
         a = _as_f32(values, self._n())
         check(self._L.eq_fluid_write_field(self._h, field_index, a.ctypes.data, a.size))

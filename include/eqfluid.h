@@ -173,6 +173,13 @@ int eq_fluid_write_field(eq_fluid* h, int field, const float* host, uint64_t n);
 int eq_fluid_read_field_async(eq_fluid* h, int field, float* host, uint64_t n);
 int eq_fluid_write_field_async(eq_fluid* h, int field, const float* host, uint64_t n);
 
+/* `count` (1..6) fields at once, field k into host[k] (n = size*size each):
+ * one device-side packing and one contiguous copy per field, then one
+ * synchronisation (the pub fields a frame loop reads back after each step:
+ * density, velocities_x, velocities_y). */
+int eq_fluid_read_fields(eq_fluid* h, int count, const int* fields, float* const* host,
+                         uint64_t n);
+
 /* cells_type (fluid.rs:80) as bytes, 1 = DefaultWall. A written mask must keep
  * the whole ghost frame as DefaultWall (init_walls, fluid.rs:552-570, makes it
  * so and nothing in the reference clears it); otherwise EQ_ERR_ARG. */

@@ -94,3 +94,28 @@ def test_add_noise_impulse_geometry(eqlib):
         assert abs(rx - round(rx)) < 0.05 and abs(ry - round(ry)) < 0.05
         assert 0 <= round(rx) < size and 0 <= round(ry) < size
     g.close()
+
+
+def test_read_fields_matches_read_field(eqlib):
+    """eq_fluid_read_fields (device packing, one copy per field) gives each
+    field bit for bit as eq_fluid_read_field does, into numpy and pinned
+    torch buffers, for one to six fields; bad arguments are refused."""
+    import torch
+    size = 133
+    f = Fluid(FluidConfigs(1e-4, 1e-4, False), SimulationConfigs(0.1, 5, size))
+    rng = np.random.default_rng(3)
+    for k in range(6):
+        f.write_field(k, rng.uniform(-1, 1, size * size).astype(np.float32))
+    f.step()
+    want = [f.read_field(k) for k in range(6)]
+    for sel in ((1,), (1, 2, 3), (5, 0, 4, 2), tuple(range(6))):
+        got = f.read_fields(sel)
+        for k, g in zip(sel, got):
+            np.testing.assert_array_equal(g.view(np.uint32), want[k].view(np.uint32))
+    pinned = [torch.empty(size * size, dtype=torch.float32).pin_memory() for _ in range(3)]
+    f.read_fields((1, 2, 3), pinned)
+    for k, t in zip((1, 2, 3), pinned):
+        np.testing.assert_array_equal(t.numpy().view(np.uint32), want[k].view(np.uint32))
+    with pytest.raises(_lib.EqError):
+        f.read_fields((1, 7))
+    f.close()

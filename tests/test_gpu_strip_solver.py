@@ -44,7 +44,7 @@ def scene(size, K, seed):
 
 
 @pytest.mark.parametrize("size,K", [(20, 1), (20, 20), (34, 3), (66, 20), (97, 7), (130, 21),
-                                    (258, 20), (514, 20), (1026, 20), (1026, 45)])
+                                    (258, 20), (514, 20), (1026, 20), (1026, 45), (2050, 20)])
 @pytest.mark.parametrize("mode", [ROW, COL, PAS])
 def test_strip_lin_solve_bitexact(eqlib, size, K, mode):
     L = _lib.load()
