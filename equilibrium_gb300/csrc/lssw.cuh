@@ -146,10 +146,14 @@ __device__ __forceinline__ void sw_st1(unsigned long long* p, float v, unsigned 
   asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p),
                "l"((unsigned long long)__float_as_uint(v) | ((unsigned long long)tag << 32)));
 }
-__device__ __forceinline__ void sw_st2(unsigned long long* p, float v0, float v1, unsigned tag) {
-  asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p),
-               "l"((unsigned long long)__float_as_uint(v0) | ((unsigned long long)tag << 32)),
-               "l"((unsigned long long)__float_as_uint(v1) | ((unsigned long long)tag << 32)));
+// Two words, stored only where `on` (a predicate inside the instruction, so
+// that the lanes that export nothing take no branch around it).
+__device__ __forceinline__ void sw_st2(unsigned long long* p, float v0, float v1, unsigned tag,
+                                       bool on) {
+  asm volatile(
+      "{ .reg .pred q; setp.ne.b32 q, %3, 0; @q st.relaxed.gpu.global.v2.u64 [%0], {%1, %2}; }" ::"l"(p),
+      "l"((unsigned long long)__float_as_uint(v0) | ((unsigned long long)tag << 32)),
+      "l"((unsigned long long)__float_as_uint(v1) | ((unsigned long long)tag << 32)), "r"((int)on));
 }
 
 // The Gauss-Seidel update; the FMA build contracts x0 + a*sum.
@@ -183,7 +187,8 @@ struct SwWarp {
   const float* xt;     // frame rows and column flags in shared memory
   const float* xb;
   const uint8_t* cf;
-  unsigned long long* edgeOut;  // halo export (lanes 30, 31), null if none
+  unsigned long long* edgeOut;  // halo export (lanes 30, 31; the base elsewhere, unused)
+  bool edgeOn;
   float* xlast;                 // x + j P - lane for the last sweep, else null
   unsigned tag;
 };
@@ -287,8 +292,8 @@ __device__ __forceinline__ void sw_compute(SwWarp& w, int dp, int q, const SwOps
   wrow[lane + 2] = post;
   if (MODE == kCol && fix) wrow[1] = -vnew;
   // lanes 30, 31: halo record d-1 = [post30, -, uval31, post31]
-  if (w.edgeOut && d >= 1)
-    sw_st2(w.edgeOut + (size_t)(d - 1) * 4, lane == 31 ? w.vcur : post, post, w.tag);
+  sw_st2(w.edgeOut + (size_t)(d - 1) * 4, lane == 31 ? w.vcur : post, post, w.tag,
+         w.edgeOn && d >= 1);
   if (w.xlast && w.interior && (unsigned)(i - 1) < (unsigned)N) w.xlast[d] = vnew;
   w.vprev = w.vcur;
   w.vcur = vnew;
@@ -344,7 +349,7 @@ __device__ __forceinline__ void sw_step_fast(SwWarp& w, int dp, int q, const SwO
   wrow[lane + 2] = post;
   if (MODE == kCol && fix) wrow[1] = -vnew;
   // lanes 30, 31: halo record d-1 = [post30, -, uval31, post31] (d >= 2 here)
-  if (w.edgeOut) sw_st2(w.edgeOut + (size_t)(d - 1) * 4, lane == 31 ? w.vcur : post, post, w.tag);
+  sw_st2(w.edgeOut + (size_t)(d - 1) * 4, lane == 31 ? w.vcur : post, post, w.tag, w.edgeOn);
   if (w.xlast && w.interior) w.xlast[d] = vnew;  // 1 <= i - 1 < N in the fast range
   w.vprev = w.vcur;
   w.vcur = vnew;
@@ -752,9 +757,8 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
     W.xb = XB;
     W.xf = W.bot ? XB : XT;
     W.cf = CF;
-    W.edgeOut = (real && b < B - 1 && lane >= 30)
-                    ? A.edge + ((size_t)b * K + k) * A.RE * 4 + (lane == 30 ? 0 : 2)
-                    : nullptr;
+    W.edgeOn = real && b < B - 1 && lane >= 30;
+    W.edgeOut = W.edgeOn ? A.edge + ((size_t)b * K + k) * A.RE * 4 + (lane == 30 ? 0 : 2) : A.edge;
     W.xlast = (real && k == K - 1) ? A.x + (size_t)max(W.j, 0) * P - lane : nullptr;
     W.tag = tag;
     W.vcur = W.vprev = W.uprev = 0.0f;
