@@ -97,6 +97,13 @@ __device__ __forceinline__ float lds_f32(uint32_t a) {
 __device__ __forceinline__ void sts_f32(uint32_t a, float v) {
   asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
 }
+// A store only where `on`: the predicate sits inside the instruction, so the
+// lanes that store nothing take no branch around it.
+__device__ __forceinline__ void sts_f32_if(uint32_t a, float v, bool on) {
+  asm volatile("{ .reg .pred q; setp.ne.b32 q, %2, 0; @q st.shared.f32 [%0], %1; }" ::"r"(a), "f"(v),
+               "r"((int)on)
+               : "memory");
+}
 
 // One scene grid as the block solver sees it (diagonal layout; fields in
 // storage format ST, arithmetic in FP32).
@@ -255,28 +262,32 @@ __device__ __forceinline__ void wave_chunk(const WTask<ST>& T, WLaneState& st, i
       if (LAST) {
         if (T.valid && colok) hs(gO, (ptrdiff_t)q * P, val);
       } else {
-        if (colok) sts_f32(sO + 4u * q, val);
-        if (T.scarry && colok) {
+        if (EDGE) {
+          if (colok) sts_f32(sO + 4u * q, val);
+        } else {
+          sts_f32(sO + 4u * q, val);
+        }
+        if (EDGE && tau0 < 2 * kWQ) {
           // Columns 0 / 1 of the carry rows are produced in chunk 1, the
           // super-step in which the next warp still reads the previous strip's
           // columns 0 / 1; they are held back and written when the task ends.
-          if (EDGE && tau0 < 2 * kWQ) {
+          if (T.scarry && colok) {
             if (i - 1 == 0) st.h0 = val;
             if (i - 1 == 1) st.h1 = val;
-          } else {
-            sts_f32(T.scarry + 4u * (uint32_t)(i - 1), val);
           }
+        } else {
+          sts_f32_if(T.scarry + 4u * (uint32_t)(i - 1), val, T.scarry && colok);
         }
       }
-      if (lane == 31 && (EDGE ? (i >= 0 && i <= S - 1) : true))
-        sts_f32(T.sedge + 4u * (uint32_t)i, g);
+      sts_f32_if(T.sedge + 4u * (uint32_t)i, g,
+                 lane == 31 && (EDGE ? (i >= 0 && i <= S - 1) : true));
       // (a lane whose row lies outside the grid reads a clamped row's code)
-      if (MODE == kCol && lane == 0 && T.valid && (Cv[r] & kCodeAboveDown) &&
-          (EDGE ? (i >= 1 && i <= N) : true)) {
-        if (LAST)
-          hs(T.gfix, (ptrdiff_t)i * P, -g);
-        else
-          sts_f32(T.sfix + 4u * (uint32_t)i, -g);
+      const bool fixc = MODE == kCol && lane == 0 && T.valid && (Cv[r] & kCodeAboveDown) &&
+                        (EDGE ? (i >= 1 && i <= N) : true);
+      if (LAST) {
+        if (fixc) hs(T.gfix, (ptrdiff_t)i * P, -g);
+      } else if (MODE == kCol) {
+        sts_f32_if(T.sfix + 4u * (uint32_t)i, -g, fixc);
       }
 
       st.g2 = st.g1;
