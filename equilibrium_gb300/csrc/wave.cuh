@@ -97,8 +97,18 @@ __device__ __forceinline__ float lds_f32(uint32_t a) {
 __device__ __forceinline__ void sts_f32(uint32_t a, float v) {
   asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
 }
-// A store only where `on`: the predicate sits inside the instruction, so the
-// lanes that store nothing take no branch around it.
+// A load only where `on` (else 0), and a store only where `on`: the
+// predicate sits inside the instruction, so the lanes that skip it take no
+// branch around it.
+__device__ __forceinline__ float lds_f32_if(uint32_t a, bool on) {
+  float v;
+  asm volatile(
+      "{ .reg .pred q; setp.ne.b32 q, %2, 0; mov.f32 %0, 0f00000000; @q ld.shared.f32 %0, [%1]; }"
+      : "=f"(v)
+      : "r"(a), "r"((int)on)
+      : "memory");
+  return v;
+}
 __device__ __forceinline__ void sts_f32_if(uint32_t a, float v, bool on) {
   asm volatile("{ .reg .pred q; setp.ne.b32 q, %2, 0; @q st.shared.f32 [%0], %1; }" ::"r"(a), "f"(v),
                "r"((int)on)
@@ -221,9 +231,9 @@ __device__ __forceinline__ void wave_chunk(const WTask<ST>& T, WLaneState& st, i
         const bool okR = T.rring || (i + 1 >= 0 && i + 1 <= S - 1);
         const bool okD = T.dring || (i >= 0 && i <= S - 1);
         const bool okI = (i >= 0 && i <= S - 1);
-        Rv[r] = okR ? lds_f32(sR + 4u * q) : 0.0f;
-        Dv[r] = okD ? lds_f32(sD + 4u * q) : 0.0f;
-        Ev[r] = (lane == 0 && okI) ? lds_f32(T.sedge + 4u * (uint32_t)i) : 0.0f;
+        Rv[r] = lds_f32_if(sR + 4u * q, okR);
+        Dv[r] = lds_f32_if(sD + 4u * q, okD);
+        Ev[r] = lds_f32_if(T.sedge + 4u * (uint32_t)i, lane == 0 && okI);
       } else {
         Rv[r] = lds_f32(sR + 4u * q);
         Dv[r] = lds_f32(sD + 4u * q);
@@ -262,11 +272,7 @@ __device__ __forceinline__ void wave_chunk(const WTask<ST>& T, WLaneState& st, i
       if (LAST) {
         if (T.valid && colok) hs(gO, (ptrdiff_t)q * P, val);
       } else {
-        if (EDGE) {
-          if (colok) sts_f32(sO + 4u * q, val);
-        } else {
-          sts_f32(sO + 4u * q, val);
-        }
+        sts_f32_if(sO + 4u * q, val, colok);
         if (EDGE && tau0 < 2 * kWQ) {
           // Columns 0 / 1 of the carry rows are produced in chunk 1, the
           // super-step in which the next warp still reads the previous strip's
@@ -367,13 +373,12 @@ __device__ __noinline__ void wave_lin_solve(const WGrid<ST> G, const WBufs Bf, i
           for (int q = 0; q < kWQ; ++q) {
             sts_f32(sO + 4u * q, xs[q]);
             const int is = tau0 + q - lane;
-            if (lane >= 30 && is >= 0 && is <= S - 1) {
-              if (tau0 < 2 * kWQ) {  // held back: see the sweep warps' carry rows
-                if (is == 0) h0 = xs[q];
-                if (is == 1) h1 = xs[q];
-              } else {
-                sts_f32(sC + 4u * (uint32_t)is, xs[q]);
-              }
+            const bool carried = lane >= 30 && is >= 0 && is <= S - 1;
+            if (tau0 < 2 * kWQ) {  // held back: see the sweep warps' carry rows
+              if (carried && is == 0) h0 = xs[q];
+              if (carried && is == 1) h1 = xs[q];
+            } else {
+              sts_f32_if(sC + 4u * (uint32_t)is, xs[q], carried);
             }
           }
           if (c == NCH - 1 && lane >= 30) {
