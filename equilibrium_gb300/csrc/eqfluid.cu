@@ -501,8 +501,7 @@ int launch_lin_solve_sw(eq_fluid* h, int mode, float* x, const float* x0, float 
     const int Kc = (int)std::min<int64_t>(eqk::kSwMaxK, h->frames - done);
     const int G = sw_groups_for(h, Kc);
     const int KG = (Kc + G - 1) / G;
-    EQ_CUDA(cudaMemsetAsync(h->sw_ctr[sl], 0, 2 * sizeof(unsigned), h->cur));
-    eqk::LsSwArgs A;
+    eqk::LsSwArgs A;  // its ticket / done counters are zero (reset by the last launch's last block)
     A.x = x;
     A.x0 = x0;
     A.code = h->code;
@@ -999,6 +998,8 @@ int read_err_word(eq_fluid* h) {
     EQ_CUDA(cudaMemsetAsync(h->counters, 0, 2 * sizeof(unsigned), h->stream));
     for (int k = 0; k < 2; ++k)
       EQ_CUDA(cudaMemsetAsync(h->xcounters[k], 0, 2 * sizeof(unsigned), h->stream));
+    for (int k = 0; k < 3; ++k)
+      EQ_CUDA(cudaMemsetAsync(h->sw_ctr[k], 0, 2 * sizeof(unsigned), h->stream));
     EQ_CUDA(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
     EQ_CUDA(cudaStreamSynchronize(h->stream));
     if (e == EQ_ERR_TIMEOUT)

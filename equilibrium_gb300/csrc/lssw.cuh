@@ -98,7 +98,7 @@ struct LsSwArgs {
   const uint8_t* colfl;
   unsigned long long* edge;  // [B-1][K][RE][4] halo exports
   unsigned long long* gexp;  // [B][G-1][RE+1][kSwGrpWords] group exports
-  unsigned* ctr;             // [0] ticket, [1] done (zeroed per launch), [2] epoch
+  unsigned* ctr;             // [0] ticket, [1] done (zeroed by each launch's last block), [2] epoch
   int* err;
   long long spin_limit;
   int S, P, K, B, G, KG, RE;
@@ -797,12 +797,18 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
       }
     }
   }
-  // ---- completion: the last block to finish advances the epoch
+  // ---- completion: the last block to finish (every block has taken its
+  // ticket) resets the ticket and done counters for the next launch on the
+  // stream and advances the epoch
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
     const unsigned prev = atom_add_acq_rel_u32(&A.ctr[1], 1u);
-    if (prev == (unsigned)(B * G) - 1u) atomicAdd(&A.ctr[2], 1u);
+    if (prev == (unsigned)(B * G) - 1u) {
+      atomicExch(&A.ctr[0], 0u);
+      atomicExch(&A.ctr[1], 0u);
+      atomicAdd(&A.ctr[2], 1u);
+    }
   }
 }
 

@@ -1,6 +1,6 @@
-"""The code either side of the step (SURVEY-ranked next rows): the frame
-image (render_image), device add_noise, device obstacle rasterisation and the
-graph-captured frame loop."""
+"""The code either side of the step: the frame image (render_image), device
+add_noise, device obstacle rasterisation, the graph-captured frame loop and
+the packed read-back of the pub fields."""
 import math
 
 import numpy as np
