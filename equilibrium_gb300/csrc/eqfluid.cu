@@ -139,7 +139,8 @@ struct eq_fluid {
   unsigned long long* sw_edge[3] = {};
   unsigned long long* sw_gexp[3] = {};  // group exports [strips][groups-1][records+1][36]
   unsigned* sw_ctr[3] = {};
-  int sw_groups = 0;  // sweep groups per strip (0: by size)
+  int sw_groups = 0;  // sweep groups per strip (0: by size and by what runs beside)
+  bool sw_pair = false;  // step(): the vx diffusion runs beside the vy diffusion
   int sw_slack = 0;   // periods a block's producers must be ahead before it starts
 
   size_t grid_elems() const { return (size_t)P * S; }
@@ -448,14 +449,18 @@ int launch_lin_solve_cluster(eq_fluid* h, int mode, float* x, const float* x0, f
 
 // Sweep groups of the strip wavefront for K sweeps on this grid: blocks of
 // one strip share its sweeps so that about one block per SM works on a solve.
-// The same for the diffusions step() runs side by side: their blocks queue
-// for SMs, which measured faster than fewer groups each (N = 1024, 20
-// sweeps: 2.02 against 2.06 ms a step).
+// The two velocity diffusions that step() runs side by side (the critical
+// path) take the fewest groups, so that both fit the SMs at once; the density
+// diffusion beside them (lower stream priority, needed only at the frame's
+// end) keeps about one block per SM (N = 1024, 20 sweeps: 1.91 ms a step,
+// against 1.98 with one block per SM for all three and 1.94 with the fewest).
 int sw_groups_for(const eq_fluid* h, int K) {
   int G = h->sw_groups;
   if (G <= 0) {
     const int B = eqk::ls_sw_strips((int)h->S, K);
-    G = std::max(1, std::min(kSwMaxGroups, 152 / std::max(B, 1)));
+    G = (h->sw_pair || h->cur_slot == 1)
+            ? 1
+            : std::max(1, std::min(kSwMaxGroups, 152 / std::max(B, 1)));
   }
   G = std::min(G, std::min(K, kSwMaxGroups));
   G = std::max(G, (K + eqk::kSwMaxKG - 1) / eqk::kSwMaxKG);  // at most kSwMaxKG sweeps a block
@@ -745,7 +750,10 @@ int launch_step(eq_fluid* h, float* tape = nullptr) {
     h->cur_slot = slot;
   };
   // the critical path's solve first, then the side solves
-  if ((rc = launch_diffuse(h, eqk::kRow, vx0, vx, h->visc))) return rc;
+  h->sw_pair = sideVy;
+  rc = launch_diffuse(h, eqk::kRow, vx0, vx, h->visc);
+  h->sw_pair = false;
+  if (rc) return rc;
   if (sideVy) {
     EQ_CUDA(cudaStreamWaitEvent(h->side[0], h->fork_ev, 0));
     on(h->side[0], 1);

@@ -543,7 +543,8 @@ int eq_fluid_set_cluster_interval(eq_fluid* h, int max_m);
 /* Sweep groups per strip of the strip wavefront: each strip's sweeps of one
  * launch are split over `groups` blocks (1..5; a block holds at most 10
  * sweeps, so 20 sweeps take at least 2 groups). 0 (default) = by grid size,
- * about one block per SM. */
+ * about one block per SM, except for the two velocity diffusions that step()
+ * runs side by side (the fewest groups, so that both fit the SMs at once). */
 int eq_fluid_set_strip_groups(eq_fluid* h, int groups);
 /* Periods (of 4 wavefront steps) a strip-wavefront block waits, before its
  * first step, for the blocks it reads from to be ahead of it (0..64; 0 by
