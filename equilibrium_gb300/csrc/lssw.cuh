@@ -232,61 +232,56 @@ __device__ __forceinline__ SwOps sw_load(const SwWarp& w, int dp, int q) {
   return o;
 }
 
-// Step d = dp + q from its loaded operands by the general rules (frame
-// columns, frame rows, idle lanes, every boundary code): the steps outside a
-// warp's fast range.
+// Step d = dp + q outside a warp's fast range (its first and last 8 or 9
+// periods, which the next strip and the next group wait for): the fast step
+// plus the frame columns. Only values that some later update reads have to
+// follow the general rules there: an interior row's frame columns i = 0
+// (the frame value; Passive fluid rows from sweep 1 on: the previous sweep's
+// cell (1, j)) and i = S-1, and the post value of column S-1 (Passive fluid
+// rows: cell S-2 as this sweep left it; the codes of frame cells hold no
+// boundary rule, so the other modes keep the frame value). A lane before its
+// row's column 0 or past column S-1, an idle lane, the post value of column
+// 0 and a top frame row's post values are never read: they hold whatever the
+// arithmetic gives, and nothing of them reaches x (the last sweep stores
+// columns 1 .. N only) or another warp's read.
 template <int MODE, bool FRAME>
-__device__ __forceinline__ void sw_compute(SwWarp& w, int dp, int q, const SwOps& o) {
+__device__ __forceinline__ void sw_step_edge(SwWarp& w, int dp, int q, const SwOps& o) {
   const unsigned FULL = 0xffffffffu;
   const int lane = w.lane;
   const int d = dp + q;
   const int i = d - lane;
   const int slot = (dp & (kSwRD - 1)) + q;
-  const float R = o.R, D = o.D;
-  const unsigned cd = o.cd;
-  float U = __shfl_up_sync(FULL, w.vcur, 1);
-  if (lane == 0) U = o.Ui;
   const int S = w.S, N = w.N;
-  const float gs = gs_update(o.X0, w.a, fadd(fadd(fadd(R, w.vcur), D), U), w.cr);
-  const bool fix = MODE == kCol && lane == 0 && (cd & kCodeAboveDown) != 0 &&
-                   (w.interior || w.bot) && (unsigned)(i - 1) < (unsigned)N;
-  float vnew, post;
-  // ---- the general rules, every lane
-  vnew = w.vcur;
-  if (w.interior) {
-    if ((unsigned)(i - 1) < (unsigned)N)
-      vnew = gs;
-    else if (i == 0)
-      vnew = (MODE == kPassive && w.k > 0 && w.pasRow) ? R : w.xL;
-    else if (i == S - 1)
-      vnew = w.xR;
-  } else if (w.top || w.bot) {
-    if ((unsigned)i < (unsigned)S) {
-      const float xf = w.top ? w.xt[i] : w.xb[i];
-      vnew = (MODE == kPassive && w.top && w.k > 0 && w.cf[i]) ? D : xf;
+  float U = __shfl_up_sync(FULL, w.vcur, 1);
+  U = lane == 0 ? o.Ui : U;
+  const float gs = gs_update(o.X0, w.a, fadd(fadd(fadd(o.R, w.vcur), o.D), U), w.cr);
+  const bool inI = (unsigned)(i - 1) < (unsigned)N;  // 1 <= i <= N
+  const bool fix = MODE == kCol && lane == 0 && (o.cd & kCodeAboveDown) != 0 &&
+                   (w.interior || w.bot) && inI;
+  const float vL = (MODE == kPassive && w.k > 0 && w.pasRow) ? o.R : w.xL;
+  float vnew = i == 0 ? vL : (i == S - 1 ? w.xR : gs);
+  float post = w.vcur;
+  if (FRAME) {
+    const bool fl = w.top || w.bot;
+    const float vf = (MODE == kPassive && w.top && w.k > 0 && o.cf) ? o.D : o.xf;
+    vnew = fl ? vf : vnew;
+    if (MODE == kPassive) {
+      const float vdown = __shfl_down_sync(FULL, vnew, 1);
+      const bool pc = fl && (unsigned)(i - 2) < (unsigned)N && w.cfprev != 0u;
+      post = pc ? (w.top ? vdown : w.uprev) : post;
     }
-  } else {
-    vnew = 0.0f;
   }
-  const float vdown = __shfl_down_sync(FULL, vnew, 1);
-  const int im1 = i - 1;
-  post = w.vcur;
-  if (w.interior) {
-    if ((unsigned)(im1 - 1) < (unsigned)N) {
-      if (MODE == kRow)
-        post = (w.cprev & kCodeRowRight) ? -vnew : ((w.cprev & kCodeRowLeft) ? -w.vprev : w.vcur);
-      else if (MODE == kCol)
-        post = (w.cprev & kCodeColUp) ? -w.uprev : ((w.cprev & kCodeColDown) ? -vdown : w.vcur);
-    } else if (im1 == 0) {
-      post = w.pasRow ? vnew : w.vcur;
-    } else if (im1 == S - 1) {
-      post = w.pasRow ? w.vprev : w.vcur;
-    }
-  } else if (w.top || w.bot) {
-    if (MODE == kPassive && (unsigned)(im1 - 1) < (unsigned)N && w.cf[im1])
-      post = w.top ? vdown : w.uprev;
+  if (MODE == kRow) {
+    const float pr =
+        (w.cprev & kCodeRowRight) ? -vnew : ((w.cprev & kCodeRowLeft) ? -w.vprev : w.vcur);
+    post = w.interior ? pr : post;
+  } else if (MODE == kCol) {
+    const float vdown = __shfl_down_sync(FULL, vnew, 1);
+    const float pc =
+        (w.cprev & kCodeColUp) ? -w.uprev : ((w.cprev & kCodeColDown) ? -vdown : w.vcur);
+    post = w.interior ? pc : post;
   } else {
-    post = 0.0f;
+    post = (w.pasRow && i - 1 == S - 1) ? w.vprev : post;
   }
   float* const wrow = w.own + slot * kSwRW;
   wrow[lane + 2] = post;
@@ -294,11 +289,11 @@ __device__ __forceinline__ void sw_compute(SwWarp& w, int dp, int q, const SwOps
   // lanes 30, 31: halo record d-1 = [post30, -, uval31, post31]
   sw_st2(w.edgeOut + (size_t)(d - 1) * 4, lane == 31 ? w.vcur : post, post, w.tag,
          w.edgeOn && d >= 1);
-  if (w.xlast && w.interior && (unsigned)(i - 1) < (unsigned)N) w.xlast[d] = vnew;
+  if (w.xlast && w.interior && inI) w.xlast[d] = vnew;
   w.vprev = w.vcur;
   w.vcur = vnew;
   w.uprev = U;
-  w.cprev = cd;
+  w.cprev = o.cd;
   if (FRAME) w.cfprev = o.cf;
 }
 
@@ -367,6 +362,21 @@ __device__ __forceinline__ void sw_period_fast(SwWarp& w, int dp) {
   for (int q = 0; q < kSwQ; ++q) o[q] = sw_load<MODE, FIRSTX, FRAME>(w, dp, q);
 #pragma unroll
   for (int q = 0; q < kSwQ; ++q) sw_step_fast<MODE, FRAME>(w, dp, q, o[q]);
+}
+
+// A period outside the fast range: every operand loaded first (the loads
+// stay inside the rings for any d), then the steps of the warp's diagonals
+// 0 .. S + 31.
+template <int MODE, bool FIRSTX, bool FRAME>
+__device__ __forceinline__ void sw_period_edge(SwWarp& w, int dp) {
+  SwOps o[kSwQ];
+#pragma unroll
+  for (int q = 0; q < kSwQ; ++q) o[q] = sw_load<MODE, FIRSTX, FRAME>(w, dp, q);
+#pragma unroll
+  for (int q = 0; q < kSwQ; ++q) {
+    const int d = dp + q;
+    if (d >= 0 && d <= w.S + 31) sw_step_edge<MODE, FRAME>(w, dp, q, o[q]);
+  }
 }
 
 // Warps of a block: kSwMaxKG sweep warps at most, the copy warp, the group
@@ -782,15 +792,15 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
             } else {
               sw_period_fast<MODE, false, false>(W, dp);
             }
+          } else if (firstX) {
+            if (hasFrame)
+              sw_period_edge<MODE, true, true>(W, dp);
+            else
+              sw_period_edge<MODE, true, false>(W, dp);
+          } else if (hasFrame) {
+            sw_period_edge<MODE, false, true>(W, dp);
           } else {
-            for (int q = 0; q < kSwQ; ++q) {
-              const int d = dp + q;
-              if (d < 0 || d > S + 31) continue;
-              if (firstX)
-                sw_compute<MODE, true>(W, dp, q, sw_load<MODE, true, true>(W, dp, q));
-              else
-                sw_compute<MODE, true>(W, dp, q, sw_load<MODE, false, true>(W, dp, q));
-            }
+            sw_period_edge<MODE, false, false>(W, dp);
           }
         }
         if (__syncthreads_or(0)) break;

@@ -319,6 +319,48 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                                                   gs[interior].view(np.uint32))
                             assert np.array_equal(post[interior].view(np.uint32),
                                                   pf[interior].view(np.uint32))
+                        else:
+                            # outside the fast range the kernel follows the general
+                            # rules only where a later read needs them (an interior
+                            # row's columns 0 .. S-1 and post values of columns
+                            # 1 .. S-1, the frame rows' columns 0 .. S-1 and the
+                            # bottom row's post values of columns 1 .. N); its other
+                            # values are whatever the arithmetic gives, and the model
+                            # carries them on, so a read of one changes the result
+                            pasr = (mode == PAS) & interior & (rowfl[jj] != 0)
+                            vL = np.where(pasr & (k > 0), R, np.where(interior, xin[jj, 0], F(0)))
+                            xR = np.where(interior, xin[jj, S - 1], F(0))
+                            ve = np.where(i == 0, vL, np.where(i == S - 1, xR, gs))
+                            pe = vc.copy()
+                            fl = top | bot
+                            if fl.any():
+                                xf = np.where(bot, xin[S - 1, ii], xin[0, ii])
+                                ve = np.where(fl, np.where((mode == PAS) & top & (k > 0) &
+                                                           (colfl[ii] != 0), D, xf), ve)
+                            ve = ve.astype(np.float32)
+                            vde = np.append(ve[1:], ve[31]).astype(np.float32)
+                            if fl.any() and mode == PAS:
+                                pc = fl & (im1 >= 1) & (im1 <= N) & \
+                                     (colfl[np.clip(im1, 0, S - 1)] != 0)
+                                pe = np.where(pc, np.where(top, vde, uprev[kk]), pe)
+                            if mode == ROW:
+                                pe = np.where(interior, np.where(cprev[kk] & C_RR, -ve,
+                                              np.where(cprev[kk] & C_RL, -vprev[kk], vc)), pe)
+                            elif mode == COL:
+                                pe = np.where(interior, np.where(cprev[kk] & C_CU, -uprev[kk],
+                                              np.where(cprev[kk] & C_CD, -vde, vc)), pe)
+                            else:
+                                pe = np.where(pasr & (im1 == S - 1), vprev[kk], pe)
+                            pe = pe.astype(np.float32)
+                            inr = (i >= 0) & (i <= S - 1)
+                            need_v = (interior | fl) & inr
+                            need_p = (interior & (im1 >= 1) & (im1 <= S - 1)) | \
+                                     (bot & (im1 >= 1) & (im1 <= N))
+                            assert np.array_equal(ve[need_v].view(np.uint32),
+                                                  vnew[need_v].view(np.uint32))
+                            assert np.array_equal(pe[need_p].view(np.uint32),
+                                                  post[need_p].view(np.uint32))
+                            vnew, post = ve, pe
                         s = d % RD  # slot d holds diagonal d - 1
                         for l in range(32):
                             VR.write((kk, s, l + 2), post[l], ("vr", k, d - 1, l), cp + 1)
