@@ -468,8 +468,8 @@ int sw_groups_for(const eq_fluid* h, int K) {
   return (K + KG - 1) / KG;  // groups that hold a sweep
 }
 
-// Whether the strip wavefront's shared memory fits at this grid size (its
-// frame rows grow with the size; more sweep groups shrink the rest).
+// Whether the strip wavefront's shared memory fits for the sweep groups of
+// this grid (its rings grow with the sweeps a block holds, not with the size).
 bool sw_fits(const eq_fluid* h) {
   int optin = 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device) !=
@@ -479,7 +479,7 @@ bool sw_fits(const eq_fluid* h) {
   }
   const int K = (int)std::min<int64_t>(eqk::kSwMaxK, std::max<int64_t>(h->frames, 1));
   const int G = sw_groups_for(h, K);
-  return eqk::ls_sw_layout((K + G - 1) / G, (int)h->S).total <= (size_t)(optin - kSwStaticSmem);
+  return eqk::ls_sw_layout((K + G - 1) / G).total <= (size_t)(optin - kSwStaticSmem);
 }
 
 // lin_solve by the strip wavefront (lssw.cuh), kSwMaxK sweeps per launch,
@@ -511,7 +511,6 @@ int launch_lin_solve_sw(eq_fluid* h, int mode, float* x, const float* x0, float 
     A.x0 = x0;
     A.code = h->code;
     A.rowfl = h->rowfl;
-    A.colfl = h->colfl;
     A.edge = h->sw_edge[sl];
     A.gexp = h->sw_gexp[sl];
     A.ctr = h->sw_ctr[sl];
@@ -527,7 +526,7 @@ int launch_lin_solve_sw(eq_fluid* h, int mode, float* x, const float* x0, float 
     A.slack = h->sw_slack;
     A.a = a;
     A.cr = c_recip;
-    const size_t smem = eqk::ls_sw_layout(KG, S).total;
+    const size_t smem = eqk::ls_sw_layout(KG).total;
     const dim3 grid((unsigned)(A.B * G)), block(32u * (unsigned)(KG + eqk::kSwHelpers));
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     if (h->profiling) {

@@ -95,7 +95,6 @@ struct LsSwArgs {
   const float* x0;
   const uint8_t* code;
   const uint8_t* rowfl;
-  const uint8_t* colfl;
   unsigned long long* edge;  // [B-1][K][RE][4] halo exports
   unsigned long long* gexp;  // [B][G-1][RE+1][kSwGrpWords] group exports
   unsigned* ctr;             // [0] ticket, [1] done (zeroed by each launch's last block), [2] epoch
@@ -110,9 +109,9 @@ __host__ __device__ inline int ls_sw_strips(int S, int K) { return (S + 2 * (K -
 __host__ __device__ inline int ls_sw_records(int S) { return S + 32; }
 
 struct LsSwLayout {  // byte offsets in one block's shared memory
-  size_t vr, ui, vp, x0r, cr, xr, xt, xb, cf, total;
+  size_t vr, ui, vp, x0r, cr, xr, total;
 };
-__host__ __device__ inline LsSwLayout ls_sw_layout(int KG, int S) {
+__host__ __device__ inline LsSwLayout ls_sw_layout(int KG) {
   const size_t nrw = 32 + 2 * (size_t)(KG - 1);
   LsSwLayout L;
   L.vr = 0;                                        // KG RD RW floats
@@ -121,10 +120,7 @@ __host__ __device__ inline LsSwLayout ls_sw_layout(int KG, int S) {
   L.x0r = (L.vp + (size_t)kSwRD * kSwRW * 4 + 15) / 16 * 16;  // nrw PC floats
   L.cr = L.x0r + nrw * kSwPCS * 4;                 // nrw CCS bytes
   L.xr = (L.cr + nrw * kSwCCS + 15) / 16 * 16;     // 33 PXS floats
-  L.xt = L.xr + 33 * kSwPXS * 4;                   // S floats: frame row 0
-  L.xb = L.xt + (size_t)S * 4;                     // S floats: frame row S-1
-  L.cf = L.xb + (size_t)S * 4;                     // S bytes: column has fluid
-  L.total = (L.cf + (size_t)S + 15) / 16 * 16;
+  L.total = L.xr + 33 * kSwPXS * 4;
   return L;
 }
 
@@ -168,11 +164,11 @@ __device__ __forceinline__ float gs_update(float x0, float a, float sum, float c
 // One sweep warp's state and constants.
 struct SwWarp {
   // lane state: the value at the previous step (L), the one before, last
-  // step's U, the code of the previous cell and (frame rows) the column flag
-  // of the previous cell
+  // step's U and the code of the previous cell
   float vcur, vprev, uprev;
-  unsigned cprev, cfprev;
-  // lane constants
+  unsigned cprev;
+  // lane constants (cfTop / cfBot: the frame rows' column-flag masks)
+  unsigned cfTop, cfBot;
   int lane, j, S, N, k;
   bool interior, top, bot, idle, pasRow;
   float xL, xR, a, cr;
@@ -183,10 +179,6 @@ struct SwWarp {
   const uint8_t* crow;
   const float* xrl;    // first sweep of the first group: initial-x ring rows
   const float* xrd;
-  const float* xf;     // this lane's frame row (row 0 or S-1) in shared memory
-  const float* xt;     // frame rows and column flags in shared memory
-  const float* xb;
-  const uint8_t* cf;
   unsigned long long* edgeOut;  // halo export (lanes 30, 31; the base elsewhere, unused)
   bool edgeOn;
   float* xlast;                 // x + j P - lane for the last sweep, else null
@@ -196,17 +188,17 @@ struct SwWarp {
 // The shared-memory operands of step d = dp + q of a sweep warp (dp a
 // multiple of kSwQ, q < kSwQ): loaded for a whole period before its first
 // step, so that no load waits behind a previous step's ring store. Ring slot
-// d % kSwRD holds diagonal d - 1, so a period's slots are consecutive.
+// d % kSwRD holds diagonal d - 1, so a period's slots are consecutive. A
+// frame row's x0 ring row holds the frame row of x (its value before the
+// sweeps), and every code carries its column's fluid flag.
 struct SwOps {
-  float R, D, Ui, X0, xf;
-  unsigned cd, cf;
+  float R, D, Ui, X0;
+  unsigned cd;
 };
 
-template <int MODE, bool FIRSTX, bool FRAME>
+template <bool FIRSTX>
 __device__ __forceinline__ SwOps sw_load(const SwWarp& w, int dp, int q) {
   const int lane = w.lane;
-  const int d = dp + q;
-  const int i = d - lane;
   const int slot = (dp & (kSwRD - 1)) + q;
   SwOps o;
   if (FIRSTX) {
@@ -222,14 +214,22 @@ __device__ __forceinline__ SwOps sw_load(const SwWarp& w, int dp, int q) {
   const int ci = ((dp - lane) & (kSwPC - 1)) + q;  // column i, the same way
   o.X0 = w.x0row[ci];
   o.cd = w.crow[ci];
-  o.xf = 0.0f;
-  o.cf = 0u;
-  if (FRAME) {  // the frame cell of this column (frame-row lanes), every lane
-    const int ic = min(max(i, 0), w.S - 1);
-    o.xf = w.xf[ic];
-    if (MODE == kPassive) o.cf = w.cf[ic];
-  }
   return o;
+}
+
+// The frame-row lanes of a step (FRAME warps): the frame cell as the sweep
+// sees it (the frame row of x from the x0 ring; Passive, from sweep 1 on, a
+// fluid column's top cell takes the previous sweep's cell (i, 1)), and the
+// bottom row's post value (Passive: a fluid column's bottom cell takes cell
+// (i, S-2) of this sweep, last step's U). A top row's post value is never
+// read. The column flag rides in every code (0 in the frame columns), held
+// per lane as a mask: cfTop for Passive top-row lanes from sweep 1 on,
+// cfBot for Passive bottom-row lanes, 0 elsewhere.
+template <int MODE>
+__device__ __forceinline__ void sw_frame(const SwWarp& w, const SwOps& o, float& vnew,
+                                         float& post) {
+  vnew = (w.top || w.bot) ? ((o.cd & w.cfTop) ? o.D : o.X0) : vnew;
+  if (MODE == kPassive) post = (w.cprev & w.cfBot) ? w.uprev : post;
 }
 
 // Step d = dp + q outside a warp's fast range (its first and last 8 or 9
@@ -261,16 +261,7 @@ __device__ __forceinline__ void sw_step_edge(SwWarp& w, int dp, int q, const SwO
   const float vL = (MODE == kPassive && w.k > 0 && w.pasRow) ? o.R : w.xL;
   float vnew = i == 0 ? vL : (i == S - 1 ? w.xR : gs);
   float post = w.vcur;
-  if (FRAME) {
-    const bool fl = w.top || w.bot;
-    const float vf = (MODE == kPassive && w.top && w.k > 0 && o.cf) ? o.D : o.xf;
-    vnew = fl ? vf : vnew;
-    if (MODE == kPassive) {
-      const float vdown = __shfl_down_sync(FULL, vnew, 1);
-      const bool pc = fl && (unsigned)(i - 2) < (unsigned)N && w.cfprev != 0u;
-      post = pc ? (w.top ? vdown : w.uprev) : post;
-    }
-  }
+  if (FRAME) sw_frame<MODE>(w, o, vnew, post);
   if (MODE == kRow) {
     const float pr =
         (w.cprev & kCodeRowRight) ? -vnew : ((w.cprev & kCodeRowLeft) ? -w.vprev : w.vcur);
@@ -294,14 +285,13 @@ __device__ __forceinline__ void sw_step_edge(SwWarp& w, int dp, int q, const SwO
   w.vcur = vnew;
   w.uprev = U;
   w.cprev = o.cd;
-  if (FRAME) w.cfprev = o.cf;
 }
 
 // A step of a fast period: the update, the boundary rule of the interior
-// lanes, the post store and the halo export, with no warp vote and no branch,
-// so that the compiler schedules a period's kSwQ steps as one straight-line
-// block. Gives the bits of the general rules wherever every interior lane of
-// the warp is at 2 <= i <= N.
+// lanes, the post store and the halo export, with no branch, so that the
+// compiler schedules a period's kSwQ steps as one straight-line block. Gives
+// the bits of the general rules wherever a later read needs them, when every
+// interior lane of the warp is at 2 <= i <= N.
 template <int MODE, bool FRAME>
 __device__ __forceinline__ void sw_step_fast(SwWarp& w, int dp, int q, const SwOps& o) {
   const unsigned FULL = 0xffffffffu;
@@ -313,20 +303,12 @@ __device__ __forceinline__ void sw_step_fast(SwWarp& w, int dp, int q, const SwO
   float U = __shfl_up_sync(FULL, w.vcur, 1);
   U = lane == 0 ? o.Ui : U;
   const float gs = gs_update(o.X0, w.a, fadd(fadd(fadd(o.R, w.vcur), o.D), U), w.cr);
-  // a lane-0 fix outside the interior (a frame row's lane 0 does not vote)
+  // the lane-0 fix of the row above (AdjustColumn, a wall cell under a
+  // fluid cell whose rule takes its lower neighbour)
   const bool fix = MODE == kCol && lane == 0 && (o.cd & kCodeAboveDown) != 0 &&
                    (w.interior || w.bot) && (unsigned)(i - 1) < (unsigned)N;
   float vnew = gs, post = w.vcur;
-  if (FRAME) {  // frame-row lanes: the frame cell as the sweep sees it
-    const bool fl = w.top || w.bot;
-    const float vf = (MODE == kPassive && w.top && w.k > 0 && o.cf) ? o.D : o.xf;
-    vnew = fl ? vf : vnew;
-    if (MODE == kPassive) {
-      const float vdown = __shfl_down_sync(FULL, vnew, 1);
-      const bool pc = fl && (unsigned)(i - 2) < (unsigned)N && w.cfprev != 0u;
-      post = pc ? (w.top ? vdown : w.uprev) : post;
-    }
-  }
+  if (FRAME) sw_frame<MODE>(w, o, vnew, post);  // frame-row lanes
   // set_boundaries' rule for the interior cell (i-1, j) by its code, branch
   // free: AdjustRow takes -raw(i, j) (right wall) or -raw(i-2, j) (left),
   // AdjustColumn -raw(i-1, j-1) (up) or -raw(i-1, j+1) (down, lane l+1)
@@ -350,7 +332,6 @@ __device__ __forceinline__ void sw_step_fast(SwWarp& w, int dp, int q, const SwO
   w.vcur = vnew;
   w.uprev = U;
   w.cprev = o.cd;
-  if (FRAME) w.cfprev = o.cf;
 }
 
 // A period of a warp's fast range: every operand loaded first, then the
@@ -359,7 +340,7 @@ template <int MODE, bool FIRSTX, bool FRAME>
 __device__ __forceinline__ void sw_period_fast(SwWarp& w, int dp) {
   SwOps o[kSwQ];
 #pragma unroll
-  for (int q = 0; q < kSwQ; ++q) o[q] = sw_load<MODE, FIRSTX, FRAME>(w, dp, q);
+  for (int q = 0; q < kSwQ; ++q) o[q] = sw_load<FIRSTX>(w, dp, q);
 #pragma unroll
   for (int q = 0; q < kSwQ; ++q) sw_step_fast<MODE, FRAME>(w, dp, q, o[q]);
 }
@@ -371,7 +352,7 @@ template <int MODE, bool FIRSTX, bool FRAME>
 __device__ __forceinline__ void sw_period_edge(SwWarp& w, int dp) {
   SwOps o[kSwQ];
 #pragma unroll
-  for (int q = 0; q < kSwQ; ++q) o[q] = sw_load<MODE, FIRSTX, FRAME>(w, dp, q);
+  for (int q = 0; q < kSwQ; ++q) o[q] = sw_load<FIRSTX>(w, dp, q);
 #pragma unroll
   for (int q = 0; q < kSwQ; ++q) {
     const int d = dp + q;
@@ -437,24 +418,13 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
     return j0 <= S - 1 && j0 + 31 >= 0;
   };
   const int role = sw_role(warp, KG, nk);
-  const LsSwLayout lay = ls_sw_layout(KG, S);
+  const LsSwLayout lay = ls_sw_layout(KG);
   float* const VR = reinterpret_cast<float*>(ls_sw_smem + lay.vr);
   float* const UI = reinterpret_cast<float*>(ls_sw_smem + lay.ui);
   float* const VP = reinterpret_cast<float*>(ls_sw_smem + lay.vp);
   float* const X0R = reinterpret_cast<float*>(ls_sw_smem + lay.x0r);
   uint8_t* const CR = ls_sw_smem + lay.cr;
   float* const XR = reinterpret_cast<float*>(ls_sw_smem + lay.xr);
-  float* const XT = reinterpret_cast<float*>(ls_sw_smem + lay.xt);
-  float* const XB = reinterpret_cast<float*>(ls_sw_smem + lay.xb);
-  uint8_t* const CF = ls_sw_smem + lay.cf;
-  // frame rows and column flags, where a sweep of this block holds a frame row
-  if (rA <= 0 || jb + 31 >= S - 1) {
-    for (int q = threadIdx.x; q < S; q += blockDim.x) {
-      XT[q] = A.x[q];
-      XB[q] = A.x[(size_t)(S - 1) * P + q];
-      CF[q] = A.colfl[q];
-    }
-  }
   const unsigned long long* const gexpIn =
       g > 0 ? A.gexp + ((size_t)b * (G - 1) + (g - 1)) * (A.RE + 1) * kSwGrpWords : nullptr;
 
@@ -473,9 +443,10 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
     cp_async_wait<0>();
   };
   if (role == KG) {
-    // ---- the copy warp: x0 / code rows. Lane l copies rows l and l + 32 of
-    // the rings; row q's 4-column chunk n = u + c(q) is first read in use
-    // period u (c(q) from the first sweep that reads the row).
+    // ---- the copy warp: x0 / code rows (the frame rows 0 and S-1: x, the
+    // frame values the sweeps see). Lane l copies rows l and l + 32 of the
+    // rings; row q's 4-column chunk n = u + c(q) is first read in use period u
+    // (c(q) from the first sweep that reads the row).
     const float* gx[2];
     const uint8_t* gc[2];
     int cq[2], qs[2];
@@ -486,7 +457,7 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
       const int dr = jb - r;
       const int kmin = dr > 0 ? (dr + 1) >> 1 : 0;
       cq[s2] = ok ? (dr - (kSwLg + 2) * kmin + 3) >> 2 : -(1 << 28);
-      gx[s2] = A.x0 + (size_t)(ok ? r : 0) * P;
+      gx[s2] = (r == 0 || r == S - 1 ? A.x : A.x0) + (size_t)(ok ? r : 0) * P;
       gc[s2] = A.code + (size_t)(ok ? r : 0) * P;
       qs[s2] = q;
     }
@@ -750,6 +721,8 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
     W.idle = !(W.interior || W.top || W.bot);
     const bool hasFrame = __any_sync(FULL, W.top || W.bot);
     W.pasRow = MODE == kPassive && W.interior && A.rowfl[W.j] != 0;
+    W.cfTop = (MODE == kPassive && W.top && k > 0) ? kCodeColFluid : 0u;
+    W.cfBot = (MODE == kPassive && W.bot) ? kCodeColFluid : 0u;
     W.xL = W.interior ? A.x[(size_t)W.j * P] : 0.0f;
     W.xR = W.interior ? A.x[(size_t)W.j * P + (S - 1)] : 0.0f;
     W.a = A.a;
@@ -763,16 +736,12 @@ __global__ void __launch_bounds__(kSwThreads, 1) k_ls_sw(LsSwArgs A) {
     W.crow = CR + (real ? rrow : 0) * kSwCCS;
     W.xrl = XR + lane * kSwPXS;
     W.xrd = XR + (lane + 1) * kSwPXS;
-    W.xt = XT;
-    W.xb = XB;
-    W.xf = W.bot ? XB : XT;
-    W.cf = CF;
     W.edgeOn = real && b < B - 1 && lane >= 30;
     W.edgeOut = W.edgeOn ? A.edge + ((size_t)b * K + k) * A.RE * 4 + (lane == 30 ? 0 : 2) : A.edge;
     W.xlast = (real && k == K - 1) ? A.x + (size_t)max(W.j, 0) * P - lane : nullptr;
     W.tag = tag;
     W.vcur = W.vprev = W.uprev = 0.0f;
-    W.cprev = W.cfprev = 0u;
+    W.cprev = 0u;
     const bool firstX = g == 0 && kk == 0;
     // fast range: every interior lane at 2 <= i <= N
     const int lA = max(0, 1 - j0), lB = min(31, N - j0);

@@ -154,8 +154,10 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                     for e in range(CH):
                         col = CH * m + e
                         for sc in ((col % PC,) if (CH * m) % PC else (col % PC, PC + e)):
-                            X0R.write((q, sc), x0g[r, col] if col < S else F(0),
-                                      ("x0", r, col), u)
+                            # the frame rows' ring rows hold the frame rows of x
+                            fr = r == 0 or r == S - 1
+                            X0R.write((q, sc), (xin if fr else x0g)[r, col] if col < S else F(0),
+                                      ("xf" if fr else "x0", r, col), u)
                             CR.write((q, sc), code[r, col] if col < S else 0,
                                      ("cd", r, col), u)
                 if g == 0:
@@ -261,11 +263,14 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                         U[0] = UI.read((kk, d % RD), ("ui", k, d - 1), cp, bool(gsl[0]), "UI")
                         X0 = np.zeros(32, np.float32)
                         cd = np.zeros(32, np.uint8)
-                        useC = (interior | bot) & (i >= 1) & (i <= N)
+                        inr = (i >= 0) & (i <= S - 1)
+                        useC = ((interior | bot) & (i >= 1) & (i <= N)) | ((top | bot) & inr)
                         for l in range(32):
                             rr = 2 * (nk - 1 - kk) + l
                             ci = ((cp * Q - LG * kk - l) % PC) + t  # a period's columns, one base
-                            X0[l] = X0R.read((rr, ci), ("x0", j[l], i[l]), cp, bool(gsl[l]), "X0")
+                            fr = bool(top[l] or bot[l])
+                            X0[l] = X0R.read((rr, ci), ("xf" if fr else "x0", j[l], i[l]), cp,
+                                             bool(gsl[l] or (fr and inr[l])), "X0")
                             cd[l] = CR.read((rr, ci), ("cd", j[l], i[l]), cp, bool(useC[l]), "CD")
                         with np.errstate(all="ignore"):
                             gs = ((X0 + a * (((R + vcur[kk]) + D) + U)) * cr).astype(np.float32)
@@ -275,10 +280,12 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                         vnew = np.where(i0 & (mode == PAS) & (k > 0) & (rowfl[jj] != 0), R,
                                         np.where(i0, xin[jj, 0], vnew))
                         vnew = np.where(interior & (i == S - 1), xin[jj, S - 1], vnew)
-                        inr = (i >= 0) & (i <= S - 1)
-                        vtop = np.where((mode == PAS) & (k > 0) & (colfl[ii] != 0), D, xin[0, ii])
+                        # frame rows: the frame value from the x0 ring, the column
+                        # flag from the code
+                        cfl = (cd & C_CF) != 0
+                        vtop = np.where((mode == PAS) & (k > 0) & cfl, D, X0)
                         vnew = np.where(top & inr, vtop, vnew)
-                        vnew = np.where(bot & inr, xin[S - 1, ii], vnew)
+                        vnew = np.where(bot & inr, X0, vnew)
                         vnew = np.where(idle, F(0), vnew).astype(np.float32)
                         vdown = np.append(vnew[1:], vnew[31]).astype(np.float32)
                         im1 = i - 1
@@ -294,73 +301,51 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                         pasrow = (mode == PAS) & (rowfl[jj] != 0)
                         post = np.where(interior & (im1 == 0) & pasrow, vnew, post)
                         post = np.where(interior & (im1 == S - 1) & pasrow, vprev[kk], post)
-                        cfp = (mode == PAS) & (colfl[np.clip(im1, 0, S - 1)] != 0) & \
-                              (im1 >= 1) & (im1 <= N)
+                        cfp = (mode == PAS) & ((cprev[kk] & C_CF) != 0) & (im1 >= 1) & (im1 <= N)
                         post = np.where(top & cfp, vdown, post)
                         post = np.where(bot & cfp, uprev[kk], post)
                         post = np.where(idle, F(0), post).astype(np.float32)
-                        # the fast path (every interior lane at 2 <= i <= N): the
-                        # update and the interior boundary rule on the frame-selected
-                        # values, with no vote; it must give the general rules' bits
-                        if dF0 <= d <= dF1:
-                            fast += 1
-                            vf = np.where(interior, gs, vnew).astype(np.float32)
-                            vdf = np.append(vf[1:], vf[31]).astype(np.float32)
-                            if mode == ROW:
-                                pf = np.where(cprev[kk] & C_RR, -vf,
-                                              np.where(cprev[kk] & C_RL, -vprev[kk], vc))
-                            elif mode == COL:
-                                pf = np.where(cprev[kk] & C_CU, -uprev[kk],
-                                              np.where(cprev[kk] & C_CD, -vdf, vc))
-                            else:
-                                pf = vc
-                            pf = pf.astype(np.float32)
-                            assert np.array_equal(vnew[interior].view(np.uint32),
-                                                  gs[interior].view(np.uint32))
-                            assert np.array_equal(post[interior].view(np.uint32),
-                                                  pf[interior].view(np.uint32))
-                        else:
-                            # outside the fast range the kernel follows the general
-                            # rules only where a later read needs them (an interior
-                            # row's columns 0 .. S-1 and post values of columns
-                            # 1 .. S-1, the frame rows' columns 0 .. S-1 and the
-                            # bottom row's post values of columns 1 .. N); its other
-                            # values are whatever the arithmetic gives, and the model
-                            # carries them on, so a read of one changes the result
-                            pasr = (mode == PAS) & interior & (rowfl[jj] != 0)
+                        # the kernel's values: its fast step where every interior
+                        # lane is at 2 <= i <= N, its edge step elsewhere. Both
+                        # follow the general rules only where a later read needs
+                        # them (an interior row's columns 0 .. S-1 and post values
+                        # of columns 1 .. S-1, the frame rows' columns 0 .. S-1,
+                        # the bottom row's post values of columns 1 .. N); the
+                        # model carries the kernel's values on, so a read of any
+                        # other value changes the result
+                        edge_step = not (dF0 <= d <= dF1)
+                        fast += not edge_step
+                        pasr = (mode == PAS) & interior & (rowfl[jj] != 0)
+                        if edge_step:
                             vL = np.where(pasr & (k > 0), R, np.where(interior, xin[jj, 0], F(0)))
                             xR = np.where(interior, xin[jj, S - 1], F(0))
                             ve = np.where(i == 0, vL, np.where(i == S - 1, xR, gs))
-                            pe = vc.copy()
-                            fl = top | bot
-                            if fl.any():
-                                xf = np.where(bot, xin[S - 1, ii], xin[0, ii])
-                                ve = np.where(fl, np.where((mode == PAS) & top & (k > 0) &
-                                                           (colfl[ii] != 0), D, xf), ve)
-                            ve = ve.astype(np.float32)
-                            vde = np.append(ve[1:], ve[31]).astype(np.float32)
-                            if fl.any() and mode == PAS:
-                                pc = fl & (im1 >= 1) & (im1 <= N) & \
-                                     (colfl[np.clip(im1, 0, S - 1)] != 0)
-                                pe = np.where(pc, np.where(top, vde, uprev[kk]), pe)
-                            if mode == ROW:
-                                pe = np.where(interior, np.where(cprev[kk] & C_RR, -ve,
-                                              np.where(cprev[kk] & C_RL, -vprev[kk], vc)), pe)
-                            elif mode == COL:
-                                pe = np.where(interior, np.where(cprev[kk] & C_CU, -uprev[kk],
-                                              np.where(cprev[kk] & C_CD, -vde, vc)), pe)
-                            else:
-                                pe = np.where(pasr & (im1 == S - 1), vprev[kk], pe)
-                            pe = pe.astype(np.float32)
-                            inr = (i >= 0) & (i <= S - 1)
-                            need_v = (interior | fl) & inr
-                            need_p = (interior & (im1 >= 1) & (im1 <= S - 1)) | \
-                                     (bot & (im1 >= 1) & (im1 <= N))
-                            assert np.array_equal(ve[need_v].view(np.uint32),
-                                                  vnew[need_v].view(np.uint32))
-                            assert np.array_equal(pe[need_p].view(np.uint32),
-                                                  post[need_p].view(np.uint32))
-                            vnew, post = ve, pe
+                        else:
+                            ve = gs.copy()
+                        fl = top | bot
+                        ve = np.where(fl, np.where((mode == PAS) & top & (k > 0) & cfl, D, X0), ve)
+                        ve = ve.astype(np.float32)
+                        vde = np.append(ve[1:], ve[31]).astype(np.float32)
+                        pe = vc.copy()
+                        if mode == PAS:
+                            pe = np.where(bot & ((cprev[kk] & C_CF) != 0), uprev[kk], pe)
+                        if mode == ROW:
+                            pe = np.where(interior, np.where(cprev[kk] & C_RR, -ve,
+                                          np.where(cprev[kk] & C_RL, -vprev[kk], vc)), pe)
+                        elif mode == COL:
+                            pe = np.where(interior, np.where(cprev[kk] & C_CU, -uprev[kk],
+                                          np.where(cprev[kk] & C_CD, -vde, vc)), pe)
+                        elif edge_step:
+                            pe = np.where(pasr & (im1 == S - 1), vprev[kk], pe)
+                        pe = pe.astype(np.float32)
+                        need_v = (interior | fl) & inr
+                        need_p = (interior & (im1 >= 1) & (im1 <= S - 1)) | \
+                                 (bot & (im1 >= 1) & (im1 <= N))
+                        assert np.array_equal(ve[need_v].view(np.uint32),
+                                              vnew[need_v].view(np.uint32))
+                        assert np.array_equal(pe[need_p].view(np.uint32),
+                                              post[need_p].view(np.uint32))
+                        vnew, post = ve, pe
                         s = d % RD  # slot d holds diagonal d - 1
                         for l in range(32):
                             VR.write((kk, s, l + 2), post[l], ("vr", k, d - 1, l), cp + 1)
