@@ -519,14 +519,14 @@ int eq_fluid_set_concurrency(eq_fluid* h, int mask);
 /* Which kernel runs lin_solve (all are bit-exact).
  * 0 (default) = the strip wavefront (one launch per 20 sweeps over 32-row
  *   strips and groups of sweeps, blocks chained through tagged exports)
- *   wherever its shared memory fits (frame rows of S floats: N up to about
- *   17000), else as 4.
+ *   wherever x, x0 and the codes are 16-byte aligned (the handle's own grids
+ *   always are; its shared memory does not grow with N), else as 4.
  * 1 = the multi-block wavefront always.
  * 2 = the thread-block-cluster wavefront wherever it applies: 32 < N <= 1024
  *   (strips of up to 64 positions on at most 16 blocks), with its strips
  *   staged in shared memory whole where they fit (<= 32 sweeps, N up to
  *   ~320), else streamed through shared-memory rings (<= 31 sweeps).
- * 3 = the strip wavefront wherever it fits, else as 4.
+ * 3 = the strip wavefront wherever it applies (as 0), else as 4.
  * 4 = the staged cluster form where it applies; the streamed form only for
  *   the solves step() runs on its side streams (it holds few SMs, so it
  *   runs beside the critical path's solve); else the multi-block wavefront.
