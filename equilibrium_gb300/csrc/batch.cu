@@ -53,6 +53,11 @@ struct eq_batch {
 
   int nwmax = 20;  // sweeps per wavefront pass = warps per block
   int bps = 1;     // blocks per SM
+  // the wavefront's per-block staging of packed x0 / codes (8 bytes a cell
+  // of the largest scene's diagonal layout), grown to the launch's blocks
+  void* d_stage = nullptr;
+  size_t stage_stride = 0;
+  int stage_blocks = 0;
   int num_sms = 0;
   size_t max_smem_block = 0, max_smem_sm = 0;
 
@@ -80,6 +85,7 @@ void batch_free(eq_batch* b) {
   batch_drop_graph(b);
   if (b->arena2 && b->arena2 != b->arena) cudaFree(b->arena2);
   cudaFree(b->arena);
+  cudaFree(b->d_stage);
   cudaFree(b->d_dense);
   cudaFree(b->d_doff);
   cudaFree(b->marena);
@@ -222,6 +228,22 @@ int batch_launch_shape(eq_batch* b, BLaunch* L) {
     return fail(EQ_ERR_ARG, "the wavefront buffers do not fit in shared memory at this tuning");
   L->blocks = (int)std::min<int64_t>(b->n, (int64_t)b->num_sms * b->bps);
   if (L->blocks < 1) L->blocks = 1;
+  if (L->blocks > b->stage_blocks) {  // staging for every block of the launch
+    size_t stride = 256;
+    for (const eqk::BScene& d : b->desc)
+      stride = std::max<size_t>(stride, (d.fstride * 8 + 255) / 256 * 256);
+    EQ_CUDA(cudaStreamSynchronize(b->stream));
+    batch_drop_graph(b);  // the graph's kernel arguments point at the old staging
+    cudaFree(b->d_stage);
+    b->d_stage = nullptr;
+    b->stage_blocks = 0;
+    if (cudaMalloc(&b->d_stage, stride * (size_t)L->blocks) != cudaSuccess) {
+      b->d_stage = nullptr;
+      return fail(EQ_ERR_OOM, "cudaMalloc (wavefront staging)");
+    }
+    b->stage_stride = stride;
+    b->stage_blocks = L->blocks;
+  }
   EQ_CUDA(cudaFuncSetAttribute(eqk::k_batch_run<float>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem));
   EQ_CUDA(cudaFuncSetAttribute(eqk::k_batch_run<__half>,
@@ -290,6 +312,8 @@ eqk::BatchArgs batch_args(eq_batch* b, const BLaunch& L, unsigned* queue) {
   A.src_v = b->d_sval ? b->d_sval + 2 * b->src_cap : nullptr;
   A.nwmax = b->nwmax;
   A.cs = batch_cs(b);
+  A.stage = b->d_stage;
+  A.stage_stride = b->stage_stride;
   return A;
 }
 

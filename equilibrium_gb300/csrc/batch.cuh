@@ -45,6 +45,8 @@ struct BatchArgs {
   const float* src_v;
   int nwmax;         // sweeps per wavefront pass (warps per block)
   int cs;            // carry/edge row stride (floats)
+  void* stage;       // per-block staging of the wavefront's packed x0 / codes
+  unsigned long long stage_stride;  // bytes per block (>= 8 x the largest dg_size)
 };
 
 // ---- per-cell phases over one scene, by the whole block --------------------
@@ -365,6 +367,7 @@ __device__ __forceinline__ void blk_op(const BatchArgs& A, const BScene* ssc, co
   G.code = code;
   G.rowfl = rowfl;
   G.colfl = colfl;
+  G.stage = static_cast<char*>(A.stage) + (size_t)blockIdx.x * A.stage_stride;
   G.S = S;
   G.P = P;
   switch (op.kind) {
@@ -390,6 +393,7 @@ __device__ __forceinline__ void blk_op(const BatchArgs& A, const BScene* ssc, co
         H.code = code;
         H.rowfl = rowfl;
         H.colfl = colfl;
+        H.stage = G.stage;
         H.S = S;
         H.P = P;
         H.x = bscalar<STS, ST>(A, sc, op.f[0]);

@@ -124,7 +124,47 @@ struct WGrid {
   const uint8_t* code;   // boundary codes, diagonal layout
   const uint8_t* rowfl;  // [S]
   const uint8_t* colfl;  // [S]
+  void* stage;           // the block's staging (dg_size(S, P) packed words), see WPack
   int S, P;
+};
+
+// x0 and the boundary code of one cell in one word, so that a wavefront step
+// loads one value per lane instead of two (each global load of a sweep warp
+// delays the shared-memory loads issued after it): FP32 as (bits, code),
+// 16-bit formats as bits | code << 16. The raw bits are kept, so the values
+// are those of the field.
+template <class ST>
+struct WPack;
+template <>
+struct WPack<float> {
+  using T = uint2;
+  static __device__ __forceinline__ T make(float x0, uint8_t c) {
+    return make_uint2(__float_as_uint(x0), (uint32_t)c);
+  }
+  static __device__ __forceinline__ float x(T v) { return __uint_as_float(v.x); }
+  static __device__ __forceinline__ uint32_t c(T v) { return v.y; }
+};
+template <>
+struct WPack<__half> {
+  using T = uint32_t;
+  static __device__ __forceinline__ T make(__half x0, uint8_t c) {
+    return (uint32_t)__half_as_ushort(x0) | ((uint32_t)c << 16);
+  }
+  static __device__ __forceinline__ float x(T v) {
+    return __half2float(__ushort_as_half((unsigned short)(v & 0xffffu)));
+  }
+  static __device__ __forceinline__ uint32_t c(T v) { return v >> 16; }
+};
+template <>
+struct WPack<__nv_bfloat16> {
+  using T = uint32_t;
+  static __device__ __forceinline__ T make(__nv_bfloat16 x0, uint8_t c) {
+    return (uint32_t)__bfloat16_as_ushort(x0) | ((uint32_t)c << 16);
+  }
+  static __device__ __forceinline__ float x(T v) {
+    return __bfloat162float(__ushort_as_bfloat16((unsigned short)(v & 0xffffu)));
+  }
+  static __device__ __forceinline__ uint32_t c(T v) { return v >> 16; }
 };
 
 // Block-private buffers, all in the block's dynamic shared memory, given as
@@ -162,8 +202,7 @@ template <class ST>
 struct WTask {
   ST* gout;        // last sweep: x row j, global
   ST* gfix;           // last sweep: x row j-1 (AdjustColumn fix-up), global
-  const ST* x0row;
-  const uint8_t* crow;
+  const typename WPack<ST>::T* pkrow;  // packed x0 / codes of row j, column i at [i * P]
   uint32_t sr, sd;    // other sweeps: R / D source (ring lane, slot-indexed, or carry row)
   uint32_t sout;      // other sweeps: this lane's ring row (slot-indexed)
   uint32_t scarry;    // lanes 30/31 of a non-last sweep: carry row (0 = none)
@@ -174,12 +213,12 @@ struct WTask {
 };
 
 // x0 and codes of columns ib..ib+kWG-1 of this lane's row (EDGE: only the
-// ones inside the grid).
+// ones inside the grid), one packed load each. Plain (coherent) loads: the
+// block wrote the staging at the solve's start.
 template <bool EDGE, class ST>
 __device__ __forceinline__ void wave_prefetch(const WTask<ST>& T, int ib, int S, int P,
                                               float (&x)[kWG], uint32_t (&c)[kWG]) {
-  const ST* px = T.x0row + (ptrdiff_t)ib * P;
-  const uint8_t* pc = T.crow + (ptrdiff_t)ib * P;
+  const typename WPack<ST>::T* pp = T.pkrow + (ptrdiff_t)ib * P;
 #pragma unroll
   for (int r = 0; r < kWG; ++r) {
     const int i = ib + r;
@@ -187,8 +226,9 @@ __device__ __forceinline__ void wave_prefetch(const WTask<ST>& T, int ib, int S,
       x[r] = 0.0f;
       c[r] = 0u;
     } else {
-      x[r] = Store<ST>::ld(px + (ptrdiff_t)r * P);
-      c[r] = __ldg(pc + (ptrdiff_t)r * P);
+      const typename WPack<ST>::T v = pp[(ptrdiff_t)r * P];
+      x[r] = WPack<ST>::x(v);
+      c[r] = WPack<ST>::c(v);
     }
   }
 }
@@ -340,6 +380,18 @@ __device__ __noinline__ void wave_lin_solve(const WGrid<ST> G, const WBufs Bf, i
   const uint32_t edge = sbase + 4u * Bf.edge;
   const uint32_t cs4 = 4u * Bf.cs;
   constexpr uint32_t kLane4 = 4u * kWRS, kWarp4 = 32u * 4u * kWRS;
+  // x0 and the codes of every cell of the grid into the block's staging,
+  // packed (warp = anti-diagonal, lane = row: coalesced)
+  using PK = typename WPack<ST>::T;
+  PK* const pk = static_cast<PK*>(G.stage);
+  for (int d = warp; d <= 2 * S - 2; d += (int)(blockDim.x >> 5)) {
+    const int j0 = max(0, d - (S - 1)), j1 = min(d, S - 1);
+    for (int j = j0 + lane; j <= j1; j += 32) {
+      const size_t k = (size_t)d * P + j;
+      pk[k] = WPack<ST>::make(G.x0[k], G.code[k]);
+    }
+  }
+  __syncthreads();
   for (int k0 = 0; k0 < K; k0 += nwmax) {
     const int nw = min(nwmax, K - k0);
     const int B = wave_strips(S, nw);
@@ -418,8 +470,7 @@ __device__ __noinline__ void wave_lin_solve(const WGrid<ST> G, const WBufs Bf, i
             T.dring = lane >= 1;
             T.sr = T.rring ? ringIn + (uint32_t)(lane - 2) * kLane4 : carryIn + (uint32_t)lane * cs4;
             T.sd = T.dring ? ringIn + (uint32_t)(lane - 1) * kLane4 : carryIn + cs4;
-            T.x0row = G.x0 + rowJ;
-            T.crow = G.code + rowJ;
+            T.pkrow = pk + rowJ;
             T.sedge = edge + (uint32_t)sw * cs4;
             T.gout = G.x + rowJ;
             const int ja = jc > 0 ? jc - 1 : 0;
