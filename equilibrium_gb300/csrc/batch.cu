@@ -53,8 +53,9 @@ struct eq_batch {
 
   int nwmax = 20;  // sweeps per wavefront pass = warps per block
   int bps = 1;     // blocks per SM
-  // the wavefront's per-block staging of packed x0 / codes (8 bytes a cell
-  // of the largest scene's diagonal layout), grown to the launch's blocks
+  // the wavefront's per-block staging of packed x0 / codes (16 bytes a cell
+  // of the largest scene's diagonal layout, 3 diagonals more), grown to the
+  // launch's blocks
   void* d_stage = nullptr;
   size_t stage_stride = 0;
   int stage_blocks = 0;
@@ -231,7 +232,7 @@ int batch_launch_shape(eq_batch* b, BLaunch* L) {
   if (L->blocks > b->stage_blocks) {  // staging for every block of the launch
     size_t stride = 256;
     for (const eqk::BScene& d : b->desc)
-      stride = std::max<size_t>(stride, (d.fstride * 8 + 255) / 256 * 256);
+      stride = std::max<size_t>(stride, ((d.fstride + 3 * (size_t)d.P) * 16 + 255) / 256 * 256);
     EQ_CUDA(cudaStreamSynchronize(b->stream));
     batch_drop_graph(b);  // the graph's kernel arguments point at the old staging
     cudaFree(b->d_stage);

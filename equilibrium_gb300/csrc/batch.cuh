@@ -46,7 +46,7 @@ struct BatchArgs {
   int nwmax;         // sweeps per wavefront pass (warps per block)
   int cs;            // carry/edge row stride (floats)
   void* stage;       // per-block staging of the wavefront's packed x0 / codes
-  unsigned long long stage_stride;  // bytes per block (>= 8 x the largest dg_size)
+  unsigned long long stage_stride;  // bytes per block (>= 16 x (dg_size + 3 P), largest scene)
 };
 
 // ---- per-cell phases over one scene, by the whole block --------------------

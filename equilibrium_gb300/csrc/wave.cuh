@@ -128,44 +128,83 @@ struct WGrid {
   int S, P;
 };
 
-// x0 and the boundary code of one cell in one word, so that a wavefront step
-// loads one value per lane instead of two (each global load of a sweep warp
-// delays the shared-memory loads issued after it): FP32 as (bits, code),
-// 16-bit formats as bits | code << 16. The raw bits are kept, so the values
-// are those of the field.
+// x0 and the boundary codes of W consecutive cells of a row (columns i ..
+// i+W-1) in one 16-byte word, so that a lane loads a group of kWG steps'
+// operands in kWG / W loads instead of 2 kWG (each global load of a sweep
+// warp delays the shared-memory loads issued after it): FP32 as two values
+// and their codes, 16-bit formats as four (bits | code << 16). The raw bits
+// are kept, so the values are those of the field; columns outside the grid
+// hold zeros.
 template <class ST>
 struct WPack;
 template <>
 struct WPack<float> {
-  using T = uint2;
-  static __device__ __forceinline__ T make(float x0, uint8_t c) {
-    return make_uint2(__float_as_uint(x0), (uint32_t)c);
+  static constexpr int W = 2;
+  // the word of cell (i, j): cells (i + w, j) at (i + w + j) P + j
+  static __device__ __forceinline__ uint4 make(const float* x0, const uint8_t* code, int i, int j,
+                                               int S, int P) {
+    uint32_t v[2], c = 0u;
+#pragma unroll
+    for (int w = 0; w < 2; ++w) {
+      const bool ok = i + w >= 0 && i + w <= S - 1;
+      const size_t q = ok ? (size_t)(i + w + j) * P + j : 0;
+      v[w] = ok ? __float_as_uint(x0[q]) : 0u;
+      c |= (ok ? (uint32_t)code[q] : 0u) << (8 * w);
+    }
+    return make_uint4(v[0], v[1], c, 0u);
   }
-  static __device__ __forceinline__ float x(T v) { return __uint_as_float(v.x); }
-  static __device__ __forceinline__ uint32_t c(T v) { return v.y; }
+  static __device__ __forceinline__ float x(const uint4& e, int w) {
+    return __uint_as_float(w == 0 ? e.x : e.y);
+  }
+  static __device__ __forceinline__ uint32_t c(const uint4& e, int w) {
+    return (e.z >> (8 * w)) & 0xffu;
+  }
+};
+template <class H>
+struct Bits16;
+template <>
+struct Bits16<__half> {
+  static __device__ __forceinline__ unsigned short get(__half v) { return __half_as_ushort(v); }
+  static __device__ __forceinline__ float widen(unsigned short b) {
+    return __half2float(__ushort_as_half(b));
+  }
 };
 template <>
-struct WPack<__half> {
-  using T = uint32_t;
-  static __device__ __forceinline__ T make(__half x0, uint8_t c) {
-    return (uint32_t)__half_as_ushort(x0) | ((uint32_t)c << 16);
+struct Bits16<__nv_bfloat16> {
+  static __device__ __forceinline__ unsigned short get(__nv_bfloat16 v) {
+    return __bfloat16_as_ushort(v);
   }
-  static __device__ __forceinline__ float x(T v) {
-    return __half2float(__ushort_as_half((unsigned short)(v & 0xffffu)));
+  static __device__ __forceinline__ float widen(unsigned short b) {
+    return __bfloat162float(__ushort_as_bfloat16(b));
   }
-  static __device__ __forceinline__ uint32_t c(T v) { return v >> 16; }
+};
+template <class H>
+struct WPack16 {
+  static constexpr int W = 4;
+  static __device__ __forceinline__ uint4 make(const H* x0, const uint8_t* code, int i, int j,
+                                               int S, int P) {
+    uint32_t v[4];
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      const bool ok = i + w >= 0 && i + w <= S - 1;
+      const size_t q = ok ? (size_t)(i + w + j) * P + j : 0;
+      v[w] = ok ? ((uint32_t)Bits16<H>::get(x0[q]) | ((uint32_t)code[q] << 16)) : 0u;
+    }
+    return make_uint4(v[0], v[1], v[2], v[3]);
+  }
+  static __device__ __forceinline__ float x(const uint4& e, int w) {
+    const uint32_t v = w == 0 ? e.x : (w == 1 ? e.y : (w == 2 ? e.z : e.w));
+    return Bits16<H>::widen((unsigned short)(v & 0xffffu));
+  }
+  static __device__ __forceinline__ uint32_t c(const uint4& e, int w) {
+    const uint32_t v = w == 0 ? e.x : (w == 1 ? e.y : (w == 2 ? e.z : e.w));
+    return v >> 16;
+  }
 };
 template <>
-struct WPack<__nv_bfloat16> {
-  using T = uint32_t;
-  static __device__ __forceinline__ T make(__nv_bfloat16 x0, uint8_t c) {
-    return (uint32_t)__bfloat16_as_ushort(x0) | ((uint32_t)c << 16);
-  }
-  static __device__ __forceinline__ float x(T v) {
-    return __bfloat162float(__ushort_as_bfloat16((unsigned short)(v & 0xffffu)));
-  }
-  static __device__ __forceinline__ uint32_t c(T v) { return v >> 16; }
-};
+struct WPack<__half> : WPack16<__half> {};
+template <>
+struct WPack<__nv_bfloat16> : WPack16<__nv_bfloat16> {};
 
 // Block-private buffers, all in the block's dynamic shared memory, given as
 // float offsets from its start: the rings [nwmax][32][kWRS] (ring[w] is
@@ -188,6 +227,8 @@ __host__ __device__ inline int wave_strips(int S, int nw) { return (S + 2 * nw -
 __host__ __device__ inline int wave_chunks(int S) { return (S + 31 + kWQ - 1) / kWQ; }
 
 constexpr int kWG = 4;  // steps per load group (x0 / codes prefetched one group ahead)
+static_assert(kWG % WPack<float>::W == 0 && kWG % WPack<__half>::W == 0,
+              "a load group holds whole packed words");
 
 struct WLaneState {
   float g1, g2, u1, rm1;
@@ -202,7 +243,7 @@ template <class ST>
 struct WTask {
   ST* gout;        // last sweep: x row j, global
   ST* gfix;           // last sweep: x row j-1 (AdjustColumn fix-up), global
-  const typename WPack<ST>::T* pkrow;  // packed x0 / codes of row j, column i at [i * P]
+  const uint4* pkrow;  // packed x0 / codes of row j: columns i .. i+W-1 at [i * P]
   uint32_t sr, sd;    // other sweeps: R / D source (ring lane, slot-indexed, or carry row)
   uint32_t sout;      // other sweeps: this lane's ring row (slot-indexed)
   uint32_t scarry;    // lanes 30/31 of a non-last sweep: carry row (0 = none)
@@ -212,23 +253,24 @@ struct WTask {
   bool valid, interior, top, bot, rowfl;
 };
 
-// x0 and codes of columns ib..ib+kWG-1 of this lane's row (EDGE: only the
-// ones inside the grid), one packed load each. Plain (coherent) loads: the
-// block wrote the staging at the solve's start.
+// x0 and codes of columns ib..ib+kWG-1 of this lane's row, kWG / W packed
+// loads (EDGE: only words that hold a column inside the grid; the others are
+// zeros). Plain (coherent) loads: the block wrote the staging at the solve's
+// start.
 template <bool EDGE, class ST>
 __device__ __forceinline__ void wave_prefetch(const WTask<ST>& T, int ib, int S, int P,
                                               float (&x)[kWG], uint32_t (&c)[kWG]) {
-  const typename WPack<ST>::T* pp = T.pkrow + (ptrdiff_t)ib * P;
+  constexpr int W = WPack<ST>::W;
+  const uint4* pp = T.pkrow + (ptrdiff_t)ib * P;
 #pragma unroll
-  for (int r = 0; r < kWG; ++r) {
+  for (int r = 0; r < kWG; r += W) {
     const int i = ib + r;
-    if (EDGE && !(i >= 0 && i <= S - 1)) {
-      x[r] = 0.0f;
-      c[r] = 0u;
-    } else {
-      const typename WPack<ST>::T v = pp[(ptrdiff_t)r * P];
-      x[r] = WPack<ST>::x(v);
-      c[r] = WPack<ST>::c(v);
+    uint4 e = make_uint4(0u, 0u, 0u, 0u);
+    if (!EDGE || (i + W - 1 >= 0 && i <= S - 1)) e = pp[(ptrdiff_t)r * P];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      x[r + w] = WPack<ST>::x(e, w);
+      c[r + w] = WPack<ST>::c(e, w);
     }
   }
 }
@@ -380,15 +422,15 @@ __device__ __noinline__ void wave_lin_solve(const WGrid<ST> G, const WBufs Bf, i
   const uint32_t edge = sbase + 4u * Bf.edge;
   const uint32_t cs4 = 4u * Bf.cs;
   constexpr uint32_t kLane4 = 4u * kWRS, kWarp4 = 32u * 4u * kWRS;
-  // x0 and the codes of every cell of the grid into the block's staging,
-  // packed (warp = anti-diagonal, lane = row: coalesced)
-  using PK = typename WPack<ST>::T;
-  PK* const pk = static_cast<PK*>(G.stage);
-  for (int d = warp; d <= 2 * S - 2; d += (int)(blockDim.x >> 5)) {
-    const int j0 = max(0, d - (S - 1)), j1 = min(d, S - 1);
+  // x0 and the codes of every row into the block's staging, packed: the word
+  // of cell (i, j), i = -(W-1) .. S-1, at (i + W - 1 + j) P + j (the diagonal
+  // layout shifted by W - 1 columns; warp = anti-diagonal, lane = row)
+  constexpr int W = WPack<ST>::W;
+  uint4* const pk = static_cast<uint4*>(G.stage);
+  for (int d = warp; d <= 2 * S - 2 + (W - 1); d += (int)(blockDim.x >> 5)) {
+    const int j0 = max(0, d - (S - 1) - (W - 1)), j1 = min(d, S - 1);
     for (int j = j0 + lane; j <= j1; j += 32) {
-      const size_t k = (size_t)d * P + j;
-      pk[k] = WPack<ST>::make(G.x0[k], G.code[k]);
+      pk[(size_t)d * P + j] = WPack<ST>::make(G.x0, G.code, d - (W - 1) - j, j, S, P);
     }
   }
   __syncthreads();
@@ -470,7 +512,7 @@ __device__ __noinline__ void wave_lin_solve(const WGrid<ST> G, const WBufs Bf, i
             T.dring = lane >= 1;
             T.sr = T.rring ? ringIn + (uint32_t)(lane - 2) * kLane4 : carryIn + (uint32_t)lane * cs4;
             T.sd = T.dring ? ringIn + (uint32_t)(lane - 1) * kLane4 : carryIn + cs4;
-            T.pkrow = pk + rowJ;
+            T.pkrow = pk + (size_t)(W - 1) * P + rowJ;
             T.sedge = edge + (uint32_t)sw * cs4;
             T.gout = G.x + rowJ;
             const int ja = jc > 0 ? jc - 1 : 0;
