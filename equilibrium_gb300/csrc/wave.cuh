@@ -129,8 +129,8 @@ struct WGrid {
 };
 
 // x0 and the boundary codes of W consecutive cells of a row (columns i ..
-// i+W-1) in one 16-byte word, so that a lane loads a group of kWG steps'
-// operands in kWG / W loads instead of 2 kWG (each global load of a sweep
+// i+W-1) in one 16-byte word, so that a lane loads a group of W steps'
+// operands in one load instead of 2 W (each global load of a sweep
 // warp delays the shared-memory loads issued after it): FP32 as two values
 // and their codes, 16-bit formats as four (bits | code << 16). The raw bits
 // are kept, so the values are those of the field; columns outside the grid
@@ -226,9 +226,13 @@ __host__ __device__ inline size_t wave_smem_floats(int nwmax, int cs) {
 __host__ __device__ inline int wave_strips(int S, int nw) { return (S + 2 * nw - 1) / 32 + 1; }
 __host__ __device__ inline int wave_chunks(int S) { return (S + 31 + kWQ - 1) / kWQ; }
 
-constexpr int kWG = 4;  // steps per load group (x0 / codes prefetched one group ahead)
-static_assert(kWG % WPack<float>::W == 0 && kWG % WPack<__half>::W == 0,
-              "a load group holds whole packed words");
+// Steps per load group (x0 / codes prefetched one group ahead): one packed
+// word. Two-step groups for FP32 keep fewer values live than two words of a
+// four-step group (fewer spills under the 80-register cap; 3 % faster).
+template <class ST>
+__host__ __device__ constexpr int wave_group() { return WPack<ST>::W; }
+static_assert(kWQ % WPack<float>::W == 0 && kWQ % WPack<__half>::W == 0,
+              "a chunk holds whole load groups");
 
 struct WLaneState {
   float g1, g2, u1, rm1;
@@ -253,25 +257,20 @@ struct WTask {
   bool valid, interior, top, bot, rowfl;
 };
 
-// x0 and codes of columns ib..ib+kWG-1 of this lane's row, kWG / W packed
-// loads (EDGE: only words that hold a column inside the grid; the others are
-// zeros). Plain (coherent) loads: the block wrote the staging at the solve's
-// start.
+// x0 and codes of columns ib..ib+W-1 of this lane's row, one packed load
+// (EDGE: only when the word holds a column inside the grid; else zeros).
+// Plain (coherent) loads: the block wrote the staging at the solve's start.
 template <bool EDGE, class ST>
 __device__ __forceinline__ void wave_prefetch(const WTask<ST>& T, int ib, int S, int P,
-                                              float (&x)[kWG], uint32_t (&c)[kWG]) {
+                                              float (&x)[wave_group<ST>()],
+                                              uint32_t (&c)[wave_group<ST>()]) {
   constexpr int W = WPack<ST>::W;
-  const uint4* pp = T.pkrow + (ptrdiff_t)ib * P;
+  uint4 e = make_uint4(0u, 0u, 0u, 0u);
+  if (!EDGE || (ib + W - 1 >= 0 && ib <= S - 1)) e = T.pkrow[(ptrdiff_t)ib * P];
 #pragma unroll
-  for (int r = 0; r < kWG; r += W) {
-    const int i = ib + r;
-    uint4 e = make_uint4(0u, 0u, 0u, 0u);
-    if (!EDGE || (i + W - 1 >= 0 && i <= S - 1)) e = pp[(ptrdiff_t)r * P];
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      x[r + w] = WPack<ST>::x(e, w);
-      c[r + w] = WPack<ST>::c(e, w);
-    }
+  for (int w = 0; w < W; ++w) {
+    x[w] = WPack<ST>::x(e, w);
+    c[w] = WPack<ST>::c(e, w);
   }
 }
 
@@ -287,6 +286,7 @@ __device__ __forceinline__ void wave_chunk(const WTask<ST>& T, WLaneState& st, i
   const uint32_t sD = T.sd + 4u * (uint32_t)(T.dring ? half : ib);
   ST* gO = LAST ? T.gout + (ptrdiff_t)(ib - 1) * P : nullptr;
   const uint32_t sO = T.sout + 4u * (uint32_t)half;
+  constexpr int kWG = wave_group<ST>();
   float xa[kWG];
   uint32_t ca[kWG];
   wave_prefetch<EDGE>(T, ib, S, P, xa, ca);
