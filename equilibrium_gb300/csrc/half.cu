@@ -195,9 +195,11 @@ int h_project(eq_hfluid* h, int which, T* vx, T* vy, T* ps, T* divs) {
                                                        static_cast<T*>(L0.r), L0.pitch);
     EQ_CUDA(cudaMemsetAsync(L0.e, 0, (size_t)L0.pitch * L0.n * sizeof(float), st));
     h_vcycle<T>(h, 0);
+    float sh, sl;
+    eqk::df_split(scale, &sh, &sl);
     eqk::k_ir_update<<<h_grid(N, N), kHBlk, 0, st>>>(h->p32, h->plo, S, P,
                                                      static_cast<const float*>(L0.e), L0.pitch,
-                                                     scale);
+                                                     sh, sl);
     if ((rc = check_launch(pl))) return rc;
   }
   h->stats.ir_iterations[which] = it;

@@ -153,11 +153,12 @@ __global__ void k_h_div_norm(const T* __restrict__ vx, const T* __restrict__ vy,
        k += (size_t)gridDim.x * blockDim.x) {
     const int j = (int)(k / N) + 1, i = (int)(k % N) + 1;
     const size_t q = (size_t)j * P + i;
+    // (-0.5 (dvx + dvy) / S)^2 with the constant factor applied per block
     const double d =
-        -0.5 * (((double)hl(vx, q + 1) - hl(vx, q - 1)) + ((double)hl(vy, q + P) - hl(vy, q - P))) /
-        (double)S;
-    acc += d * d;
+        ((double)hl(vx, q + 1) - hl(vx, q - 1)) + ((double)hl(vy, q + P) - hl(vy, q - P));
+    acc = __fma_rn(d, d, acc);
   }
+  acc *= 0.25 / ((double)S * S);
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   __shared__ double part[32];
   if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;

@@ -244,20 +244,45 @@ __device__ __forceinline__ void block_add_f64x2(double a, double b, double* out)
 }
 
 // The refinement's pressure is a pair of FP32 grids, p = ph + pl (pl the
-// low-order part), read and updated in FP64: the residual of an FP32 pressure
-// has a floor near eps32 ||A|| ||p||, above a 1e-5 relative target on large
-// grids; the pair's floor is near eps64's.
-__device__ __forceinline__ double ir_p(const float* ph, const float* pl, size_t q) {
-  return (double)ph[q] + (double)pl[q];
+// low-order part): the residual of an FP32 pressure has a floor near
+// eps32 ||A|| ||p||, above a 1e-5 relative target on large grids. The pair is
+// read and updated in double-float arithmetic, FP32 operations only: Knuth's
+// two-sum, Dekker's fast two-sum and the FMA's exact product, about 48
+// significant bits (an error relative to the operands, not to the
+// cancelling result, near 2^-47). FP64 appears only in the reductions.
+struct DF {
+  float h, l;
+};
+__device__ __forceinline__ DF df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float v = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v))};
 }
-__device__ __forceinline__ void ir_set(float* ph, float* pl, size_t q, double v) {
-  const float hi = (float)v;
-  ph[q] = hi;
-  pl[q] = (float)(v - (double)hi);
+__device__ __forceinline__ DF df_fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  const DF s = df_two_sum(a.h, b.h);
+  return df_fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ DF df_neg(DF a) { return {-a.h, -a.l}; }
+// (s.h + s.l) * e for an FP32 e
+__device__ __forceinline__ DF df_mul_f(DF s, float e) {
+  const float p = __fmul_rn(s.h, e);
+  return df_fast_two_sum(p, __fmaf_rn(s.l, e, __fmaf_rn(s.h, e, -p)));
+}
+__device__ __forceinline__ DF ir_p(const float* ph, const float* pl, size_t q) {
+  return {ph[q], pl[q]};
+}
+// a double's nearest double-float (the host splits the refinement's scale)
+__host__ __device__ inline void df_split(double v, float* h, float* l) {
+  *h = (float)v;
+  *l = (float)(v - (double)*h);
 }
 
-// r = b - A p on the interior (FP64 arithmetic, stored FP32), with FP64 sums
-// of r and r^2.
+// r = b - A p on the interior (double-float arithmetic, stored FP32), with
+// FP64 sums of r and r^2.
 __global__ void k_ir_residual(const float* __restrict__ ph, const float* __restrict__ pl,
                               const float* __restrict__ b, int S, int P,
                               const uint8_t* __restrict__ rowfl,
@@ -270,15 +295,18 @@ __global__ void k_ir_residual(const float* __restrict__ ph, const float* __restr
        k += (size_t)gridDim.x * blockDim.x) {
     const int j = (int)(k / N) + 1, i = (int)(k % N) + 1;
     const size_t q = (size_t)j * P + i;
-    const double c = ir_p(ph, pl, q);
-    const double L = (i == 1) ? (rowfl[j] ? c : ir_p(ph, pl, q - 1)) : ir_p(ph, pl, q - 1);
-    const double R = (i == N) ? (rowfl[j] ? c : ir_p(ph, pl, q + 1)) : ir_p(ph, pl, q + 1);
-    const double U = (j == 1) ? (colfl[i] ? c : ir_p(ph, pl, q - P)) : ir_p(ph, pl, q - P);
-    const double D = (j == N) ? (colfl[i] ? c : ir_p(ph, pl, q + P)) : ir_p(ph, pl, q + P);
-    const double res = (double)b[q] - (4.0 * c - (((L + R) + U) + D));
-    r[q] = (float)res;
-    s1 += res;
-    s2 += res * res;
+    const DF c = ir_p(ph, pl, q);
+    const DF L = (i == 1) ? (rowfl[j] ? c : ir_p(ph, pl, q - 1)) : ir_p(ph, pl, q - 1);
+    const DF R = (i == N) ? (rowfl[j] ? c : ir_p(ph, pl, q + 1)) : ir_p(ph, pl, q + 1);
+    const DF U = (j == 1) ? (colfl[i] ? c : ir_p(ph, pl, q - P)) : ir_p(ph, pl, q - P);
+    const DF D = (j == N) ? (colfl[i] ? c : ir_p(ph, pl, q + P)) : ir_p(ph, pl, q + P);
+    const DF c4 = {__fmul_rn(4.0f, c.h), __fmul_rn(4.0f, c.l)};  // exact
+    const DF Ap = df_add(c4, df_neg(df_add(df_add(df_add(L, R), U), D)));
+    const DF res = df_add({b[q], 0.0f}, df_neg(Ap));
+    const float rf = __fadd_rn(res.h, res.l);
+    r[q] = rf;
+    s1 += (double)rf;
+    s2 = __fma_rn((double)rf, (double)rf, s2);
   }
   block_add_f64x2(s1, s2, acc);
 }
@@ -294,29 +322,31 @@ __global__ void k_ir_scale(const float* __restrict__ r, int S, int P, float mean
   hs(r0, (size_t)J * pitch0 + I, (r[(size_t)(J + 1) * P + I + 1] - mean) * inv_scale);
 }
 
-// p += scale * e0 on the interior (FP64, split back into the pair).
+// p += scale * e0 on the interior (double-float; scale = sh + sl).
 __global__ void k_ir_update(float* __restrict__ ph, float* __restrict__ pl, int S, int P,
-                            const float* __restrict__ e0, int pitch0, double scale) {
+                            const float* __restrict__ e0, int pitch0, float sh, float sl) {
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
   const int N = S - 2;
   if (I >= N || J >= N) return;
   const size_t q = (size_t)(J + 1) * P + I + 1;
-  ir_set(ph, pl, q, ir_p(ph, pl, q) + scale * (double)e0[(size_t)J * pitch0 + I]);
+  const DF v = df_add(ir_p(ph, pl, q), df_mul_f({sh, sl}, e0[(size_t)J * pitch0 + I]));
+  ph[q] = v.h;
+  pl[q] = v.l;
 }
 
 // Sum of p over the interior (FP64) into acc[0].
 __global__ void k_ir_sum(const float* __restrict__ ph, const float* __restrict__ pl, int S, int P,
                          double* __restrict__ acc) {
   const int N = S - 2;
-  double s1 = 0.0;
+  DF s = {0.0f, 0.0f};
   const size_t n = (size_t)N * N;
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
        k += (size_t)gridDim.x * blockDim.x) {
     const int j = (int)(k / N) + 1, i = (int)(k % N) + 1;
-    s1 += ir_p(ph, pl, (size_t)j * P + i);
+    s = df_add(s, ir_p(ph, pl, (size_t)j * P + i));
   }
-  block_add_f64x2(s1, 0.0, acc);
+  block_add_f64x2((double)s.h + (double)s.l, 0.0, acc);
 }
 
 // p -= mean(p) on the interior: the pure-Neumann solution's free constant is
@@ -326,9 +356,18 @@ __global__ void k_ir_center(float* __restrict__ ph, float* __restrict__ pl, int 
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int N = S - 2;
+  __shared__ DF s_mean;  // the mean, once per block
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    DF m;
+    df_split(acc[0] / ((double)N * N), &m.h, &m.l);
+    s_mean = m;
+  }
+  __syncthreads();
   if (i > N || j > N) return;
   const size_t q = (size_t)j * P + i;
-  ir_set(ph, pl, q, ir_p(ph, pl, q) - acc[0] / ((double)N * N));
+  const DF v = df_add(ir_p(ph, pl, q), df_neg(s_mean));
+  ph[q] = v.h;
+  pl[q] = v.l;
 }
 
 // p = 0 on the interior (project's `p[idx] = 0.0`, fluid.rs:349).
