@@ -108,6 +108,7 @@ def load(path: str = LIB_PATH):
         "eq_fluid_write_field": (i32, [H, i32, P, u64]),
         "eq_fluid_read_field_async": (i32, [H, i32, P, u64]),
         "eq_fluid_read_fields": (i32, [H, i32, P, P, u64]),
+        "eq_fluid_read_fields_async": (i32, [H, i32, P, P, u64]),
         "eq_fluid_write_field_async": (i32, [H, i32, P, u64]),
         "eq_fluid_read_cells": (i32, [H, P, u64]),
         "eq_fluid_write_cells": (i32, [H, P, u64]),

@@ -95,6 +95,13 @@ struct eq_fluid {
   // dense staging of eq_fluid_read_fields (grown on demand)
   float* d_pack = nullptr;
   size_t d_pack_cap = 0;  // floats
+  // eq_fluid_read_fields_async: two staging buffers used in turn, copied to
+  // the host on their own stream while the next step runs
+  float* d_apack[2] = {};
+  size_t d_apack_cap = 0;  // floats, each
+  int apack_next = 0;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t apack_ev[2] = {}, acopy_ev[2] = {};
 
   // source staging
   uint8_t* d_src = nullptr;
@@ -842,6 +849,12 @@ void free_handle(eq_fluid* h) {
   }
   cudaFree(h->err);
   cudaFree(h->d_pack);
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(h->d_apack[k]);
+    if (h->apack_ev[k]) cudaEventDestroy(h->apack_ev[k]);
+    if (h->acopy_ev[k]) cudaEventDestroy(h->acopy_ev[k]);
+  }
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   cudaFree(h->d_src);
   if (h->h_src) cudaFreeHost(h->h_src);
   if (h->src_ev) cudaEventDestroy(h->src_ev);
@@ -1161,6 +1174,7 @@ int eq_fluid_synchronize(eq_fluid* h) {
   EQ_CUDA(cudaStreamSynchronize(h->stream));
   for (int k = 0; k < 2; ++k)  // joined into the main stream by every step; an
     EQ_CUDA(cudaStreamSynchronize(h->side[k]));  // aborted step may have left work
+  if (h->copy_stream) EQ_CUDA(cudaStreamSynchronize(h->copy_stream));  // async read-backs
   return read_err_word(h);
 }
 
@@ -1315,6 +1329,59 @@ int eq_fluid_read_fields(eq_fluid* h, int count, const int* fields, float* const
                             cudaMemcpyDeviceToHost, h->stream));
   return read_err_word(h);  // synchronises the stream
 }
+int eq_fluid_read_fields_async(eq_fluid* h, int count, const int* fields, float* const* host,
+                               uint64_t n) {
+  if (!h || !fields || !host) return fail(EQ_ERR_ARG, "null argument");
+  if (count < 1 || count > 6) return fail(EQ_ERR_ARG, "count must be 1..6");
+  const size_t g = (size_t)h->S * h->S;
+  if (n != g) return fail(EQ_ERR_ARG, "element count must be size*size");
+  int rc;
+  for (int k = 0; k < count; ++k) {
+    if ((rc = check_field(fields[k]))) return rc;
+    if (!host[k]) return fail(EQ_ERR_ARG, "null host buffer");
+  }
+  if ((rc = select_device(h))) return rc;
+  if (!h->copy_stream) {
+    if (cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(EQ_ERR_CUDA, "cudaStreamCreate (read-back)");
+    for (int k = 0; k < 2; ++k)
+      if (cudaEventCreateWithFlags(&h->apack_ev[k], cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&h->acopy_ev[k], cudaEventDisableTiming) != cudaSuccess)
+        return fail(EQ_ERR_CUDA, "cudaEventCreate (read-back)");
+  }
+  if (h->d_apack_cap < (size_t)count * g) {
+    EQ_CUDA(cudaStreamSynchronize(h->stream));
+    EQ_CUDA(cudaStreamSynchronize(h->copy_stream));
+    for (int k = 0; k < 2; ++k) {
+      cudaFree(h->d_apack[k]);
+      h->d_apack[k] = nullptr;
+    }
+    h->d_apack_cap = 0;
+    for (int k = 0; k < 2; ++k)
+      if (cudaMalloc(&h->d_apack[k], (size_t)count * g * sizeof(float)) != cudaSuccess)
+        return fail(EQ_ERR_OOM, "cudaMalloc (read-back staging)");
+    h->d_apack_cap = (size_t)count * g;
+    for (int k = 0; k < 2; ++k) EQ_CUDA(cudaEventRecord(h->acopy_ev[k], h->copy_stream));
+  }
+  const int slot = h->apack_next;
+  h->apack_next ^= 1;
+  // the packing reuses this buffer only after its previous copy is done
+  EQ_CUDA(cudaStreamWaitEvent(h->stream, h->acopy_ev[slot], 0));
+  eqk::PackFields pf;
+  pf.count = count;
+  for (int k = 0; k < count; ++k) pf.src[k] = h->field[fields[k]];
+  const int blocks = (int)std::min<size_t>((g * count + 255) / 256, 152 * 8);
+  eqk::k_pack_fields<<<blocks, 256, 0, h->stream>>>(pf, h->d_apack[slot], (int)h->S, h->P);
+  if ((rc = check_launch(h))) return rc;
+  EQ_CUDA(cudaEventRecord(h->apack_ev[slot], h->stream));
+  EQ_CUDA(cudaStreamWaitEvent(h->copy_stream, h->apack_ev[slot], 0));
+  for (int k = 0; k < count; ++k)
+    EQ_CUDA(cudaMemcpyAsync(host[k], h->d_apack[slot] + (size_t)k * g, g * sizeof(float),
+                            cudaMemcpyDeviceToHost, h->copy_stream));
+  EQ_CUDA(cudaEventRecord(h->acopy_ev[slot], h->copy_stream));
+  return EQ_OK;
+}
+
 int eq_fluid_write_field_async(eq_fluid* h, int field, const float* host, uint64_t n) {
   return field_copy(h, field, const_cast<float*>(host), n, false, false);
 }

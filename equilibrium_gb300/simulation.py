@@ -251,6 +251,20 @@ class Fluid:
                                            ctypes.cast(ptrs, ctypes.c_void_p), self._n()))
         return outs
 
+    def read_fields_async(self, field_indices, outs) -> list:
+        """read_fields without waiting: the copies run on a read-back stream of
+        their own while later steps compute, and are complete at the next
+        synchronize(). `outs` (pinned host arrays or tensors) must stay alive
+        until then."""
+        import ctypes
+        k = len(field_indices)
+        fi = (ctypes.c_int * k)(*field_indices)
+        ptrs = (ctypes.c_void_p * k)(*[o.ctypes.data if isinstance(o, np.ndarray)
+                                       else o.data_ptr() for o in outs])
+        check(self._L.eq_fluid_read_fields_async(self._h, k, ctypes.cast(fi, ctypes.c_void_p),
+                                                 ctypes.cast(ptrs, ctypes.c_void_p), self._n()))
+        return outs
+
     def write_field(self, field_index: int, values):
         a = _as_f32(values, self._n())
         check(self._L.eq_fluid_write_field(self._h, field_index, a.ctypes.data, a.size))

@@ -180,6 +180,16 @@ int eq_fluid_write_field_async(eq_fluid* h, int field, const float* host, uint64
 int eq_fluid_read_fields(eq_fluid* h, int count, const int* fields, float* const* host,
                          uint64_t n);
 
+/* The same without waiting: the fields are packed on the handle's stream
+ * (the next step's kernels may follow at once) and copied to host[k] on a
+ * read-back stream of their own, so a frame loop's read-back of frame n
+ * overlaps the computation of frame n+1 (two staging buffers, used in turn).
+ * host[k] must stay valid, and should be pinned, until the copy is complete:
+ * at the next eq_fluid_synchronize, which waits for every read-back (and
+ * reports a device error of the steps before). */
+int eq_fluid_read_fields_async(eq_fluid* h, int count, const int* fields, float* const* host,
+                               uint64_t n);
+
 /* cells_type (fluid.rs:80) as bytes, 1 = DefaultWall. A written mask must keep
  * the whole ghost frame as DefaultWall (init_walls, fluid.rs:552-570, makes it
  * so and nothing in the reference clears it); otherwise EQ_ERR_ARG. */

@@ -119,3 +119,45 @@ def test_read_fields_matches_read_field(eqlib):
     with pytest.raises(_lib.EqError):
         f.read_fields((1, 7))
     f.close()
+
+
+@pytest.mark.gpu
+def test_read_fields_async_overlaps_later_steps(eqlib):
+    """eq_fluid_read_fields_async after each of four steps, into two pinned
+    buffer sets used in turn (the read-back of frame n in flight while frame
+    n+1 computes), gives every frame's fields bit for bit as a synchronous
+    read after the same frames; growing the field count reallocates the
+    staging; bad arguments are refused."""
+    import torch
+    size = 133
+    cfg = (FluidConfigs(1e-4, 1e-4, False), SimulationConfigs(0.1, 5, size))
+    rng = np.random.default_rng(5)
+    init = [rng.uniform(-1, 1, size * size).astype(np.float32) for _ in range(6)]
+    ref, f = Fluid(*cfg), Fluid(*cfg)
+    for g in (ref, f):
+        for k in range(6):
+            g.write_field(k, init[k])
+    sel = (1, 2, 3)
+    want = []
+    for _ in range(4):
+        ref.step()
+        want.append(ref.read_fields(sel))
+    bufs = [[torch.empty(size * size, dtype=torch.float32).pin_memory() for _ in sel]
+            for _ in range(4)]
+    for fr in range(4):
+        f.step()
+        f.read_fields_async(sel, bufs[fr])
+    f.synchronize()
+    for fr in range(4):
+        for w, t in zip(want[fr], bufs[fr]):
+            np.testing.assert_array_equal(t.numpy().view(np.uint32), w.view(np.uint32))
+    six = [torch.empty(size * size, dtype=torch.float32).pin_memory() for _ in range(6)]
+    f.read_fields_async(tuple(range(6)), six)
+    f.synchronize()
+    now = f.read_fields(tuple(range(6)))
+    for w, t in zip(now, six):
+        np.testing.assert_array_equal(t.numpy().view(np.uint32), w.view(np.uint32))
+    with pytest.raises(_lib.EqError):
+        f.read_fields_async((1, 7), six[:2])
+    ref.close()
+    f.close()
