@@ -373,6 +373,19 @@ static_assert(12 * kSwMaxKG <= 128, "the halo import warp holds 4 words a lane p
 // (it reads the initial x or the group import ring) and the last (it writes
 // x in the last group), take warps 0 and 1.
 __device__ __forceinline__ int sw_role(int w, int KG, int nk) {
+  if (KG == 5) {
+    // warps w, w + 4, w + 8 share a sub-partition: {0, 4, 8} first sweep,
+    // group export, copy; {1, 5} two middle sweeps alone; {2, 6} a sweep and
+    // the halo import; {3, 7} the last sweep and the group import
+    if (w == 4) return KG + 3;
+    if (w == 8) return KG;
+    if (w == 6) return KG + 2;
+    if (w == 7) return KG + 1;
+    const int slot = w == 0 ? 0 : (w == 3 ? 1 : (w == 2 ? 2 : (w == 1 ? 3 : 4)));
+    if (slot == 0 || nk < 2) return slot;
+    if (slot == 1) return nk - 1;
+    return slot <= nk - 1 ? slot - 1 : slot;
+  }
   const int h = KG < 4 ? KG : 4;
   // helpers in warp order: group export (light, beside the first sweep and
   // the sweep of slot 4), group import, halo import, copy
