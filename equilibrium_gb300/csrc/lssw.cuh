@@ -368,10 +368,12 @@ static_assert(12 * kSwMaxKG <= 128, "the halo import warp holds 4 words a lane p
 
 // The role of warp w of a block with KG sweep warps (nk of them real): sweep
 // kk < KG, or KG (copy), KG + 1 (group import), KG + 2 (halo import), KG + 3
-// (group export). Warp w issues from SM sub-partition w % 4, so the helpers
-// take warps h .. h+3 (h = min(4, KG)) and the two heaviest sweeps, the first
-// (it reads the initial x or the group import ring) and the last (it writes
-// x in the last group), take warps 0 and 1.
+// (group export). Warps w, w + 4, w + 8 issue from the same SM sub-partition.
+// With 5 sweeps (the usual block) the two sweeps that must share one get it
+// to themselves; otherwise the helpers take warps h .. h+3 (h = min(4, KG))
+// and the two heaviest sweeps, the first (it reads the initial x or the
+// group import ring) and the last (it writes x in the last group), take
+// warps 0 and 1.
 __device__ __forceinline__ int sw_role(int w, int KG, int nk) {
   if (KG == 5) {
     // warps w, w + 4, w + 8 share a sub-partition: {0, 4, 8} first sweep,
