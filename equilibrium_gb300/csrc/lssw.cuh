@@ -84,7 +84,7 @@ constexpr int kSwPCS = kSwPC + 4;  // x0 ring row (floats)
 constexpr int kSwCCS = kSwPC + 4;  // code ring row (bytes)
 constexpr int kSwPXS = kSwPX + 4;  // initial-x ring row (floats)
 constexpr int kSwAH = 5;      // a chunk copy is issued kSwAH periods before its use
-constexpr int kSwAHI = 2;     // an import load is checked kSwAHI periods after its issue
+constexpr int kSwAHI = 1;     // an import load is checked kSwAHI periods after its issue
 constexpr int kSwMaxK = 20;   // sweeps per launch
 constexpr int kSwMaxKG = 10;  // sweeps per block (its warps' registers hold a period's operands)
 constexpr int kSwGrpWords = 36;  // words per group-export record (34 used)
