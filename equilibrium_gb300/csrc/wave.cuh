@@ -124,7 +124,7 @@ struct WGrid {
   const uint8_t* code;   // boundary codes, diagonal layout
   const uint8_t* rowfl;  // [S]
   const uint8_t* colfl;  // [S]
-  void* stage;           // the block's staging (dg_size(S, P) packed words), see WPack
+  void* stage;           // the block's staging: (2 S + 2) P 16-byte packed words, see WPack
   int S, P;
 };
 
