@@ -25,6 +25,7 @@ class Cfg:
     PX = 32   # columns of the initial-x ring
     CH = 4    # columns per chunk copy
     AH = 5    # a row's chunk is issued AH periods before its first use period
+    EDGE_RIGHT_FRAME = True  # the edge step sets an interior row's column S-1
 
 
 def derive_codes(cells, S):
@@ -319,7 +320,8 @@ def run(mode, x, x0, cells, S, P, K, a, c, G=1, cfg=Cfg):
                         if edge_step:
                             vL = np.where(pasr & (k > 0), R, np.where(interior, xin[jj, 0], F(0)))
                             xR = np.where(interior, xin[jj, S - 1], F(0))
-                            ve = np.where(i == 0, vL, np.where(i == S - 1, xR, gs))
+                            ve = np.where(i == 0, vL, np.where(i == S - 1, xR, gs)
+                                          if cfg.EDGE_RIGHT_FRAME else gs)
                         else:
                             ve = gs.copy()
                         fl = top | bot

@@ -58,3 +58,18 @@ def test_strip_model_catches_a_small_ring():
     x = rng.uniform(-1, 1, S * S).astype(np.float32)
     with pytest.raises(AssertionError, match="XR"):
         M.run(M.ROW, x, x.copy(), cells.reshape(-1), S, 96, K, 0.5, 3.0, G=1, cfg=Narrow)
+
+
+def test_strip_model_catches_a_missing_frame_column():
+    """The relaxed edge step must still give every value a later read needs:
+    without its right frame column rule (column S-1 of an interior row left
+    to the arithmetic) the model's needed-value check fails."""
+    class NoRight(M.Cfg):
+        EDGE_RIGHT_FRAME = False
+    rng = np.random.default_rng(1)
+    S, K = 40, 3
+    cells = np.zeros((S, S), np.uint8)
+    cells[0, :] = cells[-1, :] = cells[:, 0] = cells[:, -1] = 1
+    x = rng.uniform(-1, 1, S * S).astype(np.float32)
+    with pytest.raises(AssertionError):
+        M.run(M.ROW, x, x.copy(), cells.reshape(-1), S, 64, K, 0.5, 3.0, G=1, cfg=NoRight)
