@@ -53,8 +53,10 @@ struct BatchArgs {
 // Cells are visited by anti-diagonals (warp = diagonal, lane = row j), so the
 // 32 lanes of a warp touch consecutive addresses. Each lane takes up to kU
 // cells of its diagonal per pass and issues all their loads before using
-// them (the phases are latency-bound otherwise: one block per scene).
-constexpr int kU = 4;
+// them (the phases are latency-bound otherwise: one block per scene). Two
+// cells a lane keep fewer values live than four (the kernel's 80-register
+// cap is shared with the wavefront): 1.3 % faster frames, 8 slower.
+constexpr int kU = 2;
 
 // Calls fn(r, i, j, q, ok) for r < kU cells of one diagonal pass; `ok` marks
 // the cells that exist. The callers split their work into load and use
